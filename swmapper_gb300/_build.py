@@ -1,0 +1,132 @@
+"""Build recipes for the in-tree native libraries.
+
+Everything is compiled in place (no pip install): the CUDA library for sm_103a
+with nvcc, the C host pieces with gcc. `build_all()` is what
+`__graft_entry__.build()` runs, here and on the GPU host.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+ORACLE = os.path.join(ROOT, "oracle")
+
+LIB_CUDA = os.path.join(PKG, "libswmapper_gb300.so")
+LIB_SYNTH = os.path.join(PKG, "libswm_synth.so")
+BIN_INDEX = os.path.join(PKG, "swm_index")
+BIN_MAP = os.path.join(PKG, "swm_mapper")
+LIB_ORACLE = os.path.join(ORACLE, "_build", "libswm_oracle.so")
+REF_DIR = os.path.join(ORACLE, "_ref")
+LIB_SWREF = os.path.join(REF_DIR, "libswref.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CUDA_SOURCES = ["swm_index.cu", "swm_map.cu"]
+HOST_SOURCES = ["swm_files.c"]
+
+
+def _run(cmd: list[str], cwd: str | None = None) -> None:
+    proc = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        sys.stderr.write(proc.stdout + proc.stderr)
+        raise RuntimeError("build step failed: " + " ".join(cmd))
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _newer(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(d) <= t for d in deps)
+
+
+def build_synth() -> str:
+    src = os.path.join(CSRC, "synth.c")
+    deps = [src, os.path.join(INCLUDE, "swm_synth.h")]
+    if not _newer(LIB_SYNTH, deps):
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-I", INCLUDE, src, "-o", LIB_SYNTH])
+    return LIB_SYNTH
+
+
+def build_oracle() -> str:
+    src = os.path.join(ORACLE, "swm_oracle.c")
+    deps = [src, os.path.join(ORACLE, "swm_oracle.h")]
+    os.makedirs(os.path.dirname(LIB_ORACLE), exist_ok=True)
+    if not _newer(LIB_ORACLE, deps):
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-pthread", src, "-o", LIB_ORACLE])
+    return LIB_ORACLE
+
+
+def build_ref() -> str | None:
+    """Compile the reference's own source into oracle/_ref (test infrastructure).
+
+    Works where the reference tree is present, or where oracle/_ref/src was
+    produced earlier; returns None when neither is available.
+    """
+    have_src = os.path.exists(os.path.join(REF_DIR, "src", "mapper_ref.c"))
+    have_tree = os.path.exists(os.path.join(os.environ.get("REF_DIR", "/root/reference"), "mapper_cpe.c"))
+    if not (have_src or have_tree):
+        return None
+    proc = subprocess.run(["bash", os.path.join(ORACLE, "build_ref.sh")], capture_output=True, text=True)
+    if proc.returncode != 0:
+        sys.stderr.write(proc.stdout + proc.stderr)
+        return None
+    return LIB_SWREF
+
+
+def build_cuda() -> str:
+    nvcc = _nvcc()
+    objdir = os.path.join(PKG, "_build")
+    os.makedirs(objdir, exist_ok=True)
+    headers = [os.path.join(INCLUDE, "swmapper.h"), os.path.join(CSRC, "swm_common.cuh")]
+    objs = []
+    jobs = []
+    for s in CUDA_SOURCES:
+        src = os.path.join(CSRC, s)
+        obj = os.path.join(objdir, s + ".o")
+        objs.append(obj)
+        if not _newer(obj, [src] + headers):
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj])
+    for s in HOST_SOURCES:
+        src = os.path.join(CSRC, s)
+        obj = os.path.join(objdir, s + ".o")
+        objs.append(obj)
+        if not _newer(obj, [src] + headers):
+            jobs.append(["gcc", "-O2", "-fPIC", "-std=gnu11", "-I", INCLUDE, "-c", src, "-o", obj])
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(_run, jobs))
+    if not _newer(LIB_CUDA, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", LIB_CUDA, *objs, "-lcudart", "-lpthread"])
+    return LIB_CUDA
+
+
+def build_cli() -> None:
+    for name, out in (("cli_index.c", BIN_INDEX), ("cli_mapper.c", BIN_MAP)):
+        src = os.path.join(CSRC, name)
+        if not os.path.exists(src):
+            continue
+        if not _newer(out, [src, LIB_CUDA, os.path.join(INCLUDE, "swmapper.h")]):
+            _run(["gcc", "-O2", "-std=gnu11", "-I", INCLUDE, src, "-o", out,
+                  "-L", PKG, "-lswmapper_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread"])
+
+
+def build_all(with_ref: bool = True) -> None:
+    build_synth()
+    build_oracle()
+    if with_ref:
+        build_ref()
+    build_cuda()
+    build_cli()
