@@ -1,0 +1,183 @@
+/*
+ * swmapper.h -- C ABI of the GB300 short-read mapper hot path
+ * (libswmapper_gb300.so).
+ *
+ * Drop-in boundary for SWMapper's index build and mapping kernel:
+ *   index build   serial_index.c main (818-865) and construct_hash_index
+ *                 (359-445): the same seven files under the same prefix.
+ *   index load    mapper_mpe.c load_ref_info (198-314).
+ *   mapping       athread_spawn(find_positions, &ref_info_h) / athread_join
+ *                 (mapper_mpe.c:972,1056; mapper_cpe.c:2592-2663) with the
+ *                 in/out fields of ref_info_t (fm_define.h:22-55).
+ * Plain pointers and sizes only; every call returns an int status (0 = OK,
+ * < 0 = one of the SWM_ERR_* codes) where the reference returns void.
+ */
+#ifndef SWMAPPER_H
+#define SWMAPPER_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Output layout of the reference (fm_define.h:17-19; mapper_cpe.c:1468,1481). */
+#define SWM_MAX_CIGAR 256
+#define SWM_RECORD_WORDS (SWM_MAX_CIGAR + 2) /* [cur_read, n | primary<<31, loc * n] */
+#define SWM_CIGAR_STRIDE (SWM_MAX_CIGAR * 16) /* [NM, len, text] per location     */
+/* Envelope: read length and error threshold (mapper_cpe.c:15,686,2515). */
+#define SWM_MAX_READ_LEN 254
+#define SWM_MAX_ERRORS 15
+
+enum {
+    SWM_OK = 0,
+    SWM_ERR_ARG = -1,      /* bad argument or outside the envelope          */
+    SWM_ERR_IO = -2,       /* file missing, short or unwritable             */
+    SWM_ERR_OOM = -3,      /* device or host allocation failed              */
+    SWM_ERR_CUDA = -4,     /* a CUDA call failed (see swm_last_error)       */
+    SWM_ERR_OVERFLOW = -5, /* a caller buffer is too small for the results  */
+    SWM_ERR_TIMEOUT = -6,  /* a bounded wait gave up                        */
+    SWM_ERR_STATE = -7     /* call out of order (e.g. wait without submit)  */
+};
+
+/* Text of the last error on this thread (never NULL). */
+const char *swm_last_error(void);
+
+/* ------------------------------------------------------------------ index */
+
+typedef struct swm_index swm_index;
+
+typedef struct {
+    uint32_t k;          /* seed length (-s)                                */
+    uint64_t n;          /* bases in the concatenated reference             */
+    uint64_t n_seeds;    /* entries in .positions / .pos_lseeds             */
+    uint64_t n_words2;   /* words in .base_2bits                            */
+    uint64_t n_words3;   /* words in .base_3bits                            */
+    uint64_t ref_length; /* bytes(.base_2bits) * 16, as mapper_mpe.c:288    */
+    int device;
+} swm_index_info;
+
+/* Replaces serial_index.c main + construct_hash_index (serial_index.c:818-852,
+ * 359-445): read the FASTA at fasta_path, build the k-mer index on the GPU and
+ * write <prefix>.{ref_info,hash_count,hash_offset,positions,pos_lseeds,
+ * base_2bits,base_3bits}. */
+int swm_index_build_fasta(const char *fasta_path, const char *prefix, uint32_t k, int device);
+
+/* Build a device-resident index from n bases already concatenated in host
+ * memory (the body of construct_hash_index, serial_index.c:396-438). */
+int swm_index_build(const uint8_t *seq, uint64_t n, uint32_t k, int device, swm_index **out);
+
+/* As swm_index_build, with the bases already in device memory. */
+int swm_index_build_device(const uint8_t *d_seq, uint64_t n, uint32_t k, int device, swm_index **out);
+
+/* Replaces load_ref_info (mapper_mpe.c:198-314): load the index files of
+ * `prefix` into device memory (hash_offset rebuilt from .hash_count). */
+int swm_index_open(const char *prefix, uint32_t k, int device, swm_index **out);
+
+/* Write the index files of a device-resident index (serial_index.c:73-138);
+ * ref_info is the text of <prefix>.ref_info (may be NULL for an empty file). */
+int swm_index_save(const swm_index *ix, const char *prefix, const char *ref_info, size_t ref_info_len);
+
+int swm_index_get_info(const swm_index *ix, swm_index_info *info);
+
+/* Copy the index arrays to host memory in file layout (any pointer may be
+ * NULL). hash_offset_end gets the END offsets serial_index writes. */
+int swm_index_download(const swm_index *ix, uint32_t *hash_count, uint32_t *hash_offset_end, uint32_t *positions,
+                       uint16_t *pos_lseeds, uint32_t *base_2bits, uint32_t *base_3bits);
+
+void swm_index_free(swm_index *ix);
+
+/* ---------------------------------------------------------------- mapping */
+
+typedef struct swm_mapper swm_mapper;
+
+/* Inputs of one block of reads: ref_info_t.reads[cur_block],
+ * reads_seq_len[cur_block], reads_seq_length, reads_num, errors
+ * (fm_define.h:30-40; filled at mapper_mpe.c:886-904,966-967). */
+typedef struct {
+    const char *reads;             /* reads_num reads at a fixed stride           */
+    const uint32_t *reads_len;     /* length of each read (<= SWM_MAX_READ_LEN)    */
+    uint64_t stride;               /* reads_seq_length (-l)                        */
+    uint64_t reads_num;            /* reads in this block                          */
+    uint32_t errors;               /* -e                                           */
+    const uint8_t *errors_per_read;/* optional per-read threshold (NULL = errors). */
+} swm_batch;
+
+/* Outputs: ref_info_t.ref_pos_buffer / cigar_buffer / cigar_num and the
+ * counters *cigar_ind / *unmap_ind (fm_define.h:42-49). Records are written in
+ * (read, strand, record) order; cur_read = 2 * read + strand as in
+ * mapper_cpe.c:2628. */
+typedef struct {
+    uint32_t *ref_pos_buffer;   /* records_cap * SWM_RECORD_WORDS words          */
+    uint8_t *cigar_buffer;      /* records_cap * SWM_CIGAR_STRIDE bytes (may be NULL) */
+    uint32_t *unmapped;         /* unmapped_cap cur_read ids (2 * read + 1)      */
+    uint64_t records_cap, unmapped_cap;
+    uint64_t n_records;         /* *cigar_ind                                    */
+    uint64_t n_unmapped;        /* *unmap_ind                                    */
+} swm_result;
+
+/* Work counters of the last completed block. */
+typedef struct {
+    uint64_t reads, items;      /* reads and (read, strand) items               */
+    uint64_t chunks;            /* bucket fetches of <= 32 positions            */
+    uint64_t batches;           /* candidate batches (alignment_rmdup flushes)  */
+    uint64_t fetched;           /* positions fetched                            */
+    uint64_t candidates;        /* windows verified by banded Myers              */
+    uint64_t cells;             /* sum over candidates of L * (2e + 1)           */
+    uint64_t passed;            /* candidates with error <= e                    */
+    uint64_t records;           /* output records                                */
+    uint64_t locations;         /* output locations                              */
+    uint64_t mapped_reads;      /* reads with >= 1 location on either strand     */
+    uint64_t retries;           /* block re-runs after growing a work buffer     */
+    uint64_t h2d_bytes;         /* host -> device bytes of the block (0 when resident) */
+    uint64_t d2h_bytes;         /* device -> host bytes of the block's results   */
+} swm_map_stats;
+
+/* Create a mapping context on the index's device with its own CUDA stream and
+ * work buffers for blocks of up to max_reads reads (mapper_mpe.c:727 uses
+ * 10,000). */
+int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper **out);
+
+/* find_positions over one block, synchronously: copy the reads in, map both
+ * strands of every read, copy the records out. */
+int swm_map_batch(swm_mapper *m, const swm_batch *b, swm_result *r);
+
+/* Asynchronous pair, the analog of athread_spawn / athread_join
+ * (mapper_mpe.c:972,1036): submit copies the inputs to pinned staging and
+ * queues all the work on the mapper's stream; wait blocks until it is done
+ * and fills r. One block may be in flight per mapper. */
+int swm_map_submit(swm_mapper *m, const swm_batch *b);
+int swm_map_wait(swm_mapper *m, swm_result *r);
+
+/* Device-resident variant (no host copies): d_reads / d_lens / d_errors are
+ * device pointers. Results stay on the device until swm_map_fetch. */
+int swm_map_device(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, uint64_t stride,
+                   uint64_t reads_num, uint32_t errors, const uint8_t *d_errors);
+int swm_map_fetch(swm_mapper *m, swm_result *r);
+
+int swm_mapper_stats(const swm_mapper *m, swm_map_stats *s);
+
+/* Per-stage device time of the last block in milliseconds (CUDA events on the
+ * mapper's stream); names are "seed", "plan", "candidates", "verify",
+ * "records", "total". Returns SWM_ERR_ARG for an unknown name. */
+int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float *ms);
+
+/* Kernel launches queued for the last block. */
+uint64_t swm_mapper_launches(const swm_mapper *m);
+
+/* The CUDA stream of the mapper (a cudaStream_t), for callers that order
+ * their own work around it. */
+void *swm_mapper_stream(const swm_mapper *m);
+
+/* Verified candidates of the last block in verification order: item
+ * (= 2 * read + strand), window-start candidate position, Myers error and
+ * location. For tests; n gets the total even when cap is smaller. */
+int swm_mapper_debug_candidates(const swm_mapper *m, uint32_t *item, uint32_t *pos, int32_t *err, int32_t *loc,
+                                uint64_t cap, uint64_t *n);
+
+void swm_mapper_free(swm_mapper *m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

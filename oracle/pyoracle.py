@@ -17,10 +17,7 @@ import subprocess
 
 import numpy as np
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_ORACLE = os.path.join(HERE, "_build", "libswm_oracle.so")
-REF_DIR = os.path.join(HERE, "_ref")
-LIB_SWREF = os.path.join(REF_DIR, "libswref.so")
+from .build import LIB_ORACLE, LIB_SWREF, REF_DIR
 
 RECORD_WORDS = 258
 CIGAR_STRIDE = 4096
@@ -73,7 +70,8 @@ def lib():
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_ORACLE):
-            raise RuntimeError("oracle library not built: run __graft_entry__.build()")
+            from .build import build_oracle
+            build_oracle()
         L = C.CDLL(LIB_ORACLE)
         L.swo_index_build.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(_Index)]
         L.swo_index_free.argtypes = [C.POINTER(_Index)]

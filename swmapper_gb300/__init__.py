@@ -1,0 +1,254 @@
+"""GB300 short-read mapper hot path (SWMapper's index build + mapping kernel).
+
+Thin ctypes view of the C ABI in include/swmapper.h (libswmapper_gb300.so).
+There is no CPU fallback: importing the classes below on a machine where the
+CUDA library was not built raises.
+
+    ix = Index.build(seq_bytes, k=12)            # GPU k-mer index
+    m = Mapper(ix, max_reads=65536)
+    res = m.map(reads, lens, errors=7)            # reference output layout
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+RECORD_WORDS = 258
+CIGAR_STRIDE = 4096
+MAX_READ_LEN = 254
+MAX_ERRORS = 15
+
+
+class IndexInfo(C.Structure):
+    _fields_ = [("k", C.c_uint32), ("n", C.c_uint64), ("n_seeds", C.c_uint64), ("n_words2", C.c_uint64),
+                ("n_words3", C.c_uint64), ("ref_length", C.c_uint64), ("device", C.c_int)]
+
+
+class Batch(C.Structure):
+    _fields_ = [("reads", C.c_void_p), ("reads_len", C.c_void_p), ("stride", C.c_uint64),
+                ("reads_num", C.c_uint64), ("errors", C.c_uint32), ("errors_per_read", C.c_void_p)]
+
+
+class Result(C.Structure):
+    _fields_ = [("ref_pos_buffer", C.c_void_p), ("cigar_buffer", C.c_void_p), ("unmapped", C.c_void_p),
+                ("records_cap", C.c_uint64), ("unmapped_cap", C.c_uint64), ("n_records", C.c_uint64),
+                ("n_unmapped", C.c_uint64)]
+
+
+STAT_FIELDS = ["reads", "items", "chunks", "batches", "fetched", "candidates", "cells", "passed", "records",
+               "locations", "mapped_reads", "retries", "h2d_bytes", "d2h_bytes"]
+
+
+class MapStats(C.Structure):
+    _fields_ = [(f, C.c_uint64) for f in STAT_FIELDS]
+
+
+class SwmError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library; raise if it was not built (no fallback path)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_build.LIB_CUDA):
+            raise SwmError(f"{_build.LIB_CUDA} is missing: run __graft_entry__.build() first")
+        L = C.CDLL(_build.LIB_CUDA)
+        vp, u32, u64 = C.c_void_p, C.c_uint32, C.c_uint64
+        L.swm_last_error.restype = C.c_char_p
+        L.swm_index_build.argtypes = [vp, u64, u32, C.c_int, C.POINTER(vp)]
+        L.swm_index_build_device.argtypes = [vp, u64, u32, C.c_int, C.POINTER(vp)]
+        L.swm_index_build_fasta.argtypes = [C.c_char_p, C.c_char_p, u32, C.c_int]
+        L.swm_index_open.argtypes = [C.c_char_p, u32, C.c_int, C.POINTER(vp)]
+        L.swm_index_save.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_size_t]
+        L.swm_index_get_info.argtypes = [vp, C.POINTER(IndexInfo)]
+        L.swm_index_download.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.swm_index_free.argtypes = [vp]
+        L.swm_index_free.restype = None
+        L.swm_mapper_create.argtypes = [vp, u64, C.POINTER(vp)]
+        L.swm_map_batch.argtypes = [vp, C.POINTER(Batch), C.POINTER(Result)]
+        L.swm_map_submit.argtypes = [vp, C.POINTER(Batch)]
+        L.swm_map_wait.argtypes = [vp, C.POINTER(Result)]
+        L.swm_map_device.argtypes = [vp, vp, vp, u64, u64, u32, vp]
+        L.swm_map_fetch.argtypes = [vp, C.POINTER(Result)]
+        L.swm_mapper_stats.argtypes = [vp, C.POINTER(MapStats)]
+        L.swm_mapper_stage_ms.argtypes = [vp, C.c_char_p, C.POINTER(C.c_float)]
+        L.swm_mapper_launches.argtypes = [vp]
+        L.swm_mapper_launches.restype = u64
+        L.swm_mapper_stream.argtypes = [vp]
+        L.swm_mapper_stream.restype = vp
+        L.swm_mapper_debug_candidates.argtypes = [vp, vp, vp, vp, vp, u64, C.POINTER(u64)]
+        L.swm_mapper_free.argtypes = [vp]
+        L.swm_mapper_free.restype = None
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise SwmError(f"{what} failed ({rc}): {lib().swm_last_error().decode(errors='replace')}")
+
+
+class Index:
+    """Device-resident k-mer index (swm_index)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def build(cls, seq, k: int = 12, device: int = 0) -> "Index":
+        seq = np.ascontiguousarray(np.frombuffer(seq, np.uint8) if isinstance(seq, (bytes, bytearray)) else seq,
+                                   dtype=np.uint8)
+        h = C.c_void_p()
+        _check(lib().swm_index_build(seq.ctypes.data, seq.size, k, device, C.byref(h)), "swm_index_build")
+        return cls(h)
+
+    @classmethod
+    def open(cls, prefix: str, k: int = 12, device: int = 0) -> "Index":
+        h = C.c_void_p()
+        _check(lib().swm_index_open(prefix.encode(), k, device, C.byref(h)), "swm_index_open")
+        return cls(h)
+
+    @staticmethod
+    def build_fasta(fasta: str, prefix: str, k: int = 12, device: int = 0) -> None:
+        _check(lib().swm_index_build_fasta(fasta.encode(), prefix.encode(), k, device), "swm_index_build_fasta")
+
+    def save(self, prefix: str, ref_info: bytes = b"") -> None:
+        _check(lib().swm_index_save(self._h, prefix.encode(), ref_info, len(ref_info)), "swm_index_save")
+
+    def info(self) -> IndexInfo:
+        inf = IndexInfo()
+        _check(lib().swm_index_get_info(self._h, C.byref(inf)), "swm_index_get_info")
+        return inf
+
+    def download(self) -> dict:
+        inf = self.info()
+        nb = 1 << (2 * inf.k)
+        out = dict(hash_count=np.zeros(nb, np.uint32), hash_offset=np.zeros(nb + 1, np.uint32),
+                   positions=np.zeros(inf.n_seeds, np.uint32), pos_lseeds=np.zeros(inf.n_seeds, np.uint16),
+                   base_2bits=np.zeros(inf.n_words2, np.uint32), base_3bits=np.zeros(inf.n_words3, np.uint32))
+        _check(lib().swm_index_download(self._h, *(out[k].ctypes.data for k in
+                                                   ("hash_count", "hash_offset", "positions", "pos_lseeds",
+                                                    "base_2bits", "base_3bits"))), "swm_index_download")
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            lib().swm_index_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MapOutput:
+    """Records in the reference layout plus the unmapped read ids."""
+
+    def __init__(self, ref_pos, cigar, unmapped, stats):
+        self.ref_pos, self.cigar, self.unmapped, self.stats = ref_pos, cigar, unmapped, stats
+
+    def records(self):
+        out = []
+        for r in range(self.ref_pos.shape[0]):
+            rec = self.ref_pos[r]
+            n = int(rec[1] & 0x0FFFFFFF)
+            locs = tuple(int(x) for x in rec[2:2 + n])
+            cb = self.cigar[r]
+            p = 0
+            parts = []
+            for _ in range(n):
+                ln = int(cb[p + 1])
+                parts.append(bytes(cb[p:p + 2 + ln]))
+                p += 2 + ln
+            out.append((int(rec[0]), int(rec[1]) >> 31, locs, b"".join(parts)))
+        return out
+
+
+class Mapper:
+    """Mapping context (swm_mapper): one CUDA stream and its work buffers."""
+
+    def __init__(self, index: Index, max_reads: int = 65536):
+        self.index = index
+        self.max_reads = max_reads
+        h = C.c_void_p()
+        _check(lib().swm_mapper_create(index._h, max_reads, C.byref(h)), "swm_mapper_create")
+        self._h = h
+
+    def _result(self, nreads: int, records_cap: int | None = None):
+        cap = records_cap or max(64, 4 * nreads + 64)
+        ref_pos = np.zeros((cap, RECORD_WORDS), np.uint32)
+        cigar = np.zeros((cap, CIGAR_STRIDE), np.uint8)
+        unm = np.zeros(max(1, nreads), np.uint32)
+        res = Result(ref_pos.ctypes.data, cigar.ctypes.data, unm.ctypes.data, cap, unm.size, 0, 0)
+        return res, ref_pos, cigar, unm
+
+    def map(self, reads: np.ndarray, lens: np.ndarray, errors: int, errors_per_read=None,
+            records_cap: int | None = None) -> MapOutput:
+        """Map a block of reads held in host memory (swm_map_batch)."""
+        reads = np.ascontiguousarray(reads, np.uint8)
+        lens = np.ascontiguousarray(lens, np.uint32)
+        n, stride = reads.shape
+        epr = None if errors_per_read is None else np.ascontiguousarray(errors_per_read, np.uint8)
+        b = Batch(reads.ctypes.data, lens.ctypes.data, stride, n, errors, epr.ctypes.data if epr is not None else None)
+        res, ref_pos, cigar, unm = self._result(n, records_cap)
+        _check(lib().swm_map_batch(self._h, C.byref(b), C.byref(res)), "swm_map_batch")
+        return MapOutput(ref_pos[:res.n_records], cigar[:res.n_records], unm[:res.n_unmapped], self.stats())
+
+    def map_device(self, d_reads: int, d_lens: int, stride: int, nreads: int, errors: int, d_errors: int | None = None):
+        """Map reads already resident in device memory (pointers as ints)."""
+        _check(lib().swm_map_device(self._h, d_reads, d_lens, stride, nreads, errors, d_errors),
+               "swm_map_device")
+
+    def fetch(self, nreads: int, records_cap: int | None = None) -> MapOutput:
+        res, ref_pos, cigar, unm = self._result(nreads, records_cap)
+        _check(lib().swm_map_fetch(self._h, C.byref(res)), "swm_map_fetch")
+        return MapOutput(ref_pos[:res.n_records], cigar[:res.n_records], unm[:res.n_unmapped], self.stats())
+
+    def stats(self) -> dict:
+        s = MapStats()
+        _check(lib().swm_mapper_stats(self._h, C.byref(s)), "swm_mapper_stats")
+        return {f: int(getattr(s, f)) for f in STAT_FIELDS}
+
+    def stage_ms(self, stage: str) -> float:
+        v = C.c_float()
+        _check(lib().swm_mapper_stage_ms(self._h, stage.encode(), C.byref(v)), "swm_mapper_stage_ms")
+        return float(v.value)
+
+    def launches(self) -> int:
+        return int(lib().swm_mapper_launches(self._h))
+
+    def stream(self) -> int:
+        return int(lib().swm_mapper_stream(self._h) or 0)
+
+    def debug_candidates(self):
+        n = C.c_uint64()
+        _check(lib().swm_mapper_debug_candidates(self._h, None, None, None, None, 0, C.byref(n)), "debug")
+        k = n.value
+        item = np.zeros(k, np.uint32)
+        pos = np.zeros(k, np.uint32)
+        err = np.zeros(k, np.int32)
+        loc = np.zeros(k, np.int32)
+        _check(lib().swm_mapper_debug_candidates(self._h, item.ctypes.data, pos.ctypes.data, err.ctypes.data,
+                                                 loc.ctypes.data, k, C.byref(n)), "debug")
+        return item, pos, err, loc
+
+    def close(self) -> None:
+        if self._h:
+            lib().swm_mapper_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,8 +1,7 @@
-"""Build recipes for the in-tree native libraries.
+"""Build recipes for the in-tree native libraries of the package.
 
 Everything is compiled in place (no pip install): the CUDA library for sm_103a
-with nvcc, the C host pieces with gcc. `build_all()` is what
-`__graft_entry__.build()` runs, here and on the GPU host.
+with nvcc, the C host pieces and command-line tools with gcc.
 """
 from __future__ import annotations
 
@@ -16,15 +15,11 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
-ORACLE = os.path.join(ROOT, "oracle")
 
 LIB_CUDA = os.path.join(PKG, "libswmapper_gb300.so")
 LIB_SYNTH = os.path.join(PKG, "libswm_synth.so")
 BIN_INDEX = os.path.join(PKG, "swm_index")
 BIN_MAP = os.path.join(PKG, "swm_mapper")
-LIB_ORACLE = os.path.join(ORACLE, "_build", "libswm_oracle.so")
-REF_DIR = os.path.join(ORACLE, "_ref")
-LIB_SWREF = os.path.join(REF_DIR, "libswref.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["swm_index.cu", "swm_map.cu"]
@@ -58,32 +53,6 @@ def build_synth() -> str:
     if not _newer(LIB_SYNTH, deps):
         _run(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-I", INCLUDE, src, "-o", LIB_SYNTH])
     return LIB_SYNTH
-
-
-def build_oracle() -> str:
-    src = os.path.join(ORACLE, "swm_oracle.c")
-    deps = [src, os.path.join(ORACLE, "swm_oracle.h")]
-    os.makedirs(os.path.dirname(LIB_ORACLE), exist_ok=True)
-    if not _newer(LIB_ORACLE, deps):
-        _run(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-pthread", src, "-o", LIB_ORACLE])
-    return LIB_ORACLE
-
-
-def build_ref() -> str | None:
-    """Compile the reference's own source into oracle/_ref (test infrastructure).
-
-    Works where the reference tree is present, or where oracle/_ref/src was
-    produced earlier; returns None when neither is available.
-    """
-    have_src = os.path.exists(os.path.join(REF_DIR, "src", "mapper_ref.c"))
-    have_tree = os.path.exists(os.path.join(os.environ.get("REF_DIR", "/root/reference"), "mapper_cpe.c"))
-    if not (have_src or have_tree):
-        return None
-    proc = subprocess.run(["bash", os.path.join(ORACLE, "build_ref.sh")], capture_output=True, text=True)
-    if proc.returncode != 0:
-        sys.stderr.write(proc.stdout + proc.stderr)
-        return None
-    return LIB_SWREF
 
 
 def build_cuda() -> str:
@@ -123,10 +92,7 @@ def build_cli() -> None:
                   "-L", PKG, "-lswmapper_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread"])
 
 
-def build_all(with_ref: bool = True) -> None:
+def build_all() -> None:
     build_synth()
-    build_oracle()
-    if with_ref:
-        build_ref()
     build_cuda()
     build_cli()

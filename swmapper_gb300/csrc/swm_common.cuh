@@ -1,0 +1,55 @@
+// swm_common.cuh -- shared definitions of the GB300 mapper library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "swmapper.h"
+
+#define SWM_SEED_STEP 4          // fm_define.h:13
+#define SWM_PAD_WORDS 64         // zero words after base_2bits (genome end reads base A)
+#define SWM_BATCH_POSITIONS 2048 // positions_size, mapper_cpe.c:2129
+#define SWM_PER_FETCH 32         // seeds_per_block, mapper_cpe.c:2178
+#define SWM_MAX_RUNS_BLOCK 256   // block_size bound, mapper_cpe.c:2265
+#define SWM_MAX_SEL 64           // (SWM_MAX_ERRORS + 1) * SWM_SEED_STEP
+#define SWM_MAXERROR 10000       // MAXERROR, mapper_cpe.c:17
+#define SWM_WIN_WORDS 12         // aligned window words per plane (L + 2e + 32 < 384)
+#define SWM_CIGAR_SLOT 128       // CIGAR text bytes kept per verified candidate
+
+// error helpers (implemented in swm_index.cu)
+void swm_set_error(const char *fmt, ...);
+
+#define SWM_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess) {                                                                \
+            swm_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));   \
+            return SWM_ERR_CUDA;                                                                \
+        }                                                                                       \
+    } while (0)
+
+// Device-resident index (mapper layout).
+struct swm_index {
+    int device;
+    uint32_t k;
+    uint64_t n, n_seeds, n_words2, n_words3, ref_length;
+    uint32_t *d_count;     // 4^k
+    uint32_t *d_off;       // 4^k + 1 start offsets (mapper_mpe.c:250-255)
+    uint32_t *d_pos;       // n_seeds (+8)
+    uint16_t *d_lseed;     // n_seeds (+8)
+    uint32_t *d_b2;        // n_words2 + SWM_PAD_WORDS
+    uint32_t *d_b3;        // n_words3 + SWM_PAD_WORDS
+};
+
+// Exclusive scan of n u32 values (n read from *d_n when d_n is not NULL,
+// else n_host; clamped to n_cap); out gets n + 1 entries, out[n] = total,
+// and *d_total = total when d_total is not NULL. tmp needs
+// swm_scan_tmp_words(n_cap) words. Implemented in swm_index.cu.
+uint64_t swm_scan_tmp_words(uint64_t n_cap);
+int swm_exclusive_scan(const uint32_t *d_in, uint32_t *d_out, const uint32_t *d_n, uint64_t n_host, uint64_t n_cap,
+                       uint32_t *d_tmp, uint32_t *d_total, cudaStream_t st);
+
+__device__ __forceinline__ uint32_t swm_fsr(uint32_t lo, uint32_t hi, uint32_t s) {
+    // (hi:lo) >> s for s in [0, 31]; s == 0 gives lo (defined form of the
+    // reference's x >> s | y << (32 - s))
+    return __funnelshift_r(lo, hi, s);
+}

@@ -1,0 +1,718 @@
+// swm_index.cu -- GPU k-mer index build, index files, device scan.
+//
+// Index build (serial_index.c:157-445, rebuilt for the GPU):
+//   kb_encode   32 bases per thread -> lo/hi bit planes, N mask, 2-bit seed
+//               words (get_seed, serial_index.c:157-232)
+//   kb_count    one thread per sampled position p = 4t: k-mer and N test
+//               from the packed words, atomic count (chromo_hash_index,
+//               serial_index.c:253-269)
+//   scan        start offsets (store_positions, serial_index.c:337-340)
+//   kb_scatter  atomic slot per sampled position, key = position << 16 | lseed
+//               (serial_index.c:343-352 without the serial order)
+//   kb_sort_*   per-bucket sort of the keys: positions are unique, so sorting
+//               each bucket restores the ascending order the reference's
+//               serial scatter produces
+//   kb_split    keys -> .positions (u32) + .pos_lseeds (u16)
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "swm_common.cuh"
+#include "swm_files.h"
+
+// ----------------------------------------------------------------- errors
+
+static thread_local char g_err[512] = "";
+
+void swm_set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+extern "C" const char *swm_last_error(void) { return g_err; }
+
+// ------------------------------------------------------------------- scan
+
+#define SCAN_T 256
+#define SCAN_V 8
+#define SCAN_TILE (SCAN_T * SCAN_V)
+
+uint64_t swm_scan_tmp_words(uint64_t n_cap) { return (n_cap + SCAN_TILE - 1) / SCAN_TILE + 64; }
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, d);
+        if ((threadIdx.x & 31) >= d) v += t;
+    }
+    return v;
+}
+
+// exclusive block scan of one value per thread (blockDim.x == SCAN_T or 1024)
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total) {
+    __shared__ uint32_t wsum[33];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    uint32_t inc = warp_incl_scan(v);
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t s = lane < nw ? wsum[lane] : 0u;
+        uint32_t si = warp_incl_scan(s);
+        if (lane < nw) wsum[lane] = si - s;
+        if (lane == nw - 1) wsum[32] = si;
+    }
+    __syncthreads();
+    uint32_t r = inc - v + wsum[wid];
+    if (total) *total = wsum[32];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ uint64_t scan_n(const uint32_t *d_n, uint64_t n_host, uint64_t n_cap) {
+    uint64_t n = d_n ? (uint64_t)*d_n : n_host;
+    return n < n_cap ? n : n_cap;
+}
+
+__global__ void k_scan_reduce(const uint32_t *__restrict__ in, const uint32_t *d_n, uint64_t n_host, uint64_t n_cap,
+                              uint32_t *__restrict__ part) {
+    const uint64_t n = scan_n(d_n, n_host, n_cap);
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    uint32_t s = 0;
+    if (base < n) {
+#pragma unroll
+        for (int v = 0; v < SCAN_V; v++) {
+            uint64_t i = base + threadIdx.x + (uint64_t)v * SCAN_T;
+            if (i < n) s += in[i];
+        }
+    }
+    uint32_t tot;
+    block_excl_scan(s, &tot);
+    if (threadIdx.x == 0) part[blockIdx.x] = (base < n) ? tot : 0u;
+}
+
+__global__ void k_scan_top(uint32_t *part, const uint32_t *d_n, uint64_t n_host, uint64_t n_cap, uint32_t *out,
+                           uint32_t *d_total) {
+    const uint64_t n = scan_n(d_n, n_host, n_cap);
+    const uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    const uint64_t per = (nb + blockDim.x - 1) / blockDim.x;
+    const uint64_t b0 = threadIdx.x * per;
+    uint32_t s = 0;
+    for (uint64_t i = b0; i < b0 + per && i < nb; i++) s += part[i];
+    uint32_t tot;
+    uint32_t ex = block_excl_scan(s, &tot);
+    for (uint64_t i = b0; i < b0 + per && i < nb; i++) {
+        uint32_t v = part[i];
+        part[i] = ex;
+        ex += v;
+    }
+    if (threadIdx.x == 0) {
+        out[n] = tot;
+        if (d_total) *d_total = tot;
+    }
+}
+
+__global__ void k_scan_down(const uint32_t *__restrict__ in, const uint32_t *d_n, uint64_t n_host, uint64_t n_cap,
+                            const uint32_t *__restrict__ part, uint32_t *__restrict__ out) {
+    const uint64_t n = scan_n(d_n, n_host, n_cap);
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    if (base >= n) return;
+    const uint64_t i0 = base + (uint64_t)threadIdx.x * SCAN_V;
+    uint32_t v[SCAN_V];
+#pragma unroll
+    for (int j = 0; j < SCAN_V; j++) v[j] = (i0 + j < n) ? in[i0 + j] : 0u;
+    uint32_t s = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_V; j++) s += v[j];
+    uint32_t ex = block_excl_scan(s, nullptr) + part[blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < SCAN_V; j++) {
+        if (i0 + j < n) out[i0 + j] = ex;
+        ex += v[j];
+    }
+}
+
+int swm_exclusive_scan(const uint32_t *d_in, uint32_t *d_out, const uint32_t *d_n, uint64_t n_host, uint64_t n_cap,
+                       uint32_t *d_tmp, uint32_t *d_total, cudaStream_t st) {
+    const uint64_t nb = (n_cap + SCAN_TILE - 1) / SCAN_TILE;
+    const unsigned grid = (unsigned)(nb ? nb : 1);
+    k_scan_reduce<<<grid, SCAN_T, 0, st>>>(d_in, d_n, n_host, n_cap, d_tmp);
+    k_scan_top<<<1, 1024, 0, st>>>(d_tmp, d_n, n_host, n_cap, d_out, d_total);
+    k_scan_down<<<grid, SCAN_T, 0, st>>>(d_in, d_n, n_host, n_cap, d_tmp, d_out);
+    SWM_CUDA(cudaGetLastError());
+    return SWM_OK;
+}
+
+// ------------------------------------------------------------ index build
+
+__global__ void kb_encode(const uint8_t *__restrict__ seq, uint64_t n, uint32_t *__restrict__ b2,
+                          uint32_t *__restrict__ b3, uint32_t *__restrict__ s2) {
+    __shared__ uint8_t tab[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        int u = i & 0xdf; // toupper for letters (serial_index.c:152)
+        tab[i] = u == 'A' ? 0 : u == 'C' ? 1 : u == 'G' ? 2 : u == 'T' ? 3 : 4;
+    }
+    __syncthreads();
+    const uint64_t W = (n + 31) / 32;
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < W; w += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t p0 = w * 32;
+        const uint32_t cnt = (n - p0 >= 32) ? 32u : (uint32_t)(n - p0);
+        uint8_t bytes[32];
+        if (cnt == 32 && (((uintptr_t)(seq + p0)) & 15) == 0) {
+            const uint4 *v = reinterpret_cast<const uint4 *>(seq + p0);
+            uint4 a = v[0], b = v[1];
+            memcpy(bytes, &a, 16);
+            memcpy(bytes + 16, &b, 16);
+        } else {
+            for (uint32_t j = 0; j < cnt; j++) bytes[j] = seq[p0 + j];
+        }
+        uint32_t lo = 0, hi = 0, nm = 0, sa = 0, sb = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < 32; j++) {
+            if (j < cnt) {
+                uint32_t c = tab[bytes[j]];
+                if (c == 4) {
+                    nm |= 1u << j;
+                } else {
+                    lo |= (c & 1u) << j;
+                    hi |= (c >> 1) << j;
+                    if (j < 16) sa |= c << (2 * j);
+                    else sb |= c << (2 * (j - 16));
+                }
+            }
+        }
+        b2[2 * w] = lo;
+        b2[2 * w + 1] = hi;
+        b3[w] = nm;
+        s2[2 * w] = sa;
+        s2[2 * w + 1] = sb;
+    }
+}
+
+// k-mer at sampled position i (get_seed_from_enc_bits, serial_index.c:280-331)
+__device__ __forceinline__ bool sample_at(const uint32_t *__restrict__ b2, const uint32_t *__restrict__ b3,
+                                          const uint32_t *__restrict__ s2, uint64_t i, uint32_t k, uint32_t *seed,
+                                          uint32_t *lseed) {
+    const uint32_t smask = (k >= 16) ? 0xffffffffu : ((1u << (2 * k)) - 1);
+    const uint32_t nmask = (1u << k) - 1;
+    uint32_t nf = swm_fsr(b3[i / 32], b3[i / 32 + 1], (uint32_t)(i % 32)) & nmask;
+    if (nf) return false;
+    *seed = swm_fsr(s2[i / 16], s2[i / 16 + 1], (uint32_t)(i % 16) * 2) & smask;
+    const uint32_t res = SWM_SEED_STEP - 1, rmask = (1u << res) - 1;
+    uint64_t sp = (i >= res) ? i - res : 0;
+    uint32_t fl = swm_fsr(b2[(sp / 32) * 2], b2[(sp / 32 + 1) * 2], sp % 32) & rmask;
+    uint32_t fh = swm_fsr(b2[(sp / 32) * 2 + 1], b2[(sp / 32 + 1) * 2 + 1], sp % 32) & rmask;
+    sp = i + k;
+    uint32_t bl = swm_fsr(b2[(sp / 32) * 2], b2[(sp / 32 + 1) * 2], sp % 32) & rmask;
+    uint32_t bh = swm_fsr(b2[(sp / 32) * 2 + 1], b2[(sp / 32 + 1) * 2 + 1], sp % 32) & rmask;
+    fl |= bl << res;
+    fh |= bh << res;
+    *lseed = (fl | (fh << (res * 2))) & 0xffffu;
+    return true;
+}
+
+__global__ void kb_count(const uint32_t *__restrict__ b2, const uint32_t *__restrict__ b3,
+                         const uint32_t *__restrict__ s2, uint64_t T, uint32_t k, uint32_t *__restrict__ count) {
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < T; t += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t sd, ls;
+        if (sample_at(b2, b3, s2, t * SWM_SEED_STEP, k, &sd, &ls)) atomicAdd(&count[sd], 1u);
+    }
+}
+
+__global__ void kb_scatter(const uint32_t *__restrict__ b2, const uint32_t *__restrict__ b3,
+                           const uint32_t *__restrict__ s2, uint64_t T, uint32_t k, uint32_t *__restrict__ cursor,
+                           unsigned long long *__restrict__ keys) {
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < T; t += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t sd, ls;
+        const uint64_t i = t * SWM_SEED_STEP;
+        if (sample_at(b2, b3, s2, i, k, &sd, &ls)) {
+            uint32_t slot = atomicAdd(&cursor[sd], 1u);
+            keys[slot] = ((unsigned long long)i << 16) | ls;
+        }
+    }
+}
+
+#define SORT_SMALL 32
+#define SORT_MED 2048
+
+__global__ void kb_classify(const uint32_t *__restrict__ count, uint64_t nb, uint32_t *__restrict__ lists,
+                            uint32_t *__restrict__ nlist, uint64_t list_cap) {
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t c = count[b];
+        if (c <= 1) continue;
+        int cls = c <= SORT_SMALL ? 0 : c <= SORT_MED ? 1 : 2;
+        uint32_t at = atomicAdd(&nlist[cls], 1u);
+        if (at < list_cap) lists[(uint64_t)cls * list_cap + at] = (uint32_t)b;
+    }
+}
+
+__device__ __forceinline__ unsigned long long shfl_u64(unsigned long long v, int lane_mask) {
+    uint32_t lo = (uint32_t)v, hi = (uint32_t)(v >> 32);
+    lo = __shfl_xor_sync(0xffffffffu, lo, lane_mask);
+    hi = __shfl_xor_sync(0xffffffffu, hi, lane_mask);
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+// one warp per bucket with <= 32 keys: bitonic sort across lanes
+__global__ void kb_sort_small(const uint32_t *__restrict__ list, const uint32_t *__restrict__ nlist,
+                              const uint32_t *__restrict__ off, const uint32_t *__restrict__ count,
+                              unsigned long long *__restrict__ keys) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const uint32_t total = *nlist;
+    for (uint64_t wi = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < total; wi += nwarps) {
+        const uint32_t b = list[wi];
+        const uint32_t o = off[b], c = count[b];
+        unsigned long long v = lane < c ? keys[o + lane] : ~0ull;
+#pragma unroll
+        for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                unsigned long long w = shfl_u64(v, stride);
+                bool up = ((lane & size) == 0);
+                bool lower = ((lane & stride) == 0);
+                bool take_min = (lower == up);
+                v = take_min ? (w < v ? w : v) : (w > v ? w : v);
+            }
+        }
+        if (lane < c) keys[o + lane] = v;
+    }
+}
+
+// one block per bucket with <= SORT_MED keys: bitonic sort in shared memory
+__global__ void kb_sort_med(const uint32_t *__restrict__ list, const uint32_t *__restrict__ nlist,
+                            const uint32_t *__restrict__ off, const uint32_t *__restrict__ count,
+                            unsigned long long *__restrict__ keys) {
+    __shared__ unsigned long long sm[SORT_MED];
+    const uint32_t total = *nlist;
+    for (uint32_t bi = blockIdx.x; bi < total; bi += gridDim.x) {
+        const uint32_t b = list[bi];
+        const uint32_t o = off[b], c = count[b];
+        uint32_t n2 = 1;
+        while (n2 < c) n2 <<= 1;
+        for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) sm[i] = i < c ? keys[o + i] : ~0ull;
+        __syncthreads();
+        for (uint32_t size = 2; size <= n2; size <<= 1) {
+            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t i = threadIdx.x; i < n2 / 2; i += blockDim.x) {
+                    uint32_t lo = 2 * i - (i & (stride - 1));
+                    uint32_t hi = lo + stride;
+                    bool up = ((lo & size) == 0);
+                    unsigned long long a = sm[lo], d = sm[hi];
+                    if ((a > d) == up) {
+                        sm[lo] = d;
+                        sm[hi] = a;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t i = threadIdx.x; i < c; i += blockDim.x) keys[o + i] = sm[i];
+        __syncthreads();
+    }
+}
+
+// one block per large bucket: bitonic sort in a padded global scratch region
+__global__ void kb_sort_large(const uint32_t *__restrict__ list, const uint32_t *__restrict__ off,
+                              const uint32_t *__restrict__ count, const uint64_t *__restrict__ scratch_off,
+                              unsigned long long *__restrict__ scratch, unsigned long long *__restrict__ keys) {
+    const uint32_t b = list[blockIdx.x];
+    const uint32_t o = off[b], c = count[b];
+    unsigned long long *sm = scratch + scratch_off[blockIdx.x];
+    uint32_t n2 = 1;
+    while (n2 < c) n2 <<= 1;
+    for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) sm[i] = i < c ? keys[o + i] : ~0ull;
+    __syncthreads();
+    for (uint32_t size = 2; size <= n2; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t i = threadIdx.x; i < n2 / 2; i += blockDim.x) {
+                uint32_t lo = 2 * i - (i & (stride - 1));
+                uint32_t hi = lo + stride;
+                bool up = ((lo & size) == 0);
+                unsigned long long a = sm[lo], d = sm[hi];
+                if ((a > d) == up) {
+                    sm[lo] = d;
+                    sm[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (uint32_t i = threadIdx.x; i < c; i += blockDim.x) keys[o + i] = sm[i];
+}
+
+__global__ void kb_split(const unsigned long long *__restrict__ keys, uint64_t S, uint32_t *__restrict__ pos,
+                         uint16_t *__restrict__ lseed) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < S; j += (uint64_t)gridDim.x * blockDim.x) {
+        unsigned long long v = keys[j];
+        pos[j] = (uint32_t)(v >> 16);
+        lseed[j] = (uint16_t)(v & 0xffffu);
+    }
+}
+
+// ----------------------------------------------------------- host helpers
+
+static int sm_count(int device) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
+    return n > 0 ? n : 1;
+}
+
+static unsigned grid_for(uint64_t work, unsigned threads, int device, int per_sm = 8) {
+    uint64_t g = (work + threads - 1) / threads;
+    uint64_t cap = (uint64_t)sm_count(device) * per_sm;
+    if (g > cap) g = cap;
+    return (unsigned)(g ? g : 1);
+}
+
+static void index_release(swm_index *ix) {
+    if (!ix) return;
+    cudaFree(ix->d_count);
+    cudaFree(ix->d_off);
+    cudaFree(ix->d_pos);
+    cudaFree(ix->d_lseed);
+    cudaFree(ix->d_b2);
+    cudaFree(ix->d_b3);
+    free(ix);
+}
+
+template <typename T>
+static int dalloc(T **p, uint64_t count) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void **)p, (count ? count : 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        swm_set_error("cudaMalloc(%llu bytes): %s", (unsigned long long)(count * sizeof(T)), cudaGetErrorString(e));
+        *p = nullptr;
+        return SWM_ERR_OOM;
+    }
+    return SWM_OK;
+}
+
+static int build_on_device(const uint8_t *d_seq, uint64_t n, uint32_t k, int device, swm_index **out) {
+    if (k < 1 || k > 14 || n >= 0xffffffffull) {
+        swm_set_error("swm_index_build: k must be in [1, 14] and n < 2^32 (k=%u n=%llu)", k, (unsigned long long)n);
+        return SWM_ERR_ARG;
+    }
+    SWM_CUDA(cudaSetDevice(device));
+    swm_index *ix = (swm_index *)calloc(1, sizeof(swm_index));
+    if (!ix) return SWM_ERR_OOM;
+    ix->device = device;
+    ix->k = k;
+    ix->n = n;
+    const uint64_t W = (n + 31) / 32;
+    const uint64_t nb = 1ull << (2 * k);
+    ix->n_words2 = 2 * W;
+    ix->n_words3 = W;
+    ix->ref_length = ix->n_words2 * 4 * 16;
+    cudaStream_t st = 0;
+    uint32_t *d_s2 = nullptr, *d_cursor = nullptr, *d_tmp = nullptr, *d_lists = nullptr, *d_nlist = nullptr;
+    unsigned long long *d_keys = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(d_s2);
+        cudaFree(d_cursor);
+        cudaFree(d_tmp);
+        cudaFree(d_lists);
+        cudaFree(d_nlist);
+        cudaFree(d_keys);
+    };
+#define TRYC(x)                  \
+    do {                         \
+        int rc_ = (x);           \
+        if (rc_ != SWM_OK) {     \
+            cleanup();           \
+            index_release(ix);   \
+            return rc_;          \
+        }                        \
+    } while (0)
+#define CUC(x)                                                                                   \
+    do {                                                                                         \
+        cudaError_t e_ = (x);                                                                    \
+        if (e_ != cudaSuccess) {                                                                 \
+            swm_set_error("%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_));       \
+            cleanup();                                                                           \
+            index_release(ix);                                                                   \
+            return SWM_ERR_CUDA;                                                                 \
+        }                                                                                        \
+    } while (0)
+    TRYC(dalloc(&ix->d_b2, ix->n_words2 + SWM_PAD_WORDS));
+    TRYC(dalloc(&ix->d_b3, ix->n_words3 + SWM_PAD_WORDS));
+    TRYC(dalloc(&d_s2, 2 * W + SWM_PAD_WORDS));
+    TRYC(dalloc(&ix->d_count, nb));
+    TRYC(dalloc(&ix->d_off, nb + 1));
+    TRYC(dalloc(&d_cursor, nb + 1));
+    TRYC(dalloc(&d_tmp, swm_scan_tmp_words(nb)));
+    CUC(cudaMemsetAsync(ix->d_b2 + ix->n_words2, 0, SWM_PAD_WORDS * 4, st));
+    CUC(cudaMemsetAsync(ix->d_b3 + ix->n_words3, 0, SWM_PAD_WORDS * 4, st));
+    CUC(cudaMemsetAsync(d_s2 + 2 * W, 0, SWM_PAD_WORDS * 4, st));
+    CUC(cudaMemsetAsync(ix->d_count, 0, nb * 4, st));
+    if (W) kb_encode<<<grid_for(W, 256, device, 16), 256, 0, st>>>(d_seq, n, ix->d_b2, ix->d_b3, d_s2);
+    const uint64_t T = (n >= k) ? (n - k) / SWM_SEED_STEP + 1 : 0;
+    if (T) kb_count<<<grid_for(T, 256, device, 16), 256, 0, st>>>(ix->d_b2, ix->d_b3, d_s2, T, k, ix->d_count);
+    CUC(cudaGetLastError());
+    TRYC(swm_exclusive_scan(ix->d_count, ix->d_off, nullptr, nb, nb, d_tmp, nullptr, st));
+    uint32_t S32 = 0;
+    CUC(cudaMemcpyAsync(&S32, ix->d_off + nb, 4, cudaMemcpyDeviceToHost, st));
+    CUC(cudaStreamSynchronize(st));
+    const uint64_t S = S32;
+    ix->n_seeds = S;
+    TRYC(dalloc(&ix->d_pos, S + 8));
+    TRYC(dalloc(&ix->d_lseed, S + 8));
+    CUC(cudaMemsetAsync(ix->d_pos + S, 0, 8 * 4, st));
+    CUC(cudaMemsetAsync(ix->d_lseed + S, 0, 8 * 2, st));
+    if (S) {
+        TRYC(dalloc(&d_keys, S));
+        CUC(cudaMemcpyAsync(d_cursor, ix->d_off, nb * 4, cudaMemcpyDeviceToDevice, st));
+        kb_scatter<<<grid_for(T, 256, device, 16), 256, 0, st>>>(ix->d_b2, ix->d_b3, d_s2, T, k, d_cursor, d_keys);
+        // per-bucket sort, classified by bucket size
+        const uint64_t list_cap = nb;
+        TRYC(dalloc(&d_lists, 3 * list_cap));
+        TRYC(dalloc(&d_nlist, 4));
+        CUC(cudaMemsetAsync(d_nlist, 0, 16, st));
+        kb_classify<<<grid_for(nb, 256, device, 16), 256, 0, st>>>(ix->d_count, nb, d_lists, d_nlist, list_cap);
+        kb_sort_small<<<sm_count(device) * 8, 256, 0, st>>>(d_lists, d_nlist, ix->d_off, ix->d_count, d_keys);
+        kb_sort_med<<<sm_count(device) * 4, 256, 0, st>>>(d_lists + list_cap, d_nlist + 1, ix->d_off, ix->d_count,
+                                                          d_keys);
+        CUC(cudaGetLastError());
+        uint32_t nl[3];
+        CUC(cudaMemcpyAsync(nl, d_nlist, 12, cudaMemcpyDeviceToHost, st));
+        CUC(cudaStreamSynchronize(st));
+        if (nl[2]) {
+            std::vector<uint32_t> big(nl[2]);
+            CUC(cudaMemcpy(big.data(), d_lists + 2 * list_cap, nl[2] * 4ull, cudaMemcpyDeviceToHost));
+            std::vector<uint32_t> cnt(nl[2]);
+            for (uint32_t i = 0; i < nl[2]; i++) CUC(cudaMemcpy(&cnt[i], ix->d_count + big[i], 4, cudaMemcpyDeviceToHost));
+            // process in groups whose padded scratch fits a bounded buffer
+            const uint64_t scratch_cap = 1ull << 27; // keys (1 GiB)
+            uint64_t i0 = 0;
+            while (i0 < nl[2]) {
+                std::vector<uint64_t> soff;
+                uint64_t tot = 0, i1 = i0;
+                while (i1 < nl[2]) {
+                    uint64_t n2 = 1;
+                    while (n2 < cnt[i1]) n2 <<= 1;
+                    if (tot && tot + n2 > scratch_cap) break;
+                    soff.push_back(tot);
+                    tot += n2;
+                    i1++;
+                }
+                unsigned long long *d_scr = nullptr;
+                uint64_t *d_soff = nullptr;
+                TRYC(dalloc(&d_scr, tot));
+                if (dalloc(&d_soff, soff.size()) != SWM_OK) {
+                    cudaFree(d_scr);
+                    cleanup();
+                    index_release(ix);
+                    return SWM_ERR_OOM;
+                }
+                cudaMemcpy(d_soff, soff.data(), soff.size() * 8, cudaMemcpyHostToDevice);
+                kb_sort_large<<<(unsigned)(i1 - i0), 1024, 0, st>>>(d_lists + 2 * list_cap + i0, ix->d_off,
+                                                                   ix->d_count, d_soff, d_scr, d_keys);
+                cudaError_t e = cudaStreamSynchronize(st);
+                cudaFree(d_scr);
+                cudaFree(d_soff);
+                CUC(e);
+                i0 = i1;
+            }
+        }
+        kb_split<<<grid_for(S, 256, device, 16), 256, 0, st>>>(d_keys, S, ix->d_pos, ix->d_lseed);
+        CUC(cudaGetLastError());
+    }
+    CUC(cudaStreamSynchronize(st));
+    cleanup();
+    *out = ix;
+    return SWM_OK;
+#undef TRYC
+#undef CUC
+}
+
+extern "C" int swm_index_build_device(const uint8_t *d_seq, uint64_t n, uint32_t k, int device, swm_index **out) {
+    if (!out || (!d_seq && n)) return SWM_ERR_ARG;
+    return build_on_device(d_seq, n, k, device, out);
+}
+
+extern "C" int swm_index_build(const uint8_t *seq, uint64_t n, uint32_t k, int device, swm_index **out) {
+    if (!out || (!seq && n)) return SWM_ERR_ARG;
+    SWM_CUDA(cudaSetDevice(device));
+    uint8_t *d_seq = nullptr;
+    if (n) {
+        cudaError_t e = cudaMalloc(&d_seq, n);
+        if (e != cudaSuccess) {
+            swm_set_error("cudaMalloc(sequence %llu): %s", (unsigned long long)n, cudaGetErrorString(e));
+            return SWM_ERR_OOM;
+        }
+        e = cudaMemcpy(d_seq, seq, n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(d_seq);
+            swm_set_error("H2D sequence: %s", cudaGetErrorString(e));
+            return SWM_ERR_CUDA;
+        }
+    }
+    int rc = build_on_device(d_seq, n, k, device, out);
+    cudaFree(d_seq);
+    return rc;
+}
+
+extern "C" int swm_index_get_info(const swm_index *ix, swm_index_info *info) {
+    if (!ix || !info) return SWM_ERR_ARG;
+    info->k = ix->k;
+    info->n = ix->n;
+    info->n_seeds = ix->n_seeds;
+    info->n_words2 = ix->n_words2;
+    info->n_words3 = ix->n_words3;
+    info->ref_length = ix->ref_length;
+    info->device = ix->device;
+    return SWM_OK;
+}
+
+extern "C" int swm_index_download(const swm_index *ix, uint32_t *hash_count, uint32_t *hash_offset_end,
+                                  uint32_t *positions, uint16_t *pos_lseeds, uint32_t *base_2bits,
+                                  uint32_t *base_3bits) {
+    if (!ix) return SWM_ERR_ARG;
+    SWM_CUDA(cudaSetDevice(ix->device));
+    const uint64_t nb = 1ull << (2 * ix->k);
+    if (hash_count) SWM_CUDA(cudaMemcpy(hash_count, ix->d_count, nb * 4, cudaMemcpyDeviceToHost));
+    if (hash_offset_end) {
+        // the reference's file holds the scatter cursors: start[i + 1] for
+        // bucket i, and the total once more at [4^k] (serial_index.c:337-352)
+        SWM_CUDA(cudaMemcpy(hash_offset_end, ix->d_off + 1, nb * 4, cudaMemcpyDeviceToHost));
+        hash_offset_end[nb] = (uint32_t)ix->n_seeds;
+    }
+    if (positions && ix->n_seeds) SWM_CUDA(cudaMemcpy(positions, ix->d_pos, ix->n_seeds * 4, cudaMemcpyDeviceToHost));
+    if (pos_lseeds && ix->n_seeds)
+        SWM_CUDA(cudaMemcpy(pos_lseeds, ix->d_lseed, ix->n_seeds * 2, cudaMemcpyDeviceToHost));
+    if (base_2bits && ix->n_words2)
+        SWM_CUDA(cudaMemcpy(base_2bits, ix->d_b2, ix->n_words2 * 4, cudaMemcpyDeviceToHost));
+    if (base_3bits && ix->n_words3)
+        SWM_CUDA(cudaMemcpy(base_3bits, ix->d_b3, ix->n_words3 * 4, cudaMemcpyDeviceToHost));
+    return SWM_OK;
+}
+
+extern "C" int swm_index_save(const swm_index *ix, const char *prefix, const char *ref_info, size_t ref_info_len) {
+    if (!ix || !prefix) return SWM_ERR_ARG;
+    const uint64_t nb = 1ull << (2 * ix->k);
+    std::vector<uint32_t> cnt(nb), off(nb + 1), pos(ix->n_seeds), b2(ix->n_words2), b3(ix->n_words3);
+    std::vector<uint16_t> ls(ix->n_seeds);
+    int rc = swm_index_download(ix, cnt.data(), off.data(), pos.data(), ls.data(), b2.data(), b3.data());
+    if (rc) return rc;
+    if (swmf_write(prefix, ".ref_info", ref_info ? ref_info : "", ref_info ? ref_info_len : 0) ||
+        swmf_write(prefix, ".hash_count", cnt.data(), nb * 4) ||
+        swmf_write(prefix, ".hash_offset", off.data(), (nb + 1) * 4) ||
+        swmf_write(prefix, ".positions", pos.data(), ix->n_seeds * 4) ||
+        swmf_write(prefix, ".pos_lseeds", ls.data(), ix->n_seeds * 2) ||
+        swmf_write(prefix, ".base_2bits", b2.data(), ix->n_words2 * 4) ||
+        swmf_write(prefix, ".base_3bits", b3.data(), ix->n_words3 * 4)) {
+        swm_set_error("cannot write index files under %s", prefix);
+        return SWM_ERR_IO;
+    }
+    return SWM_OK;
+}
+
+extern "C" int swm_index_build_fasta(const char *fasta_path, const char *prefix, uint32_t k, int device) {
+    if (!fasta_path || !prefix) return SWM_ERR_ARG;
+    uint8_t *seq = nullptr;
+    uint64_t n = 0;
+    char *info = nullptr;
+    size_t info_len = 0;
+    int rc = swmf_read_fasta(fasta_path, &seq, &n, &info, &info_len);
+    if (rc) {
+        swm_set_error("cannot read FASTA %s", fasta_path);
+        return rc == -3 ? SWM_ERR_OOM : SWM_ERR_IO;
+    }
+    swm_index *ix = nullptr;
+    rc = swm_index_build(seq, n, k, device, &ix);
+    free(seq);
+    if (rc == SWM_OK) {
+        rc = swm_index_save(ix, prefix, info, info_len);
+        swm_index_free(ix);
+    }
+    free(info);
+    return rc;
+}
+
+extern "C" int swm_index_open(const char *prefix, uint32_t k, int device, swm_index **out) {
+    if (!prefix || !out || k < 1 || k > 14) return SWM_ERR_ARG;
+    SWM_CUDA(cudaSetDevice(device));
+    const uint64_t nb = 1ull << (2 * k);
+    void *cnt = nullptr, *pos = nullptr, *ls = nullptr, *b2 = nullptr, *b3 = nullptr, *info = nullptr;
+    size_t ncnt = 0, npos = 0, nls = 0, nb2 = 0, nb3 = 0, ninfo = 0;
+    int rc = SWM_OK;
+    if (swmf_read(prefix, ".hash_count", &cnt, &ncnt) || swmf_read(prefix, ".positions", &pos, &npos) ||
+        swmf_read(prefix, ".pos_lseeds", &ls, &nls) || swmf_read(prefix, ".base_2bits", &b2, &nb2) ||
+        swmf_read(prefix, ".base_3bits", &b3, &nb3)) {
+        swm_set_error("cannot read index files under %s", prefix);
+        rc = SWM_ERR_IO;
+    }
+    uint64_t S = npos / 4;
+    if (rc == SWM_OK) {
+        uint64_t total = 0;
+        const uint32_t *c = (const uint32_t *)cnt;
+        if (ncnt == nb * 4)
+            for (uint64_t i = 0; i < nb; i++) total += c[i];
+        if (ncnt != nb * 4 || npos % 4 || nls != S * 2 || nb2 % 8 || total != S) {
+            swm_set_error("index files under %s are inconsistent (k=%u)", prefix, k);
+            rc = SWM_ERR_IO;
+        }
+    }
+    swm_index *ix = nullptr;
+    if (rc == SWM_OK) {
+        ix = (swm_index *)calloc(1, sizeof(swm_index));
+        if (!ix) rc = SWM_ERR_OOM;
+    }
+    if (rc == SWM_OK) {
+        ix->device = device;
+        ix->k = k;
+        ix->n_seeds = S;
+        ix->n_words2 = nb2 / 4;
+        ix->n_words3 = nb3 / 4;
+        ix->ref_length = (uint64_t)nb2 * 16; // mapper_mpe.c:288
+        ix->n = 32 * ix->n_words3;
+        if (swmf_read(prefix, ".ref_info", &info, &ninfo) == 0) {
+            uint64_t t = swmf_ref_info_total((const char *)info, ninfo);
+            if (t) ix->n = t;
+        }
+        uint32_t *d_tmp = nullptr;
+        if (dalloc(&ix->d_count, nb) || dalloc(&ix->d_off, nb + 1) || dalloc(&ix->d_pos, S + 8) ||
+            dalloc(&ix->d_lseed, S + 8) || dalloc(&ix->d_b2, ix->n_words2 + SWM_PAD_WORDS) ||
+            dalloc(&ix->d_b3, ix->n_words3 + SWM_PAD_WORDS) || dalloc(&d_tmp, swm_scan_tmp_words(nb))) {
+            rc = SWM_ERR_OOM;
+        } else if (cudaMemcpy(ix->d_count, cnt, nb * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+                   (S && cudaMemcpy(ix->d_pos, pos, S * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
+                   (S && cudaMemcpy(ix->d_lseed, ls, S * 2, cudaMemcpyHostToDevice) != cudaSuccess) ||
+                   (nb2 && cudaMemcpy(ix->d_b2, b2, nb2, cudaMemcpyHostToDevice) != cudaSuccess) ||
+                   (nb3 && cudaMemcpy(ix->d_b3, b3, nb3, cudaMemcpyHostToDevice) != cudaSuccess) ||
+                   cudaMemset(ix->d_pos + S, 0, 32) != cudaSuccess ||
+                   cudaMemset(ix->d_lseed + S, 0, 16) != cudaSuccess ||
+                   cudaMemset(ix->d_b2 + ix->n_words2, 0, SWM_PAD_WORDS * 4) != cudaSuccess ||
+                   cudaMemset(ix->d_b3 + ix->n_words3, 0, SWM_PAD_WORDS * 4) != cudaSuccess) {
+            swm_set_error("H2D of index under %s failed", prefix);
+            rc = SWM_ERR_CUDA;
+        } else {
+            // hash_offset rebuilt from the counts (mapper_mpe.c:250-255)
+            rc = swm_exclusive_scan(ix->d_count, ix->d_off, nullptr, nb, nb, d_tmp, nullptr, 0);
+            if (rc == SWM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = SWM_ERR_CUDA;
+        }
+        cudaFree(d_tmp);
+        if (rc != SWM_OK) {
+            index_release(ix);
+            ix = nullptr;
+        }
+    }
+    free(cnt);
+    free(pos);
+    free(ls);
+    free(b2);
+    free(b3);
+    free(info);
+    if (rc == SWM_OK) *out = ix;
+    return rc;
+}
+
+extern "C" void swm_index_free(swm_index *ix) {
+    if (!ix) return;
+    cudaSetDevice(ix->device);
+    index_release(ix);
+}

@@ -1,0 +1,1526 @@
+// swm_map.cu -- GB300 mapping pipeline for one block of reads.
+//
+// The reference maps one read at a time on each of 64 CPEs
+// (find_positions -> get_positions -> choose_seed / alignment_rmdup /
+// banded_myers / align_reads / put_cigar, mapper_cpe.c:2592-229). Here the
+// same per-(read, strand) semantics run as a sequence of data-parallel kernels
+// over a whole block, each sized to its natural unit of work:
+//
+//   k_seed     thread / item   read encodings, seed lookups, long-seed order,
+//                              flank codes            (mapper_cpe.c:1246-1401,
+//                                                      2451-2499)
+//   scan       chunk and element offsets per item
+//   k_plan     thread / item   the fetch schedule: 32-position chunks,
+//                              heap-ordered refills, batch boundaries
+//                                                     (mapper_cpe.c:2124-2419)
+//   k_cand     warp / batch    gather + position adjust + flank filter +
+//                              sort-unique            (mapper_cpe.c:1893-2123)
+//   scan       candidate offsets
+//   k_compact  warp / batch    dense candidate list
+//   k_verify   thread / cand   window, banded Myers, Hamming check or
+//                              traceback + CIGAR      (mapper_cpe.c:229-660,
+//                                                      1403-1435,1509-1586)
+//   k_records  thread / item   groups of 8, record flushes, dedup, primary
+//                              flag (count pass, scan, write pass)
+//                                                     (mapper_cpe.c:1437-1507,
+//                                                      1753-1860)
+//
+// All sizes flow through device memory, so the host queues the whole block
+// without synchronising; capacities are checked on the device and a block
+// whose work outgrew a buffer is re-run with larger buffers.
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "swm_common.cuh"
+
+// item = 2 * read + strand (cur_read, mapper_cpe.c:2628)
+
+enum { VR_FAIL = 0, VR_HAM = 1, VR_TB = 2, VR_INVALID = 3 };
+enum { OV_CHUNKS = 1, OV_ELEMS = 2, OV_CANDS = 4, OV_RECS = 8, OV_ARENA = 16, OV_BAD = 32 };
+enum {
+    ST_BATCHES = 0,
+    ST_CELLS,
+    ST_PASSED,
+    ST_LOCS,
+    ST_MAPPED,
+    ST_N
+};
+// device totals (u32), written by the scans
+enum { TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT_ARENA, TOT_FLAGS, TOT_N };
+
+#define ARENA_CAP_DEFAULT (1u << 20)
+
+struct MapBufs {
+    // per item
+    uint32_t *it_w;        // items * 32: [0..15] Myers planes, [16..31] Hamming planes
+    uint32_t *sel_start;   // items * 64
+    uint32_t *sel_count;   // items * 64
+    uint32_t *sel_meta;    // items * 64: base | shift << 16 | rl << 20 | rh << 24
+    uint8_t *it_nsel, *it_e;
+    uint32_t *it_nch, *it_nel, *it_nbat;
+    uint32_t *it_choff, *it_eloff; // items + 1
+    uint32_t *it_nrec, *it_nw, *it_nb;
+    uint32_t *it_recoff, *it_woff, *it_boff; // items + 1
+    // per chunk / batch slot (cap_chunks)
+    uint32_t *ch_g, *ch_meta;
+    uint32_t *bt_c0, *bt_c1, *bt_e0, *bt_item, *bt_cnt;
+    uint32_t *bt_coff; // cap_chunks + 1
+    // upper-bound candidates (cap_elems)
+    uint32_t *cand_ub;
+    // dense candidates (cap_cands)
+    uint32_t *cc_pos, *cc_item;
+    uint8_t *vr_flag;
+    uint32_t *vr_loc;
+    int32_t *vr_err, *vr_mloc;
+    uint16_t *vr_tlen;
+    uint8_t *vr_cig;  // cap_cands * SWM_CIGAR_SLOT
+    uint32_t *vr_aoff;
+    uint8_t *arena;   // long CIGAR texts
+    // records
+    uint32_t *out_w;  // cap_words
+    uint8_t *out_c;   // cap_bytes
+    uint32_t *rec_woff, *rec_boff, *rec_blen; // cap_recs
+    // bookkeeping
+    uint32_t *tot;    // TOT_N
+    unsigned long long *stat; // ST_N
+    uint32_t *scan_tmp;
+};
+
+struct swm_mapper {
+    swm_index *ix;
+    int device;
+    cudaStream_t st;
+    uint64_t max_reads;
+    uint64_t cap_items, cap_chunks, cap_elems, cap_cands, cap_recs, cap_words, cap_bytes, cap_arena;
+    uint64_t stride_cap;
+    MapBufs b;
+    // inputs (device) and pinned staging
+    char *d_reads;
+    uint32_t *d_lens;
+    uint8_t *d_e;
+    char *h_reads;
+    uint32_t *h_lens;
+    uint8_t *h_e;
+    // pinned result staging
+    uint32_t *h_w, *h_rw, *h_rb, *h_rl, *h_nrec;
+    uint8_t *h_c;
+    uint64_t h_cap_w, h_cap_c, h_cap_rw, h_cap_rb, h_cap_rl, h_cap_items;
+    uint32_t *h_tot;           // pinned copy of B.tot
+    unsigned long long *h_stat; // pinned copy of B.stat
+    // state of the block in flight / last block
+    const char *cur_reads;
+    const uint32_t *cur_lens;
+    const uint8_t *cur_e;
+    uint64_t cur_stride, cur_n;
+    uint32_t cur_errors;
+    int pending; // submitted, not yet waited
+    uint64_t h2d_pending; // bytes copied in for the block being mapped
+    int have_result;
+    uint32_t tot[TOT_N];
+    swm_map_stats stats;
+    cudaEvent_t ev[8];
+    float stage_ms[6];
+    uint64_t launches;
+};
+
+// ======================================================================
+// device helpers
+// ======================================================================
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned long long v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+    if (lane_id() == 0 && v) atomicAdd(dst, v);
+}
+
+// Encode one read base as get_seed_from_reads does (mapper_cpe.c:1260-1305):
+// 2-bit accumulator + lo/hi planes; anything but A/C/G/T encodes as C.
+__device__ __forceinline__ void enc_base(uint32_t *w, uint32_t &acc, uint32_t rp, char ch) {
+    uint32_t code = ch == 'A' ? 0u : ch == 'C' ? 1u : ch == 'G' ? 2u : ch == 'T' ? 3u : 1u;
+    acc |= code << ((rp % 16) * 2);
+    w[16 + (rp >> 5) * 2] |= (code & 1u) << (rp & 31);
+    w[16 + (rp >> 5) * 2 + 1] |= (code >> 1) << (rp & 31);
+    if (rp % 16 == 15) {
+        w[rp / 16] = acc;
+        acc = 0;
+    }
+}
+
+// get_seed_from_reads with its tail encoder (mapper_cpe.c:1246-1364).
+__device__ uint32_t read_seed(const char *s, uint32_t *w, uint32_t &acc, uint32_t pre, uint32_t k, uint32_t j,
+                              uint32_t L) {
+    uint32_t i = (j % SWM_SEED_STEP == 0) ? 0 : k - 1;
+    const uint32_t base = (j / SWM_SEED_STEP) * (k + SWM_SEED_STEP - 1) + j % SWM_SEED_STEP;
+    uint32_t seed = pre;
+    uint32_t rp = base + i;
+    for (; i < k; i++) {
+        rp = base + i;
+        char ch = s[rp];
+        uint32_t sc = ch == 'A' ? 0u : ch == 'C' ? 1u : ch == 'G' ? 2u : ch == 'T' ? 3u : (i % 4);
+        seed = (seed >> 2) | (sc << ((k - 1) * 2));
+        enc_base(w, acc, rp, ch);
+    }
+    if (L - rp < k) {
+        for (; rp < L; rp++) enc_base(w, acc, rp, s[rp]);
+        w[(rp - 1) / 16] = acc;
+    }
+    return seed;
+}
+
+__device__ __forceinline__ char comp_base(char c) {
+    return c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : c == 'T' ? 'A' : c;
+}
+
+// compress the even bits of x (16 of them) into the low half
+__device__ __forceinline__ uint32_t even_bits(uint32_t x) {
+    x &= 0x55555555u;
+    x = (x | (x >> 1)) & 0x33333333u;
+    x = (x | (x >> 2)) & 0x0f0f0f0fu;
+    x = (x | (x >> 4)) & 0x00ff00ffu;
+    x = (x | (x >> 8)) & 0x0000ffffu;
+    return x;
+}
+
+// True once any earlier stage of this block ran out of a buffer or met an
+// input outside the envelope: later stages then skip their work (their
+// inputs may be partial) and the host re-runs or rejects the block.
+__device__ __forceinline__ bool block_failed(const MapBufs &B, uint64_t cap_chunks, uint64_t cap_elems,
+                                             uint64_t cap_cands) {
+    return B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems ||
+           B.tot[TOT_CANDS] > cap_cands;
+}
+
+// ======================================================================
+// k_seed: one thread per (read, strand)
+// ======================================================================
+
+__global__ void __launch_bounds__(128) k_seed(const char *__restrict__ reads, const uint32_t *__restrict__ lens,
+                                              uint64_t stride, uint32_t nreads, uint32_t e_glob,
+                                              const uint8_t *__restrict__ e_arr, const uint32_t *__restrict__ off,
+                                              uint32_t k, MapBufs B) {
+    const uint32_t nitems = 2 * nreads;
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
+        const uint32_t r = item >> 1, strand = item & 1;
+        const uint32_t L = lens[r];
+        const uint32_t e = e_arr ? e_arr[r] : e_glob;
+        const uint32_t klong0 = k + SWM_SEED_STEP - 1;
+        if (L > SWM_MAX_READ_LEN || L > stride || L / klong0 > 16 || e > SWM_MAX_ERRORS) {
+            // outside the envelope: no work for this item, and the block fails
+            atomicOr(&B.tot[TOT_FLAGS], OV_BAD);
+            B.it_nsel[item] = 0;
+            B.it_e[item] = 0;
+            B.it_nch[item] = 0;
+            B.it_nel[item] = 0;
+            continue;
+        }
+        const char *src = reads + (uint64_t)r * stride;
+        char s[SWM_MAX_READ_LEN + 2];
+        if (strand == 0) {
+            for (uint32_t i = 0; i < L; i++) s[i] = src[i];
+        } else {
+            for (uint32_t i = 0; i < L; i++) s[L - 1 - i] = comp_base(src[i]); // reverse_read, 2429-2450
+        }
+        uint32_t w[32];
+#pragma unroll
+        for (int i = 0; i < 32; i++) w[i] = 0;
+        const uint32_t klong = k + SWM_SEED_STEP - 1;
+        const uint32_t nl = L / klong, ns_all = nl * SWM_SEED_STEP;
+        uint32_t cnt[SWM_MAX_SEL], start[SWM_MAX_SEL];
+        uint32_t acc = 0, seed = 0;
+        for (uint32_t j = 0; j < ns_all; j++) { // choose_seed, 1365-1384
+            seed = read_seed(s, w, acc, seed, k, j, L);
+            uint32_t o0 = off[seed], o1 = off[seed + 1];
+            start[j] = o0;
+            cnt[j] = o1 - o0;
+        }
+        uint32_t icount[16], iindex[16];
+        for (uint32_t j = 0; j < 16; j++) {
+            icount[j] = 0;
+            iindex[j] = j;
+        }
+        for (uint32_t j = 0; j < ns_all; j++) icount[j / SWM_SEED_STEP] += cnt[j];
+        for (uint32_t j = 0; j < nl; j++) // exchange sort, 1391-1399
+            for (uint32_t m = j + 1; m < nl; m++)
+                if (icount[j] > icount[m]) {
+                    uint32_t t = icount[j];
+                    icount[j] = icount[m];
+                    icount[m] = t;
+                    t = iindex[j];
+                    iindex[j] = iindex[m];
+                    iindex[m] = t;
+                }
+        // flank codes of the read (set_read_long_seeds, 2451-2499)
+        uint8_t res[128];
+        const uint32_t lmask = (1u << klong) - 1, rmask = (1u << (SWM_SEED_STEP - 1)) - 1;
+        for (uint32_t i = 0; i < nl; i++) {
+            uint32_t o = i * klong, wj = o >> 5, sh = o & 31, nx = 16 + (wj + 1) * 2;
+            uint32_t l = swm_fsr(w[16 + wj * 2], nx < 32 ? w[nx] : 0u, sh) & lmask;
+            uint32_t h = swm_fsr(w[16 + wj * 2 + 1], nx + 1 < 32 ? w[nx + 1] : 0u, sh) & lmask;
+            for (uint32_t j = 0; j < SWM_SEED_STEP; j++) {
+                uint32_t sft = k + j, m = (1u << j) - 1;
+                res[2 * (SWM_SEED_STEP * i + j)] = (uint8_t)(((l & m) | ((l >> sft) << j)) & rmask);
+                res[2 * (SWM_SEED_STEP * i + j) + 1] = (uint8_t)(((h & m) | ((h >> sft) << j)) & rmask);
+            }
+        }
+        // selected seed slots: the (e + 1) rarest long seeds x 4 shifts
+        // (alignment_rmdup, 2194-2196); slots past nl read count 0
+        const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
+        const uint32_t ns = nsl * SWM_SEED_STEP;
+        uint32_t nch = 0, nel = 0;
+        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+        for (uint32_t i = 0; i < ns; i++) {
+            uint32_t sidx = iindex[i / SWM_SEED_STEP] * SWM_SEED_STEP + i % SWM_SEED_STEP;
+            uint32_t c = cnt[sidx];
+            uint32_t base = iindex[i / SWM_SEED_STEP] * klong + i % SWM_SEED_STEP;
+            uint32_t shift = SWM_SEED_STEP - 1 - sidx % SWM_SEED_STEP;
+            B.sel_start[sb + i] = start[sidx];
+            B.sel_count[sb + i] = c;
+            B.sel_meta[sb + i] = base | (shift << 16) | ((uint32_t)res[2 * sidx] << 20) |
+                                 ((uint32_t)res[2 * sidx + 1] << 24);
+            nch += (c + SWM_PER_FETCH - 1) / SWM_PER_FETCH;
+            nel += c;
+        }
+        // Myers planes from the 2-bit words, Hamming planes as encoded
+        uint32_t *ow = B.it_w + (uint64_t)item * 32;
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            uint32_t a0 = w[2 * b], a1 = w[2 * b + 1];
+            ow[2 * b] = even_bits(a0) | (even_bits(a1) << 16);
+            ow[2 * b + 1] = even_bits(a0 >> 1) | (even_bits(a1 >> 1) << 16);
+        }
+#pragma unroll
+        for (int i = 16; i < 32; i++) ow[i] = w[i];
+        B.it_nsel[item] = (uint8_t)ns;
+        B.it_e[item] = (uint8_t)e;
+        B.it_nch[item] = nch;
+        B.it_nel[item] = nel;
+    }
+}
+
+// ======================================================================
+// k_plan: the fetch schedule of alignment_rmdup, one thread per item
+// ======================================================================
+
+__global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const uint32_t *__restrict__ pos, MapBufs B,
+                                              uint64_t cap_chunks, uint64_t cap_elems) {
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
+        const uint32_t nch = B.it_nch[item];
+        const uint32_t cb = B.it_choff[item], eb = B.it_eloff[item];
+        if (nch == 0) {
+            B.it_nbat[item] = 0;
+            continue;
+        }
+        if ((uint64_t)cb + nch > cap_chunks) {
+            atomicOr(&B.tot[TOT_FLAGS], OV_CHUNKS);
+            B.it_nbat[item] = 0;
+            for (uint64_t q = cb; q < (uint64_t)cb + nch && q < cap_chunks; q++) {
+                B.bt_c0[q] = 0;
+                B.bt_c1[q] = 0;
+                B.bt_item[q] = item;
+            }
+            continue;
+        }
+        if ((uint64_t)eb + B.it_nel[item] > cap_elems) {
+            atomicOr(&B.tot[TOT_FLAGS], OV_ELEMS);
+            B.it_nbat[item] = 0;
+            for (uint32_t q = 0; q < nch; q++) {
+                B.bt_c0[cb + q] = 0;
+                B.bt_c1[cb + q] = 0;
+                B.bt_item[cb + q] = item;
+            }
+            continue;
+        }
+        const uint32_t ns = B.it_nsel[item];
+        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+        uint32_t pc[SWM_MAX_SEL], sst[SWM_MAX_SEL], scn[SWM_MAX_SEL];
+        uint32_t hloc[SWM_MAX_SEL + 8], hidx[SWM_MAX_SEL + 8];
+        uint32_t hs = 0;
+        uint32_t c = 0, e = 0, b = 0, bc0 = 0, be0 = 0, npos = 0, runs = 0;
+#define EMIT(i_, get_)                                                    \
+    do {                                                                  \
+        B.ch_g[cb + c] = sst[i_] + pc[i_];                                \
+        B.ch_meta[cb + c] = (get_) | ((i_) << 8);                         \
+        c++;                                                              \
+        e += (get_);                                                      \
+        pc[i_] += (get_);                                                 \
+        npos += (get_);                                                   \
+        runs++;                                                           \
+    } while (0)
+        for (uint32_t i = 0; i < ns; i++) { // initial fetch, 2194-2236
+            sst[i] = B.sel_start[sb + i];
+            scn[i] = B.sel_count[sb + i];
+            pc[i] = 0;
+            uint32_t get = scn[i] > SWM_PER_FETCH ? SWM_PER_FETCH : scn[i];
+            if (get) EMIT(i, get);
+        }
+        for (uint32_t i = 0; i < ns; i++) { // seeds_heap_insert, 1919-1935
+            if (pc[i] != scn[i]) {
+                hs++;
+                hloc[hs] = pos[sst[i] + pc[i] - 1];
+                hidx[hs] = i;
+                uint32_t q = hs;
+                while (q > 1) {
+                    uint32_t t = q / 2;
+                    if (hloc[t] > hloc[q]) {
+                        uint32_t a = hloc[t];
+                        hloc[t] = hloc[q];
+                        hloc[q] = a;
+                        a = hidx[t];
+                        hidx[t] = hidx[q];
+                        hidx[q] = a;
+                    } else break;
+                    q = t;
+                }
+            }
+        }
+        for (;;) { // 2261-2419
+            if (hs > 0 && npos + SWM_PER_FETCH <= SWM_BATCH_POSITIONS && 1 + 2 * runs < SWM_MAX_RUNS_BLOCK) {
+                uint32_t i = hidx[1];
+                uint32_t left = scn[i] - pc[i];
+                uint32_t get = left > SWM_PER_FETCH ? SWM_PER_FETCH : left;
+                EMIT(i, get);
+                // seeds_heap_pop_and_insert, 1936-1962 (loop bound i * 2 < size)
+                if (pc[i] == scn[i]) {
+                    hloc[1] = hloc[hs];
+                    hidx[1] = hidx[hs];
+                    hs--;
+                } else {
+                    hloc[1] = pos[sst[i] + pc[i] - 1];
+                }
+                uint32_t q = 1;
+                while (q * 2 < hs) {
+                    uint32_t t = q * 2;
+                    if (q * 2 + 1 <= hs && hloc[q * 2] > hloc[q * 2 + 1]) t = q * 2 + 1;
+                    if (hloc[t] < hloc[q]) {
+                        uint32_t a = hloc[t];
+                        hloc[t] = hloc[q];
+                        hloc[q] = a;
+                        a = hidx[t];
+                        hidx[t] = hidx[q];
+                        hidx[q] = a;
+                    } else break;
+                    q = t;
+                }
+            }
+            if (npos + SWM_PER_FETCH > SWM_BATCH_POSITIONS || hs == 0 || 1 + 2 * runs >= SWM_MAX_RUNS_BLOCK) {
+                if (npos > 0) {
+                    const uint32_t slot = cb + b;
+                    B.bt_c0[slot] = cb + bc0;
+                    B.bt_c1[slot] = cb + c;
+                    B.bt_e0[slot] = eb + be0;
+                    B.bt_item[slot] = item;
+                    b++;
+                }
+                bc0 = c;
+                be0 = e;
+                npos = 0;
+                runs = 0;
+                if (hs == 0) break;
+            }
+        }
+#undef EMIT
+        for (uint32_t q = b; q < nch; q++) {
+            B.bt_c0[cb + q] = 0;
+            B.bt_c1[cb + q] = 0;
+            B.bt_item[cb + q] = item;
+        }
+        B.it_nbat[item] = b;
+    }
+}
+
+// ======================================================================
+// k_cand: one warp per batch slot -- gather, adjust, filter, sort-unique
+// ======================================================================
+
+#define CAND_WARPS 4
+
+__device__ __forceinline__ void warp_sort_small(uint32_t &v) {
+    const uint32_t lane = lane_id();
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            uint32_t w = __shfl_xor_sync(0xffffffffu, v, stride);
+            bool up = ((lane & size) == 0);
+            bool lower = ((lane & stride) == 0);
+            v = (lower == up) ? min(v, w) : max(v, w);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(const uint32_t *__restrict__ pos,
+                                                          const uint16_t *__restrict__ lseed, MapBufs B,
+                                                          uint64_t cap_chunks) {
+    __shared__ uint32_t sbuf[CAND_WARPS][SWM_BATCH_POSITIONS];
+    if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks) return;
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
+    uint32_t *buf = sbuf[wib];
+    const uint64_t nslots_all = B.tot[TOT_CHUNKS];
+    const uint64_t nslots = nslots_all < cap_chunks ? nslots_all : cap_chunks;
+    const uint32_t lt = (1u << lane) - 1;
+    for (uint64_t s = (uint64_t)blockIdx.x * CAND_WARPS + wib; s < nslots; s += (uint64_t)gridDim.x * CAND_WARPS) {
+        const uint32_t c0 = B.bt_c0[s], c1 = B.bt_c1[s];
+        if (c0 == c1) {
+            if (lane == 0) B.bt_cnt[s] = 0;
+            continue;
+        }
+        const uint32_t item = B.bt_item[s], e0 = B.bt_e0[s];
+        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+        uint32_t kept = 0, j = 0;
+        for (uint32_t c = c0; c < c1; c++) {
+            const uint32_t g = B.ch_g[c], meta = B.ch_meta[c];
+            const uint32_t len = meta & 0xffu, sel = meta >> 8;
+            const uint32_t sm = B.sel_meta[sb + sel];
+            const uint32_t base = sm & 0xffffu, shift = (sm >> 16) & 0xfu, rl = (sm >> 20) & 0xfu,
+                           rh = (sm >> 24) & 0xfu;
+            bool ok = false;
+            uint32_t p = 0;
+            if (lane < len) {
+                uint32_t raw = pos[g + lane];
+                uint32_t ls = lseed[g + lane];
+                p = raw > base ? raw - base : 0u;  // adjust_ref_pos_rmdup, 1893-1917
+                uint32_t rs = (((ls >> shift) ^ rl) | ((ls >> (6 + shift)) ^ rh)) & 7u; // long_seeds_filter, 2107-2112
+                ok = (rs == 0) && (j + lane != 0); // element 0 of the batch is dropped (2113)
+            }
+            uint32_t m = __ballot_sync(0xffffffffu, ok);
+            if (ok) buf[kept + __popc(m & lt)] = p;
+            kept += __popc(m);
+            j += len;
+        }
+        __syncwarp();
+        uint32_t u = 0;
+        uint32_t *dst = B.cand_ub + e0;
+        if (kept <= 32) {
+            uint32_t v = lane < kept ? buf[lane] : 0xffffffffu;
+            warp_sort_small(v);
+            uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
+            bool keep = lane < kept && (lane == 0 || prev != v);
+            uint32_t m = __ballot_sync(0xffffffffu, keep);
+            if (keep) dst[__popc(m & lt)] = v;
+            u = __popc(m);
+        } else {
+            uint32_t n2 = 64;
+            while (n2 < kept) n2 <<= 1;
+            for (uint32_t i = kept + lane; i < n2; i += 32) buf[i] = 0xffffffffu;
+            __syncwarp();
+            for (uint32_t size = 2; size <= n2; size <<= 1) {
+                for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                    for (uint32_t i = lane; i < n2 / 2; i += 32) {
+                        uint32_t lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
+                        bool up = ((lo & size) == 0);
+                        uint32_t a = buf[lo], d = buf[hi];
+                        if ((a > d) == up) {
+                            buf[lo] = d;
+                            buf[hi] = a;
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+            for (uint32_t i0 = 0; i0 < kept; i0 += 32) {
+                uint32_t i = i0 + lane;
+                bool keep = i < kept && (i == 0 || buf[i - 1] != buf[i]);
+                uint32_t m = __ballot_sync(0xffffffffu, keep);
+                if (keep) dst[u + __popc(m & lt)] = buf[i];
+                u += __popc(m);
+            }
+        }
+        if (lane == 0) B.bt_cnt[s] = u;
+        __syncwarp();
+    }
+}
+
+__global__ void k_compact(MapBufs B, uint64_t cap_chunks, uint64_t cap_elems, uint64_t cap_cands) {
+    if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint32_t lane = lane_id();
+    const uint64_t nslots_all = B.tot[TOT_CHUNKS];
+    const uint64_t nslots = nslots_all < cap_chunks ? nslots_all : cap_chunks;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslots; s += nwarps) {
+        const uint32_t n = B.bt_cnt[s];
+        if (!n) continue;
+        const uint32_t o = B.bt_coff[s], e0 = B.bt_e0[s], item = B.bt_item[s];
+        if ((uint64_t)o + n > cap_cands) {
+            if (lane == 0) atomicOr(&B.tot[TOT_FLAGS], OV_CANDS);
+            continue;
+        }
+        for (uint32_t j = lane; j < n; j += 32) {
+            B.cc_pos[o + j] = B.cand_ub[e0 + j];
+            B.cc_item[o + j] = item;
+        }
+    }
+}
+
+// ======================================================================
+// k_verify: one thread per candidate
+// ======================================================================
+
+// adjust_ref_len + pos_start (mapper_cpe.c:1403-1435) with the reference's
+// integer types; returns 0xffffffff when the window is rejected.
+__device__ __forceinline__ uint32_t window_start(uint32_t base_pos, uint32_t L, uint32_t e, uint64_t ref_length,
+                                                 uint32_t *rl_out) {
+    const uint64_t dist_error = e;
+    uint64_t shift_tmp = e;
+    uint64_t ref_len = (uint64_t)L + 2 * shift_tmp;
+    if (base_pos <= shift_tmp) {
+        shift_tmp = base_pos;
+        ref_len -= (dist_error - base_pos);
+    }
+    int64_t front = (int64_t)ref_length - (int64_t)((uint64_t)base_pos - dist_error);
+    int64_t back = (int64_t)((uint64_t)(uint32_t)(base_pos + L) + dist_error) - (int64_t)ref_length;
+    if (front > back) {
+        if (back >= 0) ref_len -= (uint64_t)(back + 1);
+    } else {
+        shift_tmp = dist_error - (uint64_t)front - 1;
+        ref_len -= (uint64_t)front;
+    }
+    uint32_t rl = (uint32_t)ref_len;
+    *rl_out = rl;
+    if ((uint64_t)rl < (uint64_t)L - dist_error) return 0xffffffffu;
+    return (uint32_t)((uint64_t)base_pos - shift_tmp);
+}
+
+// Banded Myers / Hyyro recurrence of banded_myers_simd (mapper_cpe.c:519-660)
+// with the pattern-match word built from window bit planes: at read base i
+// bit j of eq is [window[i + j] == read[i]] for j <= 2e, the same word the
+// reference keeps in peq[read[i]]. Returns (error, location) exactly as the
+// reference's final scan (634-650).
+__device__ __forceinline__ int myers_scan(const uint32_t *WL, const uint32_t *WH, const uint32_t *RW, uint32_t L,
+                                          uint32_t e, uint32_t rl, int *loc_out) {
+    const uint32_t band = 2 * e + 1;
+    const uint32_t MASK = (1u << band) - 1u;
+    uint32_t vp = 0, vn = 0, ones = 0;
+    const uint32_t nblk = (L + 31) >> 5;
+    for (uint32_t b = 0; b < nblk; b++) {
+        const uint32_t wl0 = WL[b], wl1 = WL[b + 1], wh0 = WH[b], wh1 = WH[b + 1];
+        const uint32_t rlw = RW[2 * b], rhw = RW[2 * b + 1];
+        const uint32_t steps = min(32u, L - 32 * b);
+        uint32_t acc = 0;
+        if (steps == 32) {
+#pragma unroll
+            for (uint32_t t = 0; t < 32; t++) {
+                const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
+                const uint32_t mL = (uint32_t)((int32_t)(rlw << (31 - t)) >> 31);
+                const uint32_t mH = (uint32_t)((int32_t)(rhw << (31 - t)) >> 31);
+                const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
+                uint32_t x = eq | vn;
+                const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;
+                const uint32_t hn = vp & d0;
+                const uint32_t hp = vn | ~(vp | d0);
+                x = d0 >> 1;
+                vn = x & hp;
+                vp = hn | ~(x | hp);
+                acc = __funnelshift_r(acc, d0, 1);
+            }
+        } else {
+            for (uint32_t t = 0; t < steps; t++) {
+                const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
+                const uint32_t mL = 0u - ((rlw >> t) & 1u), mH = 0u - ((rhw >> t) & 1u);
+                const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
+                uint32_t x = eq | vn;
+                const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;
+                const uint32_t hn = vp & d0;
+                const uint32_t hp = vn | ~(vp | d0);
+                x = d0 >> 1;
+                vn = x & hp;
+                vp = hn | ~(x | hp);
+                acc = __funnelshift_r(acc, d0, 1);
+            }
+        }
+        ones += __popc(acc);
+    }
+    int err = (int)L - (int)ones;
+    const int last_high = (int)rl - (int)L;
+    const int site = (int)L - 1;
+    int location = -1, error = SWM_MAXERROR;
+    if (err <= (int)e && err < error) {
+        error = err;
+        location = site;
+    }
+    for (int i = 0; i < last_high; i++) {
+        err += (int)((vp >> i) & 1u);
+        err -= (int)((vn >> i) & 1u);
+        if (err <= (int)e && err < error) {
+            error = err;
+            location = site + i + 1;
+        }
+    }
+    *loc_out = location;
+    return error;
+}
+
+// Same recurrence keeping D0 / HP per read base for the traceback
+// (align_reads, mapper_cpe.c:288-362).
+__device__ void myers_history(const uint32_t *WL, const uint32_t *WH, const uint32_t *RW, uint32_t L, uint32_t e,
+                              uint32_t *d0h, uint32_t *hph) {
+    const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
+    uint32_t vp = 0, vn = 0;
+    for (uint32_t i = 0; i < L; i++) {
+        const uint32_t b = i >> 5, t = i & 31;
+        const uint32_t wls = __funnelshift_r(WL[b], WL[b + 1], t), whs = __funnelshift_r(WH[b], WH[b + 1], t);
+        const uint32_t mL = 0u - ((RW[2 * b] >> t) & 1u), mH = 0u - ((RW[2 * b + 1] >> t) & 1u);
+        const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
+        uint32_t x = eq | vn;
+        const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;
+        const uint32_t hn = vp & d0;
+        const uint32_t hp = vn | ~(vp | d0);
+        x = d0 >> 1;
+        vn = x & hp;
+        vp = hn | ~(x | hp);
+        d0h[i] = d0;
+        hph[i] = hp;
+    }
+}
+
+// sprint_length (mapper_cpe.c:214-228) including its signed-char digit:
+// '0' + (char)v % 10 with the cast binding first.
+__device__ __forceinline__ int put_len(uint8_t *p, uint32_t v) {
+    int n = 0;
+    for (uint32_t t = v; t; t /= 10) n++;
+    for (int i = n - 1; i >= 0; i--) {
+        int b = (int)(v & 0xffu);
+        if (b >= 128) b -= 256;
+        p[i] = (uint8_t)('0' + b % 10);
+        v /= 10;
+    }
+    return n;
+}
+
+#define TB_TEXT_MAX 2304 // >= 4 bytes x every route entry a bounded walk can make
+
+__global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ lens, const uint32_t *__restrict__ b2,
+                                                uint64_t b2_words, uint64_t ref_length, MapBufs B,
+                                                uint64_t cap_chunks, uint64_t cap_elems, uint64_t cap_cands,
+                                                uint64_t cap_arena) {
+    if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint64_t nc_all = B.tot[TOT_CANDS];
+    const uint64_t nc = nc_all < cap_cands ? nc_all : cap_cands;
+    unsigned long long cells = 0, passed = 0;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t item = B.cc_item[c], p = B.cc_pos[c];
+        const uint32_t L = lens[item >> 1], e = B.it_e[item];
+        uint32_t rl;
+        const uint32_t ws = window_start(p, L, e, ref_length, &rl);
+        if (ws == 0xffffffffu) {
+            B.vr_flag[c] = VR_INVALID;
+            B.vr_err[c] = SWM_MAXERROR;
+            B.vr_mloc[c] = -1;
+            continue;
+        }
+        // aligned window planes (shift_ref_pos_v, 1509-1586)
+        uint32_t WL[SWM_WIN_WORDS], WH[SWM_WIN_WORDS];
+        const uint64_t w0 = (uint64_t)(ws >> 5) * 2;
+        const uint32_t sh = ws & 31;
+        const uint32_t nw = (L + 2 * e + 31) / 32 + 2;
+        uint32_t plo = (w0 < b2_words) ? b2[w0] : 0u, phi = (w0 + 1 < b2_words) ? b2[w0 + 1] : 0u;
+        for (uint32_t j = 0; j < SWM_WIN_WORDS; j++) {
+            uint32_t nlo = 0, nhi = 0;
+            if (j < nw) {
+                const uint64_t q = w0 + 2 * j + 2;
+                nlo = q < b2_words ? b2[q] : 0u;
+                nhi = q + 1 < b2_words ? b2[q + 1] : 0u;
+            }
+            WL[j] = swm_fsr(plo, nlo, sh);
+            WH[j] = swm_fsr(phi, nhi, sh);
+            plo = nlo;
+            phi = nhi;
+        }
+        const uint32_t *RW = B.it_w + (uint64_t)item * 32;
+        uint32_t rw[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) rw[i] = RW[i];
+        int loc;
+        const int err = myers_scan(WL, WH, rw, L, e, rl, &loc);
+        cells += (unsigned long long)L * (2 * e + 1);
+        B.vr_err[c] = err;
+        B.vr_mloc[c] = loc;
+        if (err > (int)e) {
+            B.vr_flag[c] = VR_FAIL;
+            continue;
+        }
+        passed++;
+        // Hamming shortcut (align_reads, 252-287)
+        int start = loc - (int)L + 1;
+        int ham = 0;
+        for (uint32_t ii = 0; ii * 32 < L; ii++) {
+            uint32_t mask = 0xffffffffu;
+            if ((ii + 1) * 32 > L) mask >>= (32 - (L - ii * 32));
+            const uint32_t lref = swm_fsr(WL[ii], WL[ii + 1], (uint32_t)start);
+            const uint32_t href = swm_fsr(WH[ii], WH[ii + 1], (uint32_t)start);
+            const uint32_t x = ((RW[16 + 2 * ii + 1] ^ href) | (RW[16 + 2 * ii] ^ lref)) & mask;
+            ham += __popc(x);
+        }
+        uint8_t *slot = B.vr_cig + c * SWM_CIGAR_SLOT;
+        if (ham == err) {
+            uint8_t txt[8];
+            int n = put_len(txt, L);
+            txt[n++] = 'M';
+            slot[0] = (uint8_t)ham;
+            slot[1] = (uint8_t)n;
+            for (int i = 0; i < n; i++) slot[2 + i] = txt[i];
+            B.vr_tlen[c] = (uint16_t)n;
+            B.vr_loc[c] = ws + (uint32_t)start + 1;
+            B.vr_flag[c] = VR_HAM;
+            continue;
+        }
+        // traceback (align_reads, 288-509)
+        uint32_t d0h[SWM_MAX_READ_LEN], hph[SWM_MAX_READ_LEN];
+        myers_history(WL, WH, rw, L, e, d0h, hph);
+        int match_site = loc;
+        int search_site = match_site - ((int)L - 1);
+        int i = (int)L - 1, sum_err = 0, jj = 1;
+        int pre_size = 1;
+        char pre_char = 'N';
+        uint16_t rsz[3 * SWM_MAX_READ_LEN + 64];
+        char rch[3 * SWM_MAX_READ_LEN + 64];
+#define TBBIT(arr, ii_, s_) (((s_) >= 0 && (s_) < 32) ? (((arr)[ii_] >> (s_)) & 1u) : 0u)
+#define TBREF(m_) (((WL[(m_) >> 5] >> ((m_) & 31)) & 1u) | (((WH[(m_) >> 5] >> ((m_) & 31)) & 1u) << 1))
+#define TBREAD(r_) (((rw[2 * ((r_) >> 5)] >> ((r_) & 31)) & 1u) | (((rw[2 * ((r_) >> 5) + 1] >> ((r_) & 31)) & 1u) << 1))
+        if (TBBIT(d0h, i, search_site) && TBREF(match_site) == TBREAD(i)) {
+            i--; pre_size = 1; pre_char = 'M'; match_site--;
+        } else if (!TBBIT(d0h, i, search_site) && TBREF(match_site) != TBREAD(i)) {
+            i--; pre_size = 1; pre_char = 'S'; match_site--; sum_err++;
+        } else if (TBBIT(hph, i, search_site)) {
+            i--; search_site++; pre_size = 1; pre_char = 'S'; sum_err++; start++;
+        } else {
+            search_site--; pre_size = 1; pre_char = 'D'; match_site--; sum_err++; start--;
+        }
+        while (i >= 0) {
+            if (sum_err == err) break;
+            if (match_site < 0) break; // defined stop below the window start
+            if (TBBIT(d0h, i, search_site) && TBREF(match_site) == TBREAD(i)) {
+                i--; match_site--;
+                if (pre_char != 'M') { rsz[jj] = (uint16_t)pre_size; rch[jj++] = pre_char; pre_size = 1; pre_char = 'M'; }
+                else pre_size++;
+            } else if (!TBBIT(d0h, i, search_site) && TBREF(match_site) != TBREAD(i)) {
+                i--; match_site--; sum_err++;
+                if (pre_char != 'S') { rsz[jj] = (uint16_t)pre_size; rch[jj++] = pre_char; pre_size = 1; pre_char = 'S'; }
+                else pre_size++;
+            } else if (TBBIT(hph, i, search_site)) {
+                i--; search_site++; sum_err++;
+                if (pre_char != 'I') { rsz[jj] = (uint16_t)pre_size; rch[jj++] = pre_char; pre_size = 1; pre_char = 'I'; }
+                else pre_size++;
+                start++;
+            } else {
+                search_site--; match_site--; sum_err++;
+                if (pre_char != 'D') { rsz[jj] = (uint16_t)pre_size; rch[jj++] = pre_char; pre_size = 1; pre_char = 'D'; }
+                else pre_size++;
+                start--;
+            }
+        }
+#undef TBBIT
+#undef TBREF
+#undef TBREAD
+        rsz[jj] = (uint16_t)pre_size;
+        rch[jj++] = pre_char;
+        if (i >= 0) {
+            rsz[jj] = (uint16_t)(i + 1);
+            rch[jj++] = 'M';
+        }
+        uint8_t txt[TB_TEXT_MAX];
+        int n = 0;
+        for (jj = jj - 1; jj > 0; jj--) {
+            if (n > TB_TEXT_MAX - 8) break;
+            if (rch[jj] == 'M' || rch[jj] == 'S') {
+                int smv = 0;
+                while (jj > 0 && (rch[jj] == 'M' || rch[jj] == 'S')) {
+                    smv += rsz[jj];
+                    jj--;
+                }
+                jj++;
+                n += put_len(txt + n, (uint32_t)smv);
+                txt[n++] = 'M';
+            } else {
+                n += put_len(txt + n, rsz[jj]);
+                txt[n++] = (uint8_t)rch[jj];
+            }
+        }
+        slot[0] = (uint8_t)err;
+        slot[1] = (uint8_t)n;
+        if (n <= SWM_CIGAR_SLOT - 2) {
+            for (int q = 0; q < n; q++) slot[2 + q] = txt[q];
+        } else {
+            uint32_t at = atomicAdd(&B.tot[TOT_ARENA], (uint32_t)n);
+            if ((uint64_t)at + n <= cap_arena) {
+                for (int q = 0; q < n; q++) B.arena[at + q] = txt[q];
+                B.vr_aoff[c] = at;
+            } else {
+                atomicOr(&B.tot[TOT_FLAGS], OV_ARENA);
+            }
+        }
+        B.vr_tlen[c] = (uint16_t)n;
+        B.vr_loc[c] = ws + (uint32_t)start + 1;
+        B.vr_flag[c] = VR_TB;
+    }
+    warp_add_u64(&B.stat[ST_CELLS], cells);
+    warp_add_u64(&B.stat[ST_PASSED], passed);
+}
+
+// ======================================================================
+// k_records: groups of 8, record flushes, dedup, primary flag
+// ======================================================================
+
+template <bool WRITE>
+__global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
+                                                 uint64_t cap_cands, uint64_t cap_recs, uint64_t cap_words,
+                                                 uint64_t cap_bytes) {
+    if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    unsigned long long locs_total = 0, mapped = 0;
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
+        const uint32_t s0 = B.it_choff[item], nb = B.it_nbat[item];
+        uint32_t num = 0, len = 0, last = 0, mainf = 1, nrec = 0, nw = 0, nby = 0;
+        uint32_t recbase = 0, wbase = 0, bbase = 0;
+        bool ok = true;
+        if (WRITE) {
+            recbase = B.it_recoff[item];
+            wbase = B.it_woff[item];
+            bbase = B.it_boff[item];
+            ok = (uint64_t)recbase + B.it_nrec[item] <= cap_recs && (uint64_t)wbase + B.it_nw[item] <= cap_words &&
+                 (uint64_t)bbase + B.it_nb[item] <= cap_bytes;
+            if (!ok) atomicOr(&B.tot[TOT_FLAGS], OV_RECS);
+        }
+        uint32_t wrec = wbase, bcur = bbase;
+        auto put = [&]() { // put_cigar, 1437-1507
+            if (num > 0) {
+                if (WRITE && ok) {
+                    B.out_w[wrec] = item;
+                    B.out_w[wrec + 1] = num | (mainf ? (1u << 31) : 0u);
+                    B.rec_woff[recbase + nrec] = wrec;
+                    B.rec_boff[recbase + nrec] = bcur - len;
+                    B.rec_blen[recbase + nrec] = len;
+                }
+                mainf = 0;
+                nrec++;
+                nw += 2 + num;
+                nby += len;
+                wrec += 2 + num;
+                locs_total += num;
+            }
+            num = 0;
+            len = 0;
+        };
+        for (uint32_t s = s0; s < s0 + nb; s++) {
+            const uint32_t cbeg = B.bt_coff[s], cn = B.bt_cnt[s];
+            uint32_t g = 0;
+            for (uint32_t c = cbeg; c < cbeg + cn; c++) {
+                const uint8_t f = B.vr_flag[c];
+                if (f == VR_INVALID) continue;
+                if (f == VR_HAM || f == VR_TB) {
+                    const uint32_t loc = B.vr_loc[c];
+                    if (f == VR_HAM || !(num > 0 && last == loc)) { // 475-477
+                        const uint32_t tl = B.vr_tlen[c];
+                        if (WRITE && ok) {
+                            B.out_w[wrec + 2 + num] = loc;
+                            const uint8_t *sl = B.vr_cig + (uint64_t)c * SWM_CIGAR_SLOT;
+                            B.out_c[bcur] = sl[0];
+                            B.out_c[bcur + 1] = sl[1];
+                            const uint8_t *tx = (tl <= SWM_CIGAR_SLOT - 2) ? sl + 2 : B.arena + B.vr_aoff[c];
+                            for (uint32_t q = 0; q < tl; q++) B.out_c[bcur + 2 + q] = tx[q];
+                        }
+                        bcur += 2 + tl;
+                        num++;
+                        len += 2 + tl;
+                        last = loc;
+                    }
+                }
+                if (++g == 8) {
+                    g = 0;
+                    if (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16) put(); // 1790
+                }
+            }
+            if (g > 0 && (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16)) put(); // 1858
+        }
+        put();
+        if (!WRITE) {
+            B.it_nrec[item] = nrec;
+            B.it_nw[item] = nw;
+            B.it_nb[item] = nby;
+        } else if ((item & 1) && (nrec + B.it_nrec[item - 1]) > 0) {
+            mapped++;
+        }
+    }
+    if (WRITE) {
+        warp_add_u64(&B.stat[ST_LOCS], locs_total);
+        warp_add_u64(&B.stat[ST_MAPPED], mapped);
+    }
+}
+
+__global__ void k_batches_stat(uint32_t nitems, MapBufs B) {
+    unsigned long long s = 0;
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x)
+        s += B.it_nbat[item];
+    warp_add_u64(&B.stat[ST_BATCHES], s);
+}
+
+// ======================================================================
+// host side
+// ======================================================================
+
+static int g_sms = 0;
+
+static unsigned grid_cap(uint64_t work, unsigned threads, int per_sm) {
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    uint64_t g = (work + threads - 1) / threads;
+    uint64_t cap = (uint64_t)g_sms * per_sm;
+    if (g > cap) g = cap;
+    return (unsigned)(g ? g : 1);
+}
+
+template <typename T>
+static int dmalloc(T **p, uint64_t count) {
+    cudaError_t e = cudaMalloc((void **)p, (count ? count : 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        swm_set_error("cudaMalloc(%llu bytes): %s", (unsigned long long)(count * sizeof(T)), cudaGetErrorString(e));
+        return SWM_ERR_OOM;
+    }
+    return SWM_OK;
+}
+
+static void free_bufs(MapBufs &B) {
+    void *ps[] = {B.it_w, B.sel_start, B.sel_count, B.sel_meta, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
+                  B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.ch_g,
+                  B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_item, B.bt_cnt, B.bt_coff, B.cand_ub, B.cc_pos,
+                  B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena,
+                  B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
+    for (void *p : ps) cudaFree(p);
+    memset(&B, 0, sizeof(B));
+}
+
+static uint64_t scan_cap(const swm_mapper *m) {
+    uint64_t c = m->cap_items + 1;
+    if (m->cap_chunks + 1 > c) c = m->cap_chunks + 1;
+    return c;
+}
+
+static int alloc_items(swm_mapper *m) {
+    MapBufs &B = m->b;
+    const uint64_t I = m->cap_items;
+    int rc = SWM_OK;
+    rc |= dmalloc(&B.it_w, I * 32);
+    rc |= dmalloc(&B.sel_start, I * SWM_MAX_SEL);
+    rc |= dmalloc(&B.sel_count, I * SWM_MAX_SEL);
+    rc |= dmalloc(&B.sel_meta, I * SWM_MAX_SEL);
+    rc |= dmalloc(&B.it_nsel, I);
+    rc |= dmalloc(&B.it_e, I);
+    rc |= dmalloc(&B.it_nch, I);
+    rc |= dmalloc(&B.it_nel, I);
+    rc |= dmalloc(&B.it_nbat, I);
+    rc |= dmalloc(&B.it_choff, I + 1);
+    rc |= dmalloc(&B.it_eloff, I + 1);
+    rc |= dmalloc(&B.it_nrec, I);
+    rc |= dmalloc(&B.it_nw, I);
+    rc |= dmalloc(&B.it_nb, I);
+    rc |= dmalloc(&B.it_recoff, I + 1);
+    rc |= dmalloc(&B.it_woff, I + 1);
+    rc |= dmalloc(&B.it_boff, I + 1);
+    rc |= dmalloc(&B.tot, TOT_N);
+    rc |= dmalloc(&B.stat, ST_N);
+    return rc ? SWM_ERR_OOM : SWM_OK;
+}
+
+static int alloc_work(swm_mapper *m) {
+    MapBufs &B = m->b;
+    int rc = SWM_OK;
+    cudaFree(B.ch_g); cudaFree(B.ch_meta); cudaFree(B.bt_c0); cudaFree(B.bt_c1); cudaFree(B.bt_e0);
+    cudaFree(B.bt_item); cudaFree(B.bt_cnt); cudaFree(B.bt_coff); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
+    cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
+    cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
+    cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
+    rc |= dmalloc(&B.ch_g, m->cap_chunks);
+    rc |= dmalloc(&B.ch_meta, m->cap_chunks);
+    rc |= dmalloc(&B.bt_c0, m->cap_chunks);
+    rc |= dmalloc(&B.bt_c1, m->cap_chunks);
+    rc |= dmalloc(&B.bt_e0, m->cap_chunks);
+    rc |= dmalloc(&B.bt_item, m->cap_chunks);
+    rc |= dmalloc(&B.bt_cnt, m->cap_chunks);
+    rc |= dmalloc(&B.bt_coff, m->cap_chunks + 1);
+    rc |= dmalloc(&B.cand_ub, m->cap_elems);
+    rc |= dmalloc(&B.cc_pos, m->cap_cands);
+    rc |= dmalloc(&B.cc_item, m->cap_cands);
+    rc |= dmalloc(&B.vr_flag, m->cap_cands);
+    rc |= dmalloc(&B.vr_loc, m->cap_cands);
+    rc |= dmalloc(&B.vr_err, m->cap_cands);
+    rc |= dmalloc(&B.vr_mloc, m->cap_cands);
+    rc |= dmalloc(&B.vr_tlen, m->cap_cands);
+    rc |= dmalloc(&B.vr_cig, m->cap_cands * SWM_CIGAR_SLOT);
+    rc |= dmalloc(&B.vr_aoff, m->cap_cands);
+    rc |= dmalloc(&B.arena, m->cap_arena);
+    rc |= dmalloc(&B.out_w, m->cap_words);
+    rc |= dmalloc(&B.out_c, m->cap_bytes);
+    rc |= dmalloc(&B.rec_woff, m->cap_recs);
+    rc |= dmalloc(&B.rec_boff, m->cap_recs);
+    rc |= dmalloc(&B.rec_blen, m->cap_recs);
+    rc |= dmalloc(&B.scan_tmp, swm_scan_tmp_words(scan_cap(m)));
+    return rc ? SWM_ERR_OOM : SWM_OK;
+}
+
+extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper **out) {
+    if (!ix || !out || max_reads == 0 || max_reads > (1ull << 30)) return SWM_ERR_ARG;
+    SWM_CUDA(cudaSetDevice(ix->device));
+    swm_mapper *m = (swm_mapper *)calloc(1, sizeof(swm_mapper));
+    if (!m) return SWM_ERR_OOM;
+    m->ix = ix;
+    m->device = ix->device;
+    m->max_reads = max_reads;
+    m->cap_items = 2 * max_reads;
+    m->cap_chunks = m->cap_items * 16 + 1024;
+    m->cap_elems = m->cap_items * 128 + 4096;
+    m->cap_cands = m->cap_items * 8 + 4096;
+    m->cap_recs = m->cap_items + 1024;
+    m->cap_words = m->cap_items * 8 + 4096;
+    m->cap_bytes = m->cap_items * 32 + 4096;
+    m->cap_arena = ARENA_CAP_DEFAULT;
+    m->stride_cap = 0;
+    int rc = SWM_OK;
+    if (cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking) != cudaSuccess) rc = SWM_ERR_CUDA;
+    for (int i = 0; i < 8 && rc == SWM_OK; i++)
+        if (cudaEventCreate(&m->ev[i]) != cudaSuccess) rc = SWM_ERR_CUDA;
+    if (rc == SWM_OK) rc = alloc_items(m);
+    if (rc == SWM_OK) rc = alloc_work(m);
+    if (rc == SWM_OK && (dmalloc(&m->d_lens, max_reads) || dmalloc(&m->d_e, max_reads))) rc = SWM_ERR_OOM;
+    if (rc == SWM_OK && (cudaHostAlloc((void **)&m->h_lens, max_reads * 4, 0) != cudaSuccess ||
+                         cudaHostAlloc((void **)&m->h_e, max_reads, 0) != cudaSuccess ||
+                         cudaHostAlloc((void **)&m->h_nrec, m->cap_items * 4, 0) != cudaSuccess ||
+                         cudaHostAlloc((void **)&m->h_tot, TOT_N * 4, 0) != cudaSuccess ||
+                         cudaHostAlloc((void **)&m->h_stat, ST_N * 8, 0) != cudaSuccess))
+        rc = SWM_ERR_OOM;
+    if (rc != SWM_OK) {
+        swm_mapper_free(m);
+        return rc;
+    }
+    m->h_cap_items = m->cap_items;
+    *out = m;
+    return SWM_OK;
+}
+
+extern "C" void swm_mapper_free(swm_mapper *m) {
+    if (!m) return;
+    cudaSetDevice(m->device);
+    if (m->st) cudaStreamSynchronize(m->st);
+    free_bufs(m->b);
+    cudaFree(m->d_reads);
+    cudaFree(m->d_lens);
+    cudaFree(m->d_e);
+    cudaFreeHost(m->h_reads);
+    cudaFreeHost(m->h_lens);
+    cudaFreeHost(m->h_e);
+    cudaFreeHost(m->h_w);
+    cudaFreeHost(m->h_c);
+    cudaFreeHost(m->h_rw);
+    cudaFreeHost(m->h_rb);
+    cudaFreeHost(m->h_rl);
+    cudaFreeHost(m->h_nrec);
+    cudaFreeHost(m->h_tot);
+    cudaFreeHost(m->h_stat);
+    for (int i = 0; i < 8; i++)
+        if (m->ev[i]) cudaEventDestroy(m->ev[i]);
+    if (m->st) cudaStreamDestroy(m->st);
+    free(m);
+}
+
+#define LAUNCH_CHECK()                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = cudaGetLastError();                                                        \
+        if (e_ != cudaSuccess) {                                                                    \
+            swm_set_error("kernel launch: %s", cudaGetErrorString(e_));                             \
+            return SWM_ERR_CUDA;                                                                    \
+        }                                                                                           \
+    } while (0)
+
+// Queue the whole pipeline for one block on m->st. No host synchronisation.
+static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, uint64_t stride, uint32_t nreads,
+                   uint32_t errors, const uint8_t *d_e) {
+    MapBufs &B = m->b;
+    cudaStream_t st = m->st;
+    const uint32_t nitems = 2 * nreads;
+    const swm_index *ix = m->ix;
+    m->launches = 0;
+    SWM_CUDA(cudaMemsetAsync(B.tot, 0, TOT_N * 4, st));
+    SWM_CUDA(cudaMemsetAsync(B.stat, 0, ST_N * 8, st));
+    SWM_CUDA(cudaEventRecord(m->ev[0], st));
+    k_seed<<<grid_cap(nitems, 128, 32), 128, 0, st>>>(d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, ix->k, B);
+    m->launches++;
+    LAUNCH_CHECK();
+    SWM_CUDA(cudaEventRecord(m->ev[1], st));
+    int rc = swm_exclusive_scan(B.it_nch, B.it_choff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_CHUNKS, st);
+    if (rc) return rc;
+    rc = swm_exclusive_scan(B.it_nel, B.it_eloff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_ELEMS, st);
+    if (rc) return rc;
+    m->launches += 6;
+    k_plan<<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, ix->d_pos, B, m->cap_chunks, m->cap_elems);
+    m->launches++;
+    LAUNCH_CHECK();
+    SWM_CUDA(cudaEventRecord(m->ev[2], st));
+    k_cand<<<grid_cap(m->cap_chunks * 32, CAND_WARPS * 32, 8), CAND_WARPS * 32, 0, st>>>(ix->d_pos, ix->d_lseed, B,
+                                                                                           m->cap_chunks);
+    m->launches++;
+    LAUNCH_CHECK();
+    rc = swm_exclusive_scan(B.bt_cnt, B.bt_coff, B.tot + TOT_CHUNKS, 0, m->cap_chunks, B.scan_tmp, B.tot + TOT_CANDS,
+                            st);
+    if (rc) return rc;
+    m->launches += 3;
+    k_compact<<<grid_cap(m->cap_chunks * 32, 256, 16), 256, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands);
+    m->launches++;
+    LAUNCH_CHECK();
+    SWM_CUDA(cudaEventRecord(m->ev[3], st));
+    k_verify<<<grid_cap(m->cap_cands, 128, 64), 128, 0, st>>>(d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
+                                                               ix->ref_length, B, m->cap_chunks, m->cap_elems,
+                                                               m->cap_cands, m->cap_arena);
+    m->launches++;
+    LAUNCH_CHECK();
+    SWM_CUDA(cudaEventRecord(m->ev[4], st));
+    k_records<false><<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems, m->cap_cands,
+                                                                 m->cap_recs, m->cap_words, m->cap_bytes);
+    rc = swm_exclusive_scan(B.it_nrec, B.it_recoff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_RECS, st);
+    if (rc) return rc;
+    rc = swm_exclusive_scan(B.it_nw, B.it_woff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_WORDS, st);
+    if (rc) return rc;
+    rc = swm_exclusive_scan(B.it_nb, B.it_boff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_BYTES, st);
+    if (rc) return rc;
+    k_records<true><<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems, m->cap_cands,
+                                                                m->cap_recs, m->cap_words, m->cap_bytes);
+    k_batches_stat<<<grid_cap(nitems, 256, 8), 256, 0, st>>>(nitems, B);
+    m->launches += 12;
+    LAUNCH_CHECK();
+    SWM_CUDA(cudaEventRecord(m->ev[5], st));
+    return SWM_OK;
+}
+
+static void grow(uint64_t *cap, uint64_t need) {
+    if (need <= *cap) return;
+    uint64_t n = *cap;
+    while (n < need) n *= 2;
+    *cap = n + n / 4;
+}
+
+// Queue the copy of the block's totals to pinned memory (after enqueue).
+static int queue_totals(swm_mapper *m) {
+    SWM_CUDA(cudaMemcpyAsync(m->h_tot, m->b.tot, TOT_N * 4, cudaMemcpyDeviceToHost, m->st));
+    SWM_CUDA(cudaMemcpyAsync(m->h_stat, m->b.stat, ST_N * 8, cudaMemcpyDeviceToHost, m->st));
+    return SWM_OK;
+}
+
+// Wait for the queued block and inspect its totals. *again is set when a
+// work buffer was too small; the capacities are grown and the buffers
+// reallocated, and the caller must queue the block again.
+static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *again) {
+    *again = 0;
+    cudaError_t se = cudaStreamSynchronize(m->st);
+    if (se != cudaSuccess) {
+        swm_set_error("mapping block failed: %s", cudaGetErrorString(se));
+        return SWM_ERR_CUDA;
+    }
+    memcpy(m->tot, m->h_tot, sizeof(m->tot));
+    const uint32_t fl = m->tot[TOT_FLAGS];
+    if (fl & OV_BAD) {
+        swm_set_error("a read is outside the envelope (length <= %d and <= stride, threshold <= %d)",
+                      SWM_MAX_READ_LEN, SWM_MAX_ERRORS);
+        return SWM_ERR_ARG;
+    }
+    bool need = false;
+    // totals from the item scans are exact even when a later buffer overflowed
+    if (m->tot[TOT_CHUNKS] > m->cap_chunks) {
+        grow(&m->cap_chunks, m->tot[TOT_CHUNKS]);
+        need = true;
+    }
+    if (m->tot[TOT_ELEMS] > m->cap_elems) {
+        grow(&m->cap_elems, m->tot[TOT_ELEMS]);
+        need = true;
+    }
+    if (!need) {
+        if ((fl & OV_CANDS) || m->tot[TOT_CANDS] > m->cap_cands) {
+            grow(&m->cap_cands, m->tot[TOT_CANDS]);
+            need = true;
+        }
+        if (fl & OV_ARENA) {
+            grow(&m->cap_arena, (uint64_t)m->tot[TOT_ARENA] + 1);
+            need = true;
+        }
+        if (!need && ((fl & OV_RECS) || m->tot[TOT_RECS] > m->cap_recs || m->tot[TOT_WORDS] > m->cap_words ||
+                      m->tot[TOT_BYTES] > m->cap_bytes)) {
+            grow(&m->cap_recs, m->tot[TOT_RECS]);
+            grow(&m->cap_words, m->tot[TOT_WORDS]);
+            grow(&m->cap_bytes, m->tot[TOT_BYTES]);
+            need = true;
+        }
+    }
+    if (need) {
+        *again = 1;
+        return alloc_work(m);
+    }
+    float t;
+    for (int i = 0; i < 5; i++) {
+        cudaEventElapsedTime(&t, m->ev[i], m->ev[i + 1]);
+        m->stage_ms[i] = t;
+    }
+    cudaEventElapsedTime(&t, m->ev[0], m->ev[5]);
+    m->stage_ms[5] = t;
+    const unsigned long long *stat = m->h_stat;
+    swm_map_stats &S = m->stats;
+    memset(&S, 0, sizeof S);
+    S.reads = nreads;
+    S.items = 2ull * nreads;
+    S.chunks = m->tot[TOT_CHUNKS];
+    S.fetched = m->tot[TOT_ELEMS];
+    S.batches = stat[ST_BATCHES];
+    S.candidates = m->tot[TOT_CANDS];
+    S.cells = stat[ST_CELLS];
+    S.passed = stat[ST_PASSED];
+    S.records = m->tot[TOT_RECS];
+    S.locations = stat[ST_LOCS];
+    S.mapped_reads = stat[ST_MAPPED];
+    S.retries = retries;
+    S.h2d_bytes = m->h2d_pending;
+    m->h2d_pending = 0;
+    m->have_result = 1;
+    m->cur_n = nreads;
+    return SWM_OK;
+}
+
+// Run one block on device-resident inputs, re-running it with larger work
+// buffers when a capacity was exceeded.
+static int run_block(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, uint64_t stride, uint32_t nreads,
+                     uint32_t errors, const uint8_t *d_e, uint64_t retries) {
+    for (int attempt = 0; attempt < 8; attempt++) {
+        int rc = enqueue(m, d_reads, d_lens, stride, nreads, errors, d_e);
+        if (!rc) rc = queue_totals(m);
+        if (rc) return rc;
+        int again = 0;
+        rc = finish_block(m, nreads, retries, &again);
+        if (rc) return rc;
+        if (!again) return SWM_OK;
+        retries++;
+    }
+    swm_set_error("mapping block did not fit after repeated buffer growth");
+    return SWM_ERR_OOM;
+}
+
+static int check_batch(const swm_mapper *m, uint64_t nreads, uint64_t stride, uint32_t errors) {
+    if (nreads > m->max_reads) {
+        swm_set_error("block of %llu reads exceeds max_reads %llu", (unsigned long long)nreads,
+                      (unsigned long long)m->max_reads);
+        return SWM_ERR_ARG;
+    }
+    if (errors > SWM_MAX_ERRORS || stride == 0) {
+        swm_set_error("errors must be <= %d and stride > 0", SWM_MAX_ERRORS);
+        return SWM_ERR_ARG;
+    }
+    return SWM_OK;
+}
+
+static int check_host_reads(const swm_mapper *m, const uint32_t *lens, const uint8_t *e_arr, uint64_t nreads,
+                            uint64_t stride) {
+    const uint32_t klong = m->ix->k + SWM_SEED_STEP - 1;
+    for (uint64_t r = 0; r < nreads; r++) {
+        if (lens[r] > SWM_MAX_READ_LEN || lens[r] > stride || lens[r] / klong > 16 ||
+            (e_arr && e_arr[r] > SWM_MAX_ERRORS)) {
+            swm_set_error("read %llu: length %u or threshold outside the envelope (L <= %d, L <= stride, e <= %d)",
+                          (unsigned long long)r, lens[r], SWM_MAX_READ_LEN, SWM_MAX_ERRORS);
+            return SWM_ERR_ARG;
+        }
+    }
+    return SWM_OK;
+}
+
+extern "C" int swm_map_device(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, uint64_t stride,
+                              uint64_t reads_num, uint32_t errors, const uint8_t *d_errors) {
+    if (!m || (!d_reads && reads_num) || (!d_lens && reads_num)) return SWM_ERR_ARG;
+    int rc = check_batch(m, reads_num, stride, errors);
+    if (rc) return rc;
+    SWM_CUDA(cudaSetDevice(m->device));
+    if (m->pending) return SWM_ERR_STATE;
+    m->have_result = 0;
+    return run_block(m, d_reads, d_lens, stride, (uint32_t)reads_num, errors, d_errors, 0);
+}
+
+static int ensure_host(void **p, uint64_t *cap, uint64_t need, size_t elt) {
+    if (need <= *cap && *p) return SWM_OK;
+    uint64_t n = need + need / 4 + 1024;
+    cudaFreeHost(*p);
+    *p = nullptr;
+    if (cudaHostAlloc(p, n * elt, 0) != cudaSuccess) {
+        *p = nullptr;
+        *cap = 0;
+        swm_set_error("cudaHostAlloc(%llu bytes) failed", (unsigned long long)(n * elt));
+        return SWM_ERR_OOM;
+    }
+    *cap = n;
+    return SWM_OK;
+}
+
+// Copy the packed records of the last block to pinned staging and expand
+// them into the reference layout (records at SWM_RECORD_WORDS, CIGARs at
+// SWM_CIGAR_STRIDE, unmapped ids).
+extern "C" int swm_map_fetch(swm_mapper *m, swm_result *r) {
+    if (!m || !r) return SWM_ERR_ARG;
+    if (!m->have_result) return SWM_ERR_STATE;
+    SWM_CUDA(cudaSetDevice(m->device));
+    const uint64_t nitems = 2 * m->cur_n;
+    const uint64_t nrec = m->tot[TOT_RECS], nw = m->tot[TOT_WORDS], nby = m->tot[TOT_BYTES];
+    int rc = ensure_host((void **)&m->h_w, &m->h_cap_w, nw, 4);
+    if (!rc) rc = ensure_host((void **)&m->h_c, &m->h_cap_c, nby, 1);
+    if (!rc) rc = ensure_host((void **)&m->h_rw, &m->h_cap_rw, nrec, 4);
+    if (!rc) rc = ensure_host((void **)&m->h_rb, &m->h_cap_rb, nrec, 4);
+    if (!rc) rc = ensure_host((void **)&m->h_rl, &m->h_cap_rl, nrec, 4);
+    if (!rc) rc = ensure_host((void **)&m->h_nrec, &m->h_cap_items, nitems, 4);
+    if (rc) return rc;
+    cudaStream_t st = m->st;
+    if (nw) SWM_CUDA(cudaMemcpyAsync(m->h_w, m->b.out_w, nw * 4, cudaMemcpyDeviceToHost, st));
+    if (nby) SWM_CUDA(cudaMemcpyAsync(m->h_c, m->b.out_c, nby, cudaMemcpyDeviceToHost, st));
+    if (nrec) {
+        SWM_CUDA(cudaMemcpyAsync(m->h_rw, m->b.rec_woff, nrec * 4, cudaMemcpyDeviceToHost, st));
+        SWM_CUDA(cudaMemcpyAsync(m->h_rb, m->b.rec_boff, nrec * 4, cudaMemcpyDeviceToHost, st));
+        SWM_CUDA(cudaMemcpyAsync(m->h_rl, m->b.rec_blen, nrec * 4, cudaMemcpyDeviceToHost, st));
+    }
+    if (nitems) SWM_CUDA(cudaMemcpyAsync(m->h_nrec, m->b.it_nrec, nitems * 4, cudaMemcpyDeviceToHost, st));
+    SWM_CUDA(cudaStreamSynchronize(st));
+    m->stats.d2h_bytes = nw * 4 + nby + nrec * 12 + nitems * 4 + TOT_N * 4 + ST_N * 8;
+    int status = SWM_OK;
+    r->n_records = nrec;
+    for (uint64_t q = 0; q < nrec; q++) {
+        const uint32_t *src = m->h_w + m->h_rw[q];
+        const uint32_t n = src[1] & 0x7fffffffu;
+        const uint32_t bl = m->h_rl[q];
+        if (q < r->records_cap) {
+            if (r->ref_pos_buffer) memcpy(r->ref_pos_buffer + q * SWM_RECORD_WORDS, src, (2 + n) * 4);
+            if (r->cigar_buffer) {
+                uint32_t cl = bl <= SWM_CIGAR_STRIDE ? bl : SWM_CIGAR_STRIDE;
+                memcpy(r->cigar_buffer + q * SWM_CIGAR_STRIDE, m->h_c + m->h_rb[q], cl);
+                if (bl > SWM_CIGAR_STRIDE) status = SWM_ERR_OVERFLOW;
+            }
+        } else {
+            status = SWM_ERR_OVERFLOW;
+        }
+    }
+    uint64_t nu = 0;
+    for (uint64_t rd = 0; rd < m->cur_n; rd++) {
+        if (m->h_nrec[2 * rd] + m->h_nrec[2 * rd + 1] == 0) {
+            if (nu < r->unmapped_cap && r->unmapped) r->unmapped[nu] = (uint32_t)(2 * rd + 1);
+            else status = SWM_ERR_OVERFLOW;
+            nu++;
+        }
+    }
+    r->n_unmapped = nu;
+    if (status) swm_set_error("result buffers too small (records %llu, unmapped %llu)", (unsigned long long)nrec,
+                              (unsigned long long)nu);
+    return status;
+}
+
+static int stage_inputs(swm_mapper *m, const swm_batch *b) {
+    const uint64_t n = b->reads_num;
+    int rc = check_batch(m, n, b->stride, b->errors);
+    if (rc) return rc;
+    rc = check_host_reads(m, b->reads_len, b->errors_per_read, n, b->stride);
+    if (rc) return rc;
+    const uint64_t bytes = n * b->stride;
+    if (bytes > m->stride_cap) {
+        cudaFree(m->d_reads);
+        cudaFreeHost(m->h_reads);
+        m->d_reads = nullptr;
+        m->h_reads = nullptr;
+        uint64_t cap = m->max_reads * (b->stride > 256 ? b->stride : 256);
+        if (cap < bytes) cap = bytes;
+        if (dmalloc(&m->d_reads, cap) || cudaHostAlloc((void **)&m->h_reads, cap, 0) != cudaSuccess) {
+            m->stride_cap = 0;
+            return SWM_ERR_OOM;
+        }
+        m->stride_cap = cap;
+    }
+    memcpy(m->h_reads, b->reads, bytes);
+    memcpy(m->h_lens, b->reads_len, n * 4);
+    if (b->errors_per_read) memcpy(m->h_e, b->errors_per_read, n);
+    SWM_CUDA(cudaMemcpyAsync(m->d_reads, m->h_reads, bytes, cudaMemcpyHostToDevice, m->st));
+    SWM_CUDA(cudaMemcpyAsync(m->d_lens, m->h_lens, n * 4, cudaMemcpyHostToDevice, m->st));
+    if (b->errors_per_read) SWM_CUDA(cudaMemcpyAsync(m->d_e, m->h_e, n, cudaMemcpyHostToDevice, m->st));
+    m->h2d_pending = bytes + n * 4 + (b->errors_per_read ? n : 0);
+    return SWM_OK;
+}
+
+extern "C" int swm_map_submit(swm_mapper *m, const swm_batch *b) {
+    if (!m || !b || (!b->reads && b->reads_num) || (!b->reads_len && b->reads_num)) return SWM_ERR_ARG;
+    if (m->pending) return SWM_ERR_STATE;
+    SWM_CUDA(cudaSetDevice(m->device));
+    int rc = stage_inputs(m, b);
+    if (rc) return rc;
+    m->cur_stride = b->stride;
+    m->cur_n = b->reads_num;
+    m->cur_errors = b->errors;
+    m->cur_e = b->errors_per_read;
+    m->have_result = 0;
+    rc = enqueue(m, m->d_reads, m->d_lens, b->stride, (uint32_t)b->reads_num, b->errors,
+                 b->errors_per_read ? m->d_e : nullptr);
+    if (!rc) rc = queue_totals(m);
+    if (rc) return rc;
+    m->pending = 1;
+    return SWM_OK;
+}
+
+extern "C" int swm_map_wait(swm_mapper *m, swm_result *r) {
+    if (!m || !r) return SWM_ERR_ARG;
+    if (!m->pending) return SWM_ERR_STATE;
+    SWM_CUDA(cudaSetDevice(m->device));
+    m->pending = 0;
+    int again = 0;
+    int rc = finish_block(m, (uint32_t)m->cur_n, 0, &again);
+    if (rc) return rc;
+    if (again) {
+        // a work buffer was too small: repeat the block from the staged inputs
+        rc = run_block(m, m->d_reads, m->d_lens, m->cur_stride, (uint32_t)m->cur_n, m->cur_errors,
+                       m->cur_e ? m->d_e : nullptr, 1);
+        if (rc) return rc;
+    }
+    return swm_map_fetch(m, r);
+}
+
+extern "C" int swm_map_batch(swm_mapper *m, const swm_batch *b, swm_result *r) {
+    int rc = swm_map_submit(m, b);
+    if (rc) return rc;
+    return swm_map_wait(m, r);
+}
+
+extern "C" int swm_mapper_stats(const swm_mapper *m, swm_map_stats *s) {
+    if (!m || !s) return SWM_ERR_ARG;
+    *s = m->stats;
+    return SWM_OK;
+}
+
+extern "C" int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float *ms) {
+    static const char *names[6] = {"seed", "plan", "candidates", "verify", "records", "total"};
+    if (!m || !stage || !ms) return SWM_ERR_ARG;
+    for (int i = 0; i < 6; i++)
+        if (!strcmp(stage, names[i])) {
+            *ms = m->stage_ms[i];
+            return SWM_OK;
+        }
+    return SWM_ERR_ARG;
+}
+
+extern "C" uint64_t swm_mapper_launches(const swm_mapper *m) { return m ? m->launches : 0; }
+
+extern "C" void *swm_mapper_stream(const swm_mapper *m) { return m ? (void *)m->st : nullptr; }
+
+extern "C" int swm_mapper_debug_candidates(const swm_mapper *m, uint32_t *item, uint32_t *pos, int32_t *err,
+                                           int32_t *loc, uint64_t cap, uint64_t *n) {
+    if (!m || !n) return SWM_ERR_ARG;
+    if (!m->have_result) return SWM_ERR_STATE;
+    SWM_CUDA(cudaSetDevice(m->device));
+    const uint64_t tot = m->tot[TOT_CANDS];
+    *n = tot;
+    const uint64_t k = tot < cap ? tot : cap;
+    if (k) {
+        if (item) SWM_CUDA(cudaMemcpy(item, m->b.cc_item, k * 4, cudaMemcpyDeviceToHost));
+        if (pos) SWM_CUDA(cudaMemcpy(pos, m->b.cc_pos, k * 4, cudaMemcpyDeviceToHost));
+        if (err) SWM_CUDA(cudaMemcpy(err, m->b.vr_err, k * 4, cudaMemcpyDeviceToHost));
+        if (loc) SWM_CUDA(cudaMemcpy(loc, m->b.vr_mloc, k * 4, cudaMemcpyDeviceToHost));
+    }
+    return SWM_OK;
+}

@@ -1,0 +1,148 @@
+"""GPU mapping against the oracle and the reference's recorded outputs (gpu)."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from swmapper_gb300 import synth
+from tests.helpers import first_diff, genome, oracle_index, records_by_e
+
+pytestmark = pytest.mark.gpu
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_outputs.json")))
+
+
+def _gpu(swm, g, reads, lens, e, eper=None, max_reads=None):
+    ix = swm.Index.build(g)
+    m = swm.Mapper(ix, max_reads=max_reads or max(1, reads.shape[0]))
+    out = m.map(reads, lens, e, errors_per_read=eper)
+    return out, m, ix
+
+
+def _check(out, ref_records, ref_unmapped):
+    got = out.records()
+    d = first_diff(got, ref_records)
+    assert d is None, d
+    assert [int(x) for x in out.unmapped] == [int(x) for x in ref_unmapped]
+
+
+@pytest.mark.parametrize("key", sorted(GOLD["map"]))
+def test_gpu_equals_reference_outputs(cuda_lib, key):
+    cases = {c[0]: c for c in GOLD["cases"]["map"]}
+    name, e = key.rsplit("_e", 1)
+    _, n, gseed, kind, over, nreads, lmin, lmax, err, es, rseed = cases[name]
+    g = synth.reference(n, seed=gseed, kind=kind, **over)
+    reads, lens, _, _ = synth.reads(g, nreads, lmin, lmax, err, seed=rseed)
+    out, _, _ = _gpu(cuda_lib, g, reads, lens, int(e))
+    want = [(r[0], r[1], tuple(r[2]), bytes.fromhex(r[3])) for r in GOLD["map"][key]["records"]]
+    _check(out, want, GOLD["map"][key]["unmapped"])
+
+
+def test_gpu_plain_1mbp(cuda_lib):
+    """Plain workload shape: 1 Mbp uniform, 100 bp reads, 2% error, e=5."""
+    g = genome(1_000_000, 1)
+    reads, lens, _, _ = synth.reads(g, 4096, 100, 100, 0.02, seed=2)
+    _, mix = oracle_index(g)
+    ref = po.map_reads(mix, reads, lens, 5, nthreads=8)
+    out, m, _ = _gpu(cuda_lib, g, reads, lens, 5)
+    _check(out, ref.records(), ref.unmapped)
+    st = m.stats()
+    assert st["candidates"] == ref.stats["candidates"]
+    assert st["mapped_reads"] == ref.stats["mapped_reads"]
+
+
+def test_gpu_repeats_multibatch(cuda_lib):
+    """Heavy repeats: refills, several batches per strand, buffer growth."""
+    g = genome(3_000_000, 7, "human", nrun_min=2000, nrun_max=20000, copies_per_family=300)
+    reads, lens, _, _ = synth.reads(g, 3000, 150, 150, 0.03, seed=8)
+    _, mix = oracle_index(g)
+    for e in (7, 12):
+        ref = po.map_reads(mix, reads, lens, e, nthreads=8)
+        out, m, _ = _gpu(cuda_lib, g, reads, lens, e)
+        _check(out, ref.records(), ref.unmapped)
+        assert m.stats()["batches"] == ref.stats["batches"]
+
+
+def test_gpu_uneven_per_read_e(cuda_lib):
+    """Read lengths U[50, 250] with e = ceil(0.05 L) per read."""
+    g = genome(2_000_000, 9, "repeats100m")
+    reads, lens, _, _ = synth.reads(g, 3000, 50, 250, 0.04, seed=10, stride=250)
+    eper = np.array([math.ceil(0.05 * int(L)) for L in lens], np.uint8)
+    _, mix = oracle_index(g)
+    ref_recs, ref_unm = records_by_e(mix, reads, lens, eper)
+    out, _, _ = _gpu(cuda_lib, g, reads, lens, 0, eper=eper)
+    _check(out, ref_recs, ref_unm)
+
+
+@pytest.mark.parametrize("e", [0, 1, 3, 15])
+def test_gpu_error_thresholds_and_odd_reads(cuda_lib, e):
+    g = genome(500_000, 11, "repeats100m", copies_per_family=30, rep_len_max=3000)
+    reads, lens, _, _ = synth.reads(g, 1500, 15, 254, 0.05, seed=12, stride=254)
+    reads[::5, 7] = ord("N")
+    reads[1::7, 20] = ord("a")
+    lens[::50] = 14       # shorter than one long seed: no seeds, unmapped
+    _, mix = oracle_index(g)
+    ref = po.map_reads(mix, reads, lens, e, nthreads=8)
+    out, _, _ = _gpu(cuda_lib, g, reads, lens, e)
+    _check(out, ref.records(), ref.unmapped)
+
+
+def test_gpu_reads_at_genome_ends(cuda_lib):
+    g = genome(200_000, 13)
+    reads = np.zeros((6, 120), np.uint8)
+    lens = np.full(6, 120, np.uint32)
+    reads[0] = g[:120]
+    reads[1] = g[3:123]
+    reads[2] = g[-120:]
+    reads[3, :100] = g[-100:]
+    lens[3] = 100
+    reads[4] = g[50_000:50_120]
+    reads[5] = g[1:121]
+    _, mix = oracle_index(g)
+    ref = po.map_reads(mix, reads, lens, 6)
+    out, _, _ = _gpu(cuda_lib, g, reads, lens, 6)
+    _check(out, ref.records(), ref.unmapped)
+
+
+def test_gpu_candidates_equal_oracle_trace(cuda_lib):
+    g = genome(1_000_000, 14, "repeats100m", copies_per_family=20)
+    reads, lens, _, _ = synth.reads(g, 64, 150, 150, 0.03, seed=15)
+    _, mix = oracle_index(g)
+    out, m, _ = _gpu(cuda_lib, g, reads, lens, 7)
+    item, pos, err, loc = m.debug_candidates()
+    for it in range(128):
+        r, strand = it >> 1, it & 1
+        s = bytes(reads[r, :lens[r]])
+        if strand:
+            s = s[::-1].translate(bytes.maketrans(b"ACGT", b"TGCA"))
+        tr = po.trace_item(mix, s, 7)
+        sel = item == it
+        assert np.array_equal(pos[sel], tr["pos"]), it
+        assert np.array_equal(err[sel], tr["err"]), it
+        assert np.array_equal(loc[sel], tr["loc"]), it
+
+
+def test_gpu_empty_and_async(cuda_lib):
+    g = genome(300_000, 16)
+    ix = cuda_lib.Index.build(g)
+    m = cuda_lib.Mapper(ix, max_reads=512)
+    empty = m.map(np.zeros((0, 100), np.uint8), np.zeros(0, np.uint32), 5)
+    assert empty.ref_pos.shape[0] == 0 and empty.unmapped.size == 0
+    reads, lens, _, _ = synth.reads(g, 500, 100, 100, 0.02, seed=17)
+    a = m.map(reads, lens, 5).records()
+    b = m.map(reads, lens, 5).records()
+    assert a == b
+
+
+def test_gpu_rejects_out_of_envelope(cuda_lib):
+    g = genome(100_000, 18)
+    ix = cuda_lib.Index.build(g)
+    m = cuda_lib.Mapper(ix, max_reads=4)
+    with pytest.raises(cuda_lib.SwmError):
+        m.map(np.zeros((1, 300), np.uint8), np.array([255], np.uint32), 5)
+    with pytest.raises(cuda_lib.SwmError):
+        m.map(np.zeros((1, 100), np.uint8), np.array([100], np.uint32), 16)
+    with pytest.raises(cuda_lib.SwmError):
+        m.map(np.zeros((5, 100), np.uint8), np.full(5, 100, np.uint32), 5)
