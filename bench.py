@@ -1,0 +1,508 @@
+#!/usr/bin/env python3
+"""Mapped reads/s of SWMapper's hot path on GB300.
+
+Workload (the batched configuration): a 100 Mbp synthetic genome (41% GC, 10%
+of it repeat copies of 300 bp-6 kb families at 1% divergence), k=12 index built
+on the GPU, 1,000,000 reads of 150 bp at 3% error (70% substitutions, 15% 1-bp
+insertions, 15% 1-bp deletions) from both strands, error threshold e=7.
+
+A step maps every read of the workload (both strands, all blocks) with the
+index and the reads resident in HBM; `value` is mapped reads per second over
+the K timed steps (CUDA events on the mapper's stream). `e2e` runs the same
+reads through the public host API (pinned staging, H2D, mapping, D2H of the
+packed records) with two mappers in ping-pong, timed on the host clock.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's own CPU code for the same workload
+(the scalar mapper of mapper_cpe.c and serial_index.c compiled for the host,
+all host threads) on a bounded sample of the reads per step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = dict(workload="batched: 100 Mbp genome (41% GC, 10% repeat copies 300 bp-6 kb at 1% divergence), "
+                         "1,000,000 x 150 bp reads at 3% error, e=7, k=12",
+                genome_bp=100_000_000, genome_kind="repeats100m", genome_seed=20261203,
+                reads=1_000_000, read_len=150, error_rate=0.03, e=7, k=12, read_seed=7)
+METRIC = "mapped reads/s"
+UNIT = "reads/s"
+
+
+# ------------------------------------------------------------ plumbing
+
+def cudart():
+    for name in ("libcudart.so.13", "libcudart.so", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            L = C.CDLL(name)
+            L.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+            L.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+            L.cudaFree.argtypes = [C.c_void_p]
+            L.cudaEventCreate.argtypes = [C.POINTER(C.c_void_p)]
+            L.cudaEventRecord.argtypes = [C.c_void_p, C.c_void_p]
+            L.cudaEventSynchronize.argtypes = [C.c_void_p]
+            L.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
+            L.cudaSetDevice.argtypes = [C.c_int]
+            return L
+        except OSError:
+            continue
+    raise RuntimeError("libcudart not found")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max/sum over ranks (gloo on the host; no data-path collective)."""
+
+    def __init__(self, ws):
+        self.ws = ws
+        self.pg = None
+        if ws > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def reduce(self, values, op):
+        if self.ws == 1:
+            return values
+        import torch
+        t = torch.tensor(values, dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX if op == "max" else self.dist.ReduceOp.SUM)
+        return t.tolist()
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured", d
+    return 6800.0, "fallback", {}
+
+
+def profile_traffic(kernel):
+    """Per-launch DRAM traffic per unit of work from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    vals = {}
+    for line in open(p):
+        if ":" in line and not line.startswith("#"):
+            k, v = line.split(":", 1)
+            try:
+                vals[k.strip()] = float(v.split()[0])
+            except (ValueError, IndexError):
+                pass
+    return vals
+
+
+def make_workload(rank=0):
+    from swmapper_gb300 import synth
+    w = WORKLOAD
+    g = synth.reference(w["genome_bp"], seed=w["genome_seed"], kind=w["genome_kind"])
+    reads, lens, _, _ = synth.reads(g, w["reads"], w["read_len"], w["read_len"], w["error_rate"],
+                                    seed=w["read_seed"] + 1000 * rank)
+    return g, reads, lens
+
+
+# ------------------------------------------------------------ CPU legs
+
+def host_map_index(arrays, k):
+    """Mapper view of index arrays for the CPU legs (start offsets, padded words)."""
+    from oracle import pyoracle as po
+    hix = po.HostIndex(k, 0, arrays["hash_count"], arrays["hash_offset"], arrays["positions"],
+                       arrays["pos_lseeds"], arrays["base_2bits"], arrays["base_3bits"])
+    return po.MapIndex(hix)
+
+
+CPU_BLOCK = 10_000   # reads per block of the reference's host loop (mapper_mpe.c:727)
+_cpu_bufs = {}
+
+
+def cpu_map(mix, reads, lens, e, threads):
+    """Map on the host in blocks of 10,000 reads: the reference's own
+    get_positions() when it was compiled here (kind 'reference'), else the
+    oracle restatement (kind 'port'). Returns (mapped reads, kind)."""
+    from oracle import pyoracle as po
+    if "out" not in _cpu_bufs:
+        _cpu_bufs["out"] = po.out_buffers(CPU_BLOCK)
+    mapped = 0
+    kind = "reference" if po.have_ref() else "port"
+    for b0 in range(0, reads.shape[0], CPU_BLOCK):
+        r, ln = reads[b0:b0 + CPU_BLOCK], lens[b0:b0 + CPU_BLOCK]
+        if kind == "reference":
+            res = po.ref_map_reads(mix, r, ln, e, nthreads=threads, out=_cpu_bufs["out"])
+            mapped += r.shape[0] - res.unmapped.size
+        else:
+            res = po.map_reads(mix, r, ln, e, nthreads=threads)
+            mapped += res.stats["mapped_reads"]
+    return mapped, kind
+
+
+def timed_cpu_sample(mix, reads, lens, e, threads, target_s):
+    """Time a bounded sample sized to take about target_s seconds."""
+    n = min(2048, reads.shape[0])
+    t0 = time.perf_counter()
+    cpu_map(mix, reads[:n], lens[:n], e, threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    n = int(min(reads.shape[0], max(n, n * target_s / dt)))
+    t0 = time.perf_counter()
+    mapped, kind = cpu_map(mix, reads[:n], lens[:n], e, threads)
+    dt = time.perf_counter() - t0
+    return mapped / dt, n, dt, kind
+
+
+# ------------------------------------------------------------ GPU arm
+
+STAGES = ["seed", "plan", "candidates", "compact", "verify", "records"]
+
+
+def stage_bytes(stage, st, L, e):
+    """Algorithmic DRAM bytes of one stage over a whole step."""
+    nl = L // 15
+    items = st["items"]
+    ns = min(e + 1, nl) * 4
+    if stage == "seed":
+        return items * (L + nl * 4 * 8 + 128 + ns * 12 + 16)
+    if stage == "plan":
+        return items * (ns * 8 + 16) + st["chunks"] * 8 + st["batches"] * 16
+    if stage == "candidates":
+        return st["fetched"] * 6 + st["chunks"] * 8 + st["batches"] * 20 + st["candidates"] * 4
+    if stage == "compact":
+        return st["candidates"] * 12 + st["batches"] * 12
+    if stage == "verify":
+        win = ((L + 2 * e + 31) // 32 + 1) * 8
+        return st["candidates"] * (win + 64 + 8 + 16) + st["passed"] * 64
+    if stage == "records":
+        return st["candidates"] * 10 + st["locations"] * 12 + items * 24
+    return 0
+
+
+def run_gpu(args):
+    import swmapper_gb300 as swm
+    ws, rank, local = dist_env()
+    dist = Dist(ws)
+    rt = cudart()
+    rt.cudaSetDevice(local)
+    w = WORKLOAD
+    g, reads, lens = make_workload(rank)
+    t0 = time.perf_counter()
+    ix = swm.Index.build(g, k=w["k"], device=local)
+    index_build_s = time.perf_counter() - t0
+    nreads, stride = reads.shape
+    block = min(args.block, nreads)
+    # inputs resident in HBM
+    d_reads, d_lens = C.c_void_p(), C.c_void_p()
+    assert rt.cudaMalloc(C.byref(d_reads), reads.nbytes) == 0
+    assert rt.cudaMalloc(C.byref(d_lens), lens.nbytes) == 0
+    rt.cudaMemcpy(d_reads, reads.ctypes.data, reads.nbytes, 1)
+    rt.cudaMemcpy(d_lens, lens.ctypes.data, lens.nbytes, 1)
+    m = swm.Mapper(ix, max_reads=block)
+    stream = C.c_void_p(m.stream())
+    ev0, ev1 = C.c_void_p(), C.c_void_p()
+    rt.cudaEventCreate(C.byref(ev0))
+    rt.cudaEventCreate(C.byref(ev1))
+
+    def one_step(acc):
+        for b0 in range(0, nreads, block):
+            nb = min(block, nreads - b0)
+            m.map_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, nb, w["e"])
+            if acc is not None:
+                st = m.stats()
+                for f in ("mapped_reads", "candidates", "cells", "passed", "fetched", "chunks", "batches", "items",
+                          "locations", "records", "retries"):
+                    acc[f] = acc.get(f, 0) + st[f]
+                for sname in STAGES:
+                    acc["ms_" + sname] = acc.get("ms_" + sname, 0.0) + m.stage_ms(sname)
+                acc["launches"] = acc.get("launches", 0) + m.launches()
+                acc["blocks"] = acc.get("blocks", 0) + 1
+
+    for _ in range(args.warmup):
+        one_step(None)
+    acc = {}
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    rt.cudaDeviceSynchronize()
+    rt.cudaEventRecord(ev0, stream)
+    for _ in range(args.steps):
+        one_step(acc)
+    rt.cudaEventRecord(ev1, stream)
+    rt.cudaEventSynchronize(ev1)
+    rt.cudaDeviceSynchronize()
+    dist.barrier()
+    ms = C.c_float()
+    rt.cudaEventElapsedTime(C.byref(ms), ev0, ev1)
+    clk = clocks.stop()
+    elapsed = ms.value / 1000.0
+    tot_elapsed, = dist.reduce([elapsed], "max")
+    tot_mapped, tot_cells = dist.reduce([float(acc["mapped_reads"]), float(acc["cells"])], "sum")
+    value = tot_mapped / tot_elapsed
+    gcups = tot_cells / tot_elapsed / 1e9
+
+    # end to end through the host API: two mappers in ping-pong, packed results
+    m2 = swm.Mapper(ix, max_reads=block)
+    mappers = [m, m2]
+    bufs = [swm.PackedBuffers(block), swm.PackedBuffers(block)]
+    blocks = [(b0, min(block, nreads - b0)) for b0 in range(0, nreads, block)]
+
+    def e2e_step(acc2):
+        pend = []
+        for i, (b0, nb) in enumerate(blocks):
+            mm = mappers[i % 2]
+            if len(pend) == 2:
+                j, pm = pend.pop(0)
+                pm.wait_packed(bufs[j % 2])
+                acc2["mapped"] += count_mapped(bufs[j % 2], blocks[j][1])
+                acc2["h2d"] += pm.stats()["h2d_bytes"]
+                acc2["d2h"] += pm.stats()["d2h_bytes"]
+            mm.submit(reads[b0:b0 + nb], lens[b0:b0 + nb], w["e"])
+            pend.append((i, mm))
+        for j, pm in pend:
+            pm.wait_packed(bufs[j % 2])
+            acc2["mapped"] += count_mapped(bufs[j % 2], blocks[j][1])
+            acc2["h2d"] += pm.stats()["h2d_bytes"]
+            acc2["d2h"] += pm.stats()["d2h_bytes"]
+
+    for _ in range(min(args.warmup, 2)):
+        e2e_step({"mapped": 0, "h2d": 0, "d2h": 0})
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    acc2 = {"mapped": 0, "h2d": 0, "d2h": 0}
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step(acc2)
+    e2e_t = time.perf_counter() - t0
+    e2e_t, = dist.reduce([e2e_t], "max")
+    e2e_mapped, = dist.reduce([float(acc2["mapped"])], "sum")
+    e2e = {"value": e2e_mapped / e2e_t, "unit": UNIT,
+           "h2d_bytes_per_step": int(acc2["h2d"] / e2e_steps), "d2h_bytes_per_step": int(acc2["d2h"] / e2e_steps),
+           "steps": e2e_steps, "path": "swm_map_submit + swm_map_wait_packed, 2 mappers ping-pong"}
+
+    # roofline of the dominant kernel
+    peak, peak_kind, peaks = measured_peaks()
+    L, e = w["read_len"], w["e"]
+    per_step = {k: v / args.steps for k, v in acc.items()}
+    stage_rows = {}
+    for sname in STAGES:
+        t_ms = per_step["ms_" + sname]
+        byts = stage_bytes(sname, per_step, L, e)
+        stage_rows[sname] = {"ms_per_step": round(t_ms, 3),
+                             "gbs": round(byts / (t_ms / 1e3) / 1e9, 1) if t_ms > 0 else None,
+                             "bytes_per_step": int(byts)}
+    dom = max(STAGES, key=lambda s: per_step["ms_" + s])
+    kern = {"seed": "k_seed", "plan": "k_plan", "candidates": "k_cand", "compact": "k_compact",
+            "verify": "k_verify", "records": "k_records"}[dom]
+    launches_per_step = per_step["blocks"]
+    avg_launch_s = per_step["ms_" + dom] / 1e3 / launches_per_step
+    alg_bytes_launch = stage_bytes(dom, per_step, L, e) / launches_per_step
+    achieved = alg_bytes_launch / avg_launch_s / 1e9
+    tr = profile_traffic(kern)
+    traffic = None
+    if tr:
+        unit_key = {"k_verify": "candidates", "k_cand": "fetched", "k_seed": "items", "k_plan": "chunks"}.get(kern)
+        for key, val in tr.items():
+            if key.startswith("dram_bytes_per_") and unit_key and key.endswith(unit_key):
+                traffic = int(val * per_step[unit_key] / launches_per_step)
+    roofline = {"bound": "hbm", "kernel": kern, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
+                "fallback 6.8 TB/s"}
+    # integer-pipe view of the Myers kernel (the hot loop is LOP3/IADD/SHF work)
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    int_peak = 152 * 128 * sm_mhz * 1e6 / 1e12
+    myers_ops = per_step["candidates"] * L * 21
+    t_verify = per_step["ms_verify"] / 1e3
+    int_pipe = {"kernel": "k_verify", "ops_per_step": int(myers_ops), "achieved_tops": round(myers_ops / t_verify / 1e12, 2)
+                if t_verify > 0 else None, "peak_tops": round(int_peak, 2),
+                "frac": round(myers_ops / t_verify / 1e12 / int_peak, 4) if t_verify > 0 else None,
+                "ops_model": "21 int ops per read base per candidate (17 recurrence + 4 Peq update)",
+                "peak_model": "152 SMs x 128 int lanes x median SM clock under load"}
+
+    line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(tot_elapsed / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded genome and reads of the workload's shapes; no public dataset)",
+            "config": {**WORKLOAD, "block_reads": block, "parallelism": f"replicas x{ws} (reads sharded by rank)",
+                       "l2": "inputs larger than L2 (reads 150 MB, index ~0.2 GB); no flush"},
+            "gcups": round(gcups, 2), "index_build_s": round(index_build_s, 3),
+            "per_step": {k: int(v) if not k.startswith("ms_") else round(v, 3) for k, v in per_step.items()},
+            "stages": stage_rows, "clocks": clk, "e2e": e2e,
+            "gpu_launches": int(acc["launches"]), "roofline": roofline, "int_pipe": int_pipe}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        arrays = ix.download()
+        mix = host_map_index(arrays, w["k"])
+        threads = os.cpu_count() or 1
+        v, n, dt, kind = timed_cpu_sample(mix, reads, lens, w["e"], threads, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": round(v, 1), "unit": UNIT, "cores": threads, "kind": kind,
+                                "sample": f"first {n} reads of the workload, {dt:.1f} s, {threads} threads"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def count_mapped(buf, nreads):
+    return nreads - int(buf.c.n_unmapped)
+
+
+# ------------------------------------------------------------ reference arm
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import build as obuild
+    from oracle import pyoracle as po
+    w = WORKLOAD
+    g, reads, lens = make_workload(0)
+    kind = "reference"
+    t0 = time.perf_counter()
+    exe = os.path.join(obuild.REF_DIR, "serial_index")
+    with tempfile.TemporaryDirectory() as td:
+        if po.have_ref() and os.path.exists(exe):
+            fa = os.path.join(td, "g.fa")
+            with open(fa, "wb") as f:
+                f.write(b">chrS synthetic\n")
+                for i in range(0, g.size, 100_000):
+                    f.write(g[i:i + 100_000].tobytes() + b"\n")
+            prefix = os.path.join(td, "ix")
+            subprocess.run([exe, "-i" + fa, "-p" + prefix, f"-s{w['k']}"], check=True, capture_output=True)
+            arrays = {}
+            for ext, dt in ((".hash_count", np.uint32), (".hash_offset", np.uint32), (".positions", np.uint32),
+                            (".pos_lseeds", np.uint16), (".base_2bits", np.uint32), (".base_3bits", np.uint32)):
+                arrays[ext[1:]] = np.fromfile(prefix + ext, dtype=dt)
+        else:
+            kind = "port"
+            hix = po.build_index(g, w["k"])
+            arrays = dict(hash_count=hix.hash_count, hash_offset=hix.hash_offset_end, positions=hix.positions,
+                          pos_lseeds=hix.pos_lseeds, base_2bits=hix.base_2bits, base_3bits=hix.base_3bits)
+    index_build_s = time.perf_counter() - t0
+    mix = host_map_index(arrays, w["k"])
+    threads = os.cpu_count() or 1
+    # size one step to ~args.ref_step_seconds
+    rate, n, _, kind2 = timed_cpu_sample(mix, reads, lens, w["e"], threads, 1.0)
+    kind = kind if kind2 == "reference" else "port"
+    per_step = int(min(reads.shape[0], max(1024, rate * args.ref_step_seconds)))
+    total_mapped = 0
+    tsum = 0.0
+    off = 0
+    for s in range(args.warmup + args.steps):
+        lo = off % reads.shape[0]
+        hi = min(reads.shape[0], lo + per_step)
+        t0 = time.perf_counter()
+        mapped, _ = cpu_map(mix, reads[lo:hi], lens[lo:hi], w["e"], threads)
+        dt = time.perf_counter() - t0
+        off = hi
+        if s >= args.warmup:
+            total_mapped += mapped
+            tsum += dt
+    value = total_mapped / tsum
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tsum / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded genome and reads of the workload's shapes; no public dataset)",
+            "config": {**WORKLOAD, "parallelism": "host threads"},
+            "index_build_s": round(index_build_s, 3),
+            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{per_step} reads per step of the workload, {threads} threads"},
+            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--block", type=int, default=262144, help="reads per mapping block")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=4.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--genome-bp", type=int, default=WORKLOAD["genome_bp"], help="smaller genome for quick checks")
+    ap.add_argument("--nreads", type=int, default=WORKLOAD["reads"], help="fewer reads for quick checks")
+    args = ap.parse_args()
+    if args.genome_bp != WORKLOAD["genome_bp"] or args.nreads != WORKLOAD["reads"]:
+        WORKLOAD.update(genome_bp=args.genome_bp, reads=args.nreads,
+                        workload=f"reduced check: {args.genome_bp} bp genome, {args.nreads} x 150 bp reads, e=7")
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

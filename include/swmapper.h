@@ -155,11 +155,28 @@ int swm_map_device(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
                    uint64_t reads_num, uint32_t errors, const uint8_t *d_errors);
 int swm_map_fetch(swm_mapper *m, swm_result *r);
 
+/* Packed results: the same records without the reference's fixed strides
+ * (record q's words follow record q - 1's; its CIGAR bytes likewise), for
+ * callers that do not need the ref_info_t layout. */
+typedef struct {
+    uint32_t *words;            /* [cur_read, n | primary<<31, loc * n] per record */
+    uint8_t *cigar;             /* [NM, len, text] per location, records back to back */
+    uint32_t *record_cigar_len; /* CIGAR bytes of each record                      */
+    uint32_t *unmapped;         /* cur_read ids (2 * read + 1) of unmapped reads   */
+    uint64_t words_cap, cigar_cap, records_cap, unmapped_cap;
+    uint64_t n_words, n_cigar, n_records, n_unmapped;
+} swm_packed_result;
+
+int swm_map_fetch_packed(swm_mapper *m, swm_packed_result *r);
+
+/* swm_map_wait with packed results. */
+int swm_map_wait_packed(swm_mapper *m, swm_packed_result *r);
+
 int swm_mapper_stats(const swm_mapper *m, swm_map_stats *s);
 
 /* Per-stage device time of the last block in milliseconds (CUDA events on the
- * mapper's stream); names are "seed", "plan", "candidates", "verify",
- * "records", "total". Returns SWM_ERR_ARG for an unknown name. */
+ * mapper's stream); names are "seed", "plan", "candidates", "compact",
+ * "verify", "records", "total". Returns SWM_ERR_ARG for an unknown name. */
 int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float *ms);
 
 /* Kernel launches queued for the last block. */

@@ -272,15 +272,23 @@ def reflib():
     return _ref
 
 
-def ref_map_reads(mix: MapIndex, reads: np.ndarray, lens: np.ndarray, e: int, nthreads: int = 1) -> MapResult:
+def out_buffers(nreads: int):
+    """Output buffers in the reference layout for blocks of up to nreads reads."""
+    cap = max(16, 4 * nreads + 64)
+    return (np.zeros((cap, RECORD_WORDS), dtype=np.uint32), np.zeros((cap, CIGAR_STRIDE), dtype=np.uint8),
+            np.zeros(max(1, 2 * nreads), dtype=np.uint32))
+
+
+def ref_map_reads(mix: MapIndex, reads: np.ndarray, lens: np.ndarray, e: int, nthreads: int = 1,
+                  out=None) -> MapResult:
     """The reference's own get_positions() over the reads (records sorted canonically)."""
     reads = np.ascontiguousarray(reads, dtype=np.uint8)
     lens = np.ascontiguousarray(lens, dtype=np.uint32)
     nreads, stride = reads.shape
-    cap = max(16, 4 * nreads + 64)
-    ref_pos = np.zeros((cap, RECORD_WORDS), dtype=np.uint32)
-    cigar = np.zeros((cap, CIGAR_STRIDE), dtype=np.uint8)
-    unm = np.zeros(max(1, 2 * nreads), dtype=np.uint32)
+    ref_pos, cigar, unm = out if out is not None else out_buffers(nreads)
+    cap = ref_pos.shape[0]
+    if cap < 4 * nreads + 16 or unm.size < 2 * nreads:
+        raise ValueError("output buffers too small for this block")
     nrec = C.c_uint64()
     nun = C.c_uint64()
     rc = reflib().swref_map(mix.hash_offset.ctypes.data, mix.positions.ctypes.data, mix.pos_lseeds.ctypes.data,

@@ -39,6 +39,13 @@ class Result(C.Structure):
                 ("n_unmapped", C.c_uint64)]
 
 
+class PackedResult(C.Structure):
+    _fields_ = [("words", C.c_void_p), ("cigar", C.c_void_p), ("record_cigar_len", C.c_void_p),
+                ("unmapped", C.c_void_p), ("words_cap", C.c_uint64), ("cigar_cap", C.c_uint64),
+                ("records_cap", C.c_uint64), ("unmapped_cap", C.c_uint64), ("n_words", C.c_uint64),
+                ("n_cigar", C.c_uint64), ("n_records", C.c_uint64), ("n_unmapped", C.c_uint64)]
+
+
 STAT_FIELDS = ["reads", "items", "chunks", "batches", "fetched", "candidates", "cells", "passed", "records",
                "locations", "mapped_reads", "retries", "h2d_bytes", "d2h_bytes"]
 
@@ -78,6 +85,8 @@ def lib():
         L.swm_map_wait.argtypes = [vp, C.POINTER(Result)]
         L.swm_map_device.argtypes = [vp, vp, vp, u64, u64, u32, vp]
         L.swm_map_fetch.argtypes = [vp, C.POINTER(Result)]
+        L.swm_map_fetch_packed.argtypes = [vp, C.POINTER(PackedResult)]
+        L.swm_map_wait_packed.argtypes = [vp, C.POINTER(PackedResult)]
         L.swm_mapper_stats.argtypes = [vp, C.POINTER(MapStats)]
         L.swm_mapper_stage_ms.argtypes = [vp, C.c_char_p, C.POINTER(C.c_float)]
         L.swm_mapper_launches.argtypes = [vp]
@@ -204,6 +213,20 @@ class Mapper:
         _check(lib().swm_map_batch(self._h, C.byref(b), C.byref(res)), "swm_map_batch")
         return MapOutput(ref_pos[:res.n_records], cigar[:res.n_records], unm[:res.n_unmapped], self.stats())
 
+    def submit(self, reads: np.ndarray, lens: np.ndarray, errors: int, errors_per_read=None) -> None:
+        """Queue a block (swm_map_submit); the inputs are copied before it returns."""
+        reads = np.ascontiguousarray(reads, np.uint8)
+        lens = np.ascontiguousarray(lens, np.uint32)
+        n, stride = reads.shape
+        epr = None if errors_per_read is None else np.ascontiguousarray(errors_per_read, np.uint8)
+        b = Batch(reads.ctypes.data, lens.ctypes.data, stride, n, errors, epr.ctypes.data if epr is not None else None)
+        _check(lib().swm_map_submit(self._h, C.byref(b)), "swm_map_submit")
+
+    def wait_packed(self, out: "PackedBuffers") -> "PackedBuffers":
+        """Wait for the queued block and copy its records out packed (swm_map_wait_packed)."""
+        _check(lib().swm_map_wait_packed(self._h, C.byref(out.c)), "swm_map_wait_packed")
+        return out
+
     def map_device(self, d_reads: int, d_lens: int, stride: int, nreads: int, errors: int, d_errors: int | None = None):
         """Map reads already resident in device memory (pointers as ints)."""
         _check(lib().swm_map_device(self._h, d_reads, d_lens, stride, nreads, errors, d_errors),
@@ -252,3 +275,32 @@ class Mapper:
             self.close()
         except Exception:
             pass
+
+
+class PackedBuffers:
+    """Host buffers for packed results (swm_packed_result), reusable across blocks."""
+
+    def __init__(self, nreads: int, words_per_read: int = 16, cigar_per_read: int = 64, records_per_read: int = 4):
+        self.words = np.zeros(max(64, nreads * words_per_read), np.uint32)
+        self.cigar = np.zeros(max(256, nreads * cigar_per_read), np.uint8)
+        self.rlen = np.zeros(max(16, nreads * records_per_read), np.uint32)
+        self.unmapped = np.zeros(max(1, nreads), np.uint32)
+        self.c = PackedResult(self.words.ctypes.data, self.cigar.ctypes.data, self.rlen.ctypes.data,
+                              self.unmapped.ctypes.data, self.words.size, self.cigar.size, self.rlen.size,
+                              self.unmapped.size, 0, 0, 0, 0)
+
+    def records(self):
+        """Same canonical form as MapOutput.records()."""
+        out = []
+        w = self.words[:self.c.n_words]
+        cg = self.cigar[:self.c.n_cigar]
+        wp = cp = 0
+        for q in range(self.c.n_records):
+            n = int(w[wp + 1] & 0x0FFFFFFF)
+            locs = tuple(int(x) for x in w[wp + 2:wp + 2 + n])
+            ln = int(self.rlen[q])
+            out.append((int(w[wp]), int(w[wp + 1]) >> 31, locs, bytes(cg[cp:cp + ln])))
+            wp += 2 + n
+            cp += ln
+        return out
+

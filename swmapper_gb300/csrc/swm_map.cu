@@ -120,7 +120,7 @@ struct swm_mapper {
     uint32_t tot[TOT_N];
     swm_map_stats stats;
     cudaEvent_t ev[8];
-    float stage_ms[6];
+    float stage_ms[7];
     uint64_t launches;
 };
 
@@ -1164,6 +1164,7 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
                                                                                            m->cap_chunks);
     m->launches++;
     LAUNCH_CHECK();
+    SWM_CUDA(cudaEventRecord(m->ev[3], st));
     rc = swm_exclusive_scan(B.bt_cnt, B.bt_coff, B.tot + TOT_CHUNKS, 0, m->cap_chunks, B.scan_tmp, B.tot + TOT_CANDS,
                             st);
     if (rc) return rc;
@@ -1171,13 +1172,13 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     k_compact<<<grid_cap(m->cap_chunks * 32, 256, 16), 256, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands);
     m->launches++;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[3], st));
+    SWM_CUDA(cudaEventRecord(m->ev[4], st));
     k_verify<<<grid_cap(m->cap_cands, 128, 64), 128, 0, st>>>(d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
                                                                ix->ref_length, B, m->cap_chunks, m->cap_elems,
                                                                m->cap_cands, m->cap_arena);
     m->launches++;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[4], st));
+    SWM_CUDA(cudaEventRecord(m->ev[5], st));
     k_records<false><<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems, m->cap_cands,
                                                                  m->cap_recs, m->cap_words, m->cap_bytes);
     rc = swm_exclusive_scan(B.it_nrec, B.it_recoff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_RECS, st);
@@ -1191,7 +1192,7 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     k_batches_stat<<<grid_cap(nitems, 256, 8), 256, 0, st>>>(nitems, B);
     m->launches += 12;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[5], st));
+    SWM_CUDA(cudaEventRecord(m->ev[6], st));
     return SWM_OK;
 }
 
@@ -1258,12 +1259,12 @@ static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *a
         return alloc_work(m);
     }
     float t;
-    for (int i = 0; i < 5; i++) {
+    for (int i = 0; i < 6; i++) {
         cudaEventElapsedTime(&t, m->ev[i], m->ev[i + 1]);
         m->stage_ms[i] = t;
     }
-    cudaEventElapsedTime(&t, m->ev[0], m->ev[5]);
-    m->stage_ms[5] = t;
+    cudaEventElapsedTime(&t, m->ev[0], m->ev[6]);
+    m->stage_ms[6] = t;
     const unsigned long long *stat = m->h_stat;
     swm_map_stats &S = m->stats;
     memset(&S, 0, sizeof S);
@@ -1357,11 +1358,8 @@ static int ensure_host(void **p, uint64_t *cap, uint64_t need, size_t elt) {
     return SWM_OK;
 }
 
-// Copy the packed records of the last block to pinned staging and expand
-// them into the reference layout (records at SWM_RECORD_WORDS, CIGARs at
-// SWM_CIGAR_STRIDE, unmapped ids).
-extern "C" int swm_map_fetch(swm_mapper *m, swm_result *r) {
-    if (!m || !r) return SWM_ERR_ARG;
+// Copy the packed records of the last block to pinned staging.
+static int download_results(swm_mapper *m) {
     if (!m->have_result) return SWM_ERR_STATE;
     SWM_CUDA(cudaSetDevice(m->device));
     const uint64_t nitems = 2 * m->cur_n;
@@ -1384,6 +1382,16 @@ extern "C" int swm_map_fetch(swm_mapper *m, swm_result *r) {
     if (nitems) SWM_CUDA(cudaMemcpyAsync(m->h_nrec, m->b.it_nrec, nitems * 4, cudaMemcpyDeviceToHost, st));
     SWM_CUDA(cudaStreamSynchronize(st));
     m->stats.d2h_bytes = nw * 4 + nby + nrec * 12 + nitems * 4 + TOT_N * 4 + ST_N * 8;
+    return SWM_OK;
+}
+
+// Expand the packed records of the last block into the reference layout
+// (records at SWM_RECORD_WORDS, CIGARs at SWM_CIGAR_STRIDE, unmapped ids).
+extern "C" int swm_map_fetch(swm_mapper *m, swm_result *r) {
+    if (!m || !r) return SWM_ERR_ARG;
+    int rc = download_results(m);
+    if (rc) return rc;
+    const uint64_t nrec = m->tot[TOT_RECS];
     int status = SWM_OK;
     r->n_records = nrec;
     for (uint64_t q = 0; q < nrec; q++) {
@@ -1412,6 +1420,38 @@ extern "C" int swm_map_fetch(swm_mapper *m, swm_result *r) {
     r->n_unmapped = nu;
     if (status) swm_set_error("result buffers too small (records %llu, unmapped %llu)", (unsigned long long)nrec,
                               (unsigned long long)nu);
+    return status;
+}
+
+extern "C" int swm_map_fetch_packed(swm_mapper *m, swm_packed_result *r) {
+    if (!m || !r) return SWM_ERR_ARG;
+    int rc = download_results(m);
+    if (rc) return rc;
+    const uint64_t nrec = m->tot[TOT_RECS], nw = m->tot[TOT_WORDS], nby = m->tot[TOT_BYTES];
+    r->n_records = nrec;
+    r->n_words = nw;
+    r->n_cigar = nby;
+    int status = SWM_OK;
+    if (nw > r->words_cap || nby > r->cigar_cap || nrec > r->records_cap) {
+        status = SWM_ERR_OVERFLOW;
+    } else {
+        // records are laid out in order on the device, so the packed words and
+        // bytes are already contiguous
+        if (nw) memcpy(r->words, m->h_w, nw * 4);
+        if (nby) memcpy(r->cigar, m->h_c, nby);
+        if (r->record_cigar_len && nrec) memcpy(r->record_cigar_len, m->h_rl, nrec * 4);
+    }
+    uint64_t nu = 0;
+    for (uint64_t rd = 0; rd < m->cur_n; rd++) {
+        if (m->h_nrec[2 * rd] + m->h_nrec[2 * rd + 1] == 0) {
+            if (nu < r->unmapped_cap && r->unmapped) r->unmapped[nu] = (uint32_t)(2 * rd + 1);
+            else status = SWM_ERR_OVERFLOW;
+            nu++;
+        }
+    }
+    r->n_unmapped = nu;
+    if (status) swm_set_error("packed result buffers too small (words %llu, bytes %llu, records %llu)",
+                              (unsigned long long)nw, (unsigned long long)nby, (unsigned long long)nrec);
     return status;
 }
 
@@ -1481,6 +1521,22 @@ extern "C" int swm_map_wait(swm_mapper *m, swm_result *r) {
     return swm_map_fetch(m, r);
 }
 
+extern "C" int swm_map_wait_packed(swm_mapper *m, swm_packed_result *r) {
+    if (!m || !r) return SWM_ERR_ARG;
+    if (!m->pending) return SWM_ERR_STATE;
+    SWM_CUDA(cudaSetDevice(m->device));
+    m->pending = 0;
+    int again = 0;
+    int rc = finish_block(m, (uint32_t)m->cur_n, 0, &again);
+    if (rc) return rc;
+    if (again) {
+        rc = run_block(m, m->d_reads, m->d_lens, m->cur_stride, (uint32_t)m->cur_n, m->cur_errors,
+                       m->cur_e ? m->d_e : nullptr, 1);
+        if (rc) return rc;
+    }
+    return swm_map_fetch_packed(m, r);
+}
+
 extern "C" int swm_map_batch(swm_mapper *m, const swm_batch *b, swm_result *r) {
     int rc = swm_map_submit(m, b);
     if (rc) return rc;
@@ -1494,9 +1550,9 @@ extern "C" int swm_mapper_stats(const swm_mapper *m, swm_map_stats *s) {
 }
 
 extern "C" int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float *ms) {
-    static const char *names[6] = {"seed", "plan", "candidates", "verify", "records", "total"};
+    static const char *names[7] = {"seed", "plan", "candidates", "compact", "verify", "records", "total"};
     if (!m || !stage || !ms) return SWM_ERR_ARG;
-    for (int i = 0; i < 6; i++)
+    for (int i = 0; i < 7; i++)
         if (!strcmp(stage, names[i])) {
             *ms = m->stage_ms[i];
             return SWM_OK;

@@ -146,3 +146,29 @@ def test_gpu_rejects_out_of_envelope(cuda_lib):
         m.map(np.zeros((1, 100), np.uint8), np.array([100], np.uint32), 16)
     with pytest.raises(cuda_lib.SwmError):
         m.map(np.zeros((5, 100), np.uint8), np.full(5, 100, np.uint32), 5)
+
+
+def test_gpu_packed_pingpong_equals_strided(cuda_lib):
+    """submit / wait_packed on two mappers (the host double-buffering of
+    mapper_mpe.c:972-1106) gives the same records as swm_map_batch."""
+    g = genome(2_000_000, 19, "repeats100m")
+    reads, lens, _, _ = synth.reads(g, 6000, 150, 150, 0.03, seed=20)
+    ix = cuda_lib.Index.build(g)
+    ma, mb = cuda_lib.Mapper(ix, max_reads=2000), cuda_lib.Mapper(ix, max_reads=2000)
+    want = []
+    for b0 in range(0, 6000, 2000):
+        recs = ma.map(reads[b0:b0 + 2000], lens[b0:b0 + 2000], 7).records()
+        want.extend((r[0] + 2 * b0,) + r[1:] for r in recs)
+    got = []
+    bufs = [cuda_lib.PackedBuffers(2000), cuda_lib.PackedBuffers(2000)]
+    ms = [ma, mb]
+    ms[0].submit(reads[0:2000], lens[0:2000], 7)
+    ms[1].submit(reads[2000:4000], lens[2000:4000], 7)
+    ms[0].wait_packed(bufs[0])
+    got.extend((r[0],) + r[1:] for r in bufs[0].records())
+    ms[0].submit(reads[4000:6000], lens[4000:6000], 7)
+    ms[1].wait_packed(bufs[1])
+    got.extend((r[0] + 4000,) + r[1:] for r in bufs[1].records())
+    ms[0].wait_packed(bufs[0])
+    got.extend((r[0] + 8000,) + r[1:] for r in bufs[0].records())
+    assert got == want
