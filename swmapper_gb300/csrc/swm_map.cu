@@ -36,7 +36,7 @@
 
 // item = 2 * read + strand (cur_read, mapper_cpe.c:2628)
 
-enum { VR_FAIL = 0, VR_HAM = 1, VR_TB = 2, VR_INVALID = 3 };
+enum { VR_FAIL = 0, VR_HAM = 1, VR_TB = 2, VR_INVALID = 3, VR_NEEDTB = 4 };
 enum { OV_CHUNKS = 1, OV_ELEMS = 2, OV_CANDS = 4, OV_RECS = 8, OV_ARENA = 16, OV_BAD = 32 };
 enum {
     ST_BATCHES = 0,
@@ -62,10 +62,10 @@ struct MapBufs {
     uint32_t *it_choff, *it_eloff; // items + 1
     uint32_t *it_nrec, *it_nw, *it_nb;
     uint32_t *it_recoff, *it_woff, *it_boff; // items + 1
-    // per chunk / batch slot (cap_chunks)
+    uint32_t *it_ncand, *it_coff;            // candidates per item, dense offsets (items + 1)
+    // per chunk / batch slot (cap_chunks; batch b of an item sits at slot it_choff + b)
     uint32_t *ch_g, *ch_meta;
-    uint32_t *bt_c0, *bt_c1, *bt_e0, *bt_item, *bt_cnt;
-    uint32_t *bt_coff; // cap_chunks + 1
+    uint32_t *bt_c0, *bt_c1, *bt_e0, *bt_cnt;
     // upper-bound candidates (cap_elems)
     uint32_t *cand_ub;
     // dense candidates (cap_cands)
@@ -316,21 +316,11 @@ __global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const uint32_t *_
         if ((uint64_t)cb + nch > cap_chunks) {
             atomicOr(&B.tot[TOT_FLAGS], OV_CHUNKS);
             B.it_nbat[item] = 0;
-            for (uint64_t q = cb; q < (uint64_t)cb + nch && q < cap_chunks; q++) {
-                B.bt_c0[q] = 0;
-                B.bt_c1[q] = 0;
-                B.bt_item[q] = item;
-            }
             continue;
         }
         if ((uint64_t)eb + B.it_nel[item] > cap_elems) {
             atomicOr(&B.tot[TOT_FLAGS], OV_ELEMS);
             B.it_nbat[item] = 0;
-            for (uint32_t q = 0; q < nch; q++) {
-                B.bt_c0[cb + q] = 0;
-                B.bt_c1[cb + q] = 0;
-                B.bt_item[cb + q] = item;
-            }
             continue;
         }
         const uint32_t ns = B.it_nsel[item];
@@ -411,7 +401,6 @@ __global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const uint32_t *_
                     B.bt_c0[slot] = cb + bc0;
                     B.bt_c1[slot] = cb + c;
                     B.bt_e0[slot] = eb + be0;
-                    B.bt_item[slot] = item;
                     b++;
                 }
                 bc0 = c;
@@ -422,11 +411,6 @@ __global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const uint32_t *_
             }
         }
 #undef EMIT
-        for (uint32_t q = b; q < nch; q++) {
-            B.bt_c0[cb + q] = 0;
-            B.bt_c1[cb + q] = 0;
-            B.bt_item[cb + q] = item;
-        }
         B.it_nbat[item] = b;
     }
 }
@@ -451,105 +435,158 @@ __device__ __forceinline__ void warp_sort_small(uint32_t &v) {
     }
 }
 
-__global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(const uint32_t *__restrict__ pos,
+#define CAND_MAXCH 128 // chunks (runs) per batch: block_size < 256 allows at most 128
+
+struct CandSmem {
+    uint32_t g[CAND_MAXCH];      // first global index of each chunk
+    uint32_t meta[CAND_MAXCH];   // len | sel << 8
+    uint16_t start[CAND_MAXCH + 1];
+    uint32_t sel[SWM_MAX_SEL];   // base | shift << 16 | rl << 20 | rh << 24
+    uint8_t cof[SWM_BATCH_POSITIONS];  // element -> chunk
+    uint32_t buf[SWM_BATCH_POSITIONS]; // kept positions
+};
+
+__device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, d);
+        if ((int)lane_id() >= d) v += t;
+    }
+    return v;
+}
+
+// One warp per item: every batch of the item, element-parallel gather of
+// positions and flank codes, position adjust, flank filter, sort-unique.
+__global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(uint32_t nitems, const uint32_t *__restrict__ pos,
                                                           const uint16_t *__restrict__ lseed, MapBufs B,
-                                                          uint64_t cap_chunks) {
-    __shared__ uint32_t sbuf[CAND_WARPS][SWM_BATCH_POSITIONS];
-    if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks) return;
+                                                          uint64_t cap_chunks, uint64_t cap_elems) {
+    __shared__ CandSmem sm_all[CAND_WARPS];
+    if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
-    uint32_t *buf = sbuf[wib];
-    const uint64_t nslots_all = B.tot[TOT_CHUNKS];
-    const uint64_t nslots = nslots_all < cap_chunks ? nslots_all : cap_chunks;
+    CandSmem &S = sm_all[wib];
     const uint32_t lt = (1u << lane) - 1;
-    for (uint64_t s = (uint64_t)blockIdx.x * CAND_WARPS + wib; s < nslots; s += (uint64_t)gridDim.x * CAND_WARPS) {
-        const uint32_t c0 = B.bt_c0[s], c1 = B.bt_c1[s];
-        if (c0 == c1) {
-            if (lane == 0) B.bt_cnt[s] = 0;
-            continue;
-        }
-        const uint32_t item = B.bt_item[s], e0 = B.bt_e0[s];
-        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
-        uint32_t kept = 0, j = 0;
-        for (uint32_t c = c0; c < c1; c++) {
-            const uint32_t g = B.ch_g[c], meta = B.ch_meta[c];
-            const uint32_t len = meta & 0xffu, sel = meta >> 8;
-            const uint32_t sm = B.sel_meta[sb + sel];
-            const uint32_t base = sm & 0xffffu, shift = (sm >> 16) & 0xfu, rl = (sm >> 20) & 0xfu,
-                           rh = (sm >> 24) & 0xfu;
-            bool ok = false;
-            uint32_t p = 0;
-            if (lane < len) {
-                uint32_t raw = pos[g + lane];
-                uint32_t ls = lseed[g + lane];
-                p = raw > base ? raw - base : 0u;  // adjust_ref_pos_rmdup, 1893-1917
-                uint32_t rs = (((ls >> shift) ^ rl) | ((ls >> (6 + shift)) ^ rh)) & 7u; // long_seeds_filter, 2107-2112
-                ok = (rs == 0) && (j + lane != 0); // element 0 of the batch is dropped (2113)
-            }
-            uint32_t m = __ballot_sync(0xffffffffu, ok);
-            if (ok) buf[kept + __popc(m & lt)] = p;
-            kept += __popc(m);
-            j += len;
-        }
-        __syncwarp();
-        uint32_t u = 0;
-        uint32_t *dst = B.cand_ub + e0;
-        if (kept <= 32) {
-            uint32_t v = lane < kept ? buf[lane] : 0xffffffffu;
-            warp_sort_small(v);
-            uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
-            bool keep = lane < kept && (lane == 0 || prev != v);
-            uint32_t m = __ballot_sync(0xffffffffu, keep);
-            if (keep) dst[__popc(m & lt)] = v;
-            u = __popc(m);
-        } else {
-            uint32_t n2 = 64;
-            while (n2 < kept) n2 <<= 1;
-            for (uint32_t i = kept + lane; i < n2; i += 32) buf[i] = 0xffffffffu;
-            __syncwarp();
-            for (uint32_t size = 2; size <= n2; size <<= 1) {
-                for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-                    for (uint32_t i = lane; i < n2 / 2; i += 32) {
-                        uint32_t lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
-                        bool up = ((lo & size) == 0);
-                        uint32_t a = buf[lo], d = buf[hi];
-                        if ((a > d) == up) {
-                            buf[lo] = d;
-                            buf[hi] = a;
+    for (uint32_t item = blockIdx.x * CAND_WARPS + wib; item < nitems; item += gridDim.x * CAND_WARPS) {
+        const uint32_t nb = B.it_nbat[item];
+        uint32_t total = 0;
+        if (nb) {
+            const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+            const uint32_t ns = B.it_nsel[item];
+            for (uint32_t i = lane; i < ns; i += 32) S.sel[i] = B.sel_meta[sb + i];
+            const uint32_t cb = B.it_choff[item];
+            for (uint32_t b = 0; b < nb; b++) {
+                const uint32_t slot = cb + b;
+                const uint32_t c0 = B.bt_c0[slot], nchk = B.bt_c1[slot] - c0, e0 = B.bt_e0[slot];
+                uint32_t carry = 0;
+                for (uint32_t q0 = 0; q0 < nchk; q0 += 32) {
+                    const uint32_t q = q0 + lane;
+                    uint32_t len = 0;
+                    if (q < nchk) {
+                        const uint32_t meta = B.ch_meta[c0 + q];
+                        S.g[q] = B.ch_g[c0 + q];
+                        S.meta[q] = meta;
+                        len = meta & 0xffu;
+                    }
+                    const uint32_t inc = warp_scan_incl(len);
+                    if (q < nchk) S.start[q] = (uint16_t)(carry + inc - len);
+                    carry += __shfl_sync(0xffffffffu, inc, 31);
+                }
+                const uint32_t E = carry;
+                __syncwarp();
+                for (uint32_t q = lane; q < nchk; q += 32) {
+                    const uint32_t st = S.start[q], len = S.meta[q] & 0xffu;
+                    for (uint32_t t = 0; t < len; t++) S.cof[st + t] = (uint8_t)q;
+                }
+                __syncwarp();
+                uint32_t kept = 0;
+                for (uint32_t eb = 0; eb < E; eb += 32) {
+                    const uint32_t e = eb + lane;
+                    bool ok = false;
+                    uint32_t p = 0;
+                    if (e < E) {
+                        const uint32_t q = S.cof[e];
+                        const uint32_t g = S.g[q] + (e - S.start[q]);
+                        const uint32_t sm = S.sel[S.meta[q] >> 8];
+                        const uint32_t base = sm & 0xffffu, shift = (sm >> 16) & 0xfu, rl = (sm >> 20) & 0xfu,
+                                       rh = (sm >> 24) & 0xfu;
+                        const uint32_t raw = pos[g];
+                        const uint32_t ls = lseed[g];
+                        p = raw > base ? raw - base : 0u; // adjust_ref_pos_rmdup, 1893-1917
+                        const uint32_t rs = (((ls >> shift) ^ rl) | ((ls >> (6 + shift)) ^ rh)) & 7u; // 2107-2112
+                        ok = (rs == 0) && (e != 0); // element 0 of the batch is dropped (2113)
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, ok);
+                    if (ok) S.buf[kept + __popc(m & lt)] = p;
+                    kept += __popc(m);
+                }
+                __syncwarp();
+                uint32_t u = 0;
+                uint32_t *dst = B.cand_ub + e0;
+                if (kept <= 32) {
+                    uint32_t v = lane < kept ? S.buf[lane] : 0xffffffffu;
+                    warp_sort_small(v);
+                    const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
+                    const bool keep = lane < kept && (lane == 0 || prev != v);
+                    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+                    if (keep) dst[__popc(m & lt)] = v;
+                    u = __popc(m);
+                } else {
+                    uint32_t n2 = 64;
+                    while (n2 < kept) n2 <<= 1;
+                    uint32_t *buf = S.buf;
+                    for (uint32_t i = kept + lane; i < n2; i += 32) buf[i] = 0xffffffffu;
+                    __syncwarp();
+                    for (uint32_t size = 2; size <= n2; size <<= 1) {
+                        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                            for (uint32_t i = lane; i < n2 / 2; i += 32) {
+                                const uint32_t lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
+                                const bool up = ((lo & size) == 0);
+                                const uint32_t a = buf[lo], d = buf[hi];
+                                if ((a > d) == up) {
+                                    buf[lo] = d;
+                                    buf[hi] = a;
+                                }
+                            }
+                            __syncwarp();
                         }
                     }
-                    __syncwarp();
+                    for (uint32_t i0 = 0; i0 < kept; i0 += 32) {
+                        const uint32_t i = i0 + lane;
+                        const bool keep = i < kept && (i == 0 || buf[i - 1] != buf[i]);
+                        const uint32_t m = __ballot_sync(0xffffffffu, keep);
+                        if (keep) dst[u + __popc(m & lt)] = buf[i];
+                        u += __popc(m);
+                    }
                 }
-            }
-            for (uint32_t i0 = 0; i0 < kept; i0 += 32) {
-                uint32_t i = i0 + lane;
-                bool keep = i < kept && (i == 0 || buf[i - 1] != buf[i]);
-                uint32_t m = __ballot_sync(0xffffffffu, keep);
-                if (keep) dst[u + __popc(m & lt)] = buf[i];
-                u += __popc(m);
+                if (lane == 0) B.bt_cnt[slot] = u;
+                total += u;
+                __syncwarp();
             }
         }
-        if (lane == 0) B.bt_cnt[s] = u;
-        __syncwarp();
+        if (lane == 0) B.it_ncand[item] = total;
     }
 }
 
-__global__ void k_compact(MapBufs B, uint64_t cap_chunks, uint64_t cap_elems, uint64_t cap_cands) {
-    if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+// Dense candidate list: item by item, batch by batch, in verification order.
+__global__ void k_compact(uint32_t nitems, MapBufs B, uint64_t cap_chunks, uint64_t cap_elems, uint64_t cap_cands) {
+    if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     const uint32_t lane = lane_id();
-    const uint64_t nslots_all = B.tot[TOT_CHUNKS];
-    const uint64_t nslots = nslots_all < cap_chunks ? nslots_all : cap_chunks;
-    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-    for (uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslots; s += nwarps) {
-        const uint32_t n = B.bt_cnt[s];
-        if (!n) continue;
-        const uint32_t o = B.bt_coff[s], e0 = B.bt_e0[s], item = B.bt_item[s];
-        if ((uint64_t)o + n > cap_cands) {
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < nitems; item += nwarps) {
+        const uint32_t nb = B.it_nbat[item];
+        if (!nb) continue;
+        uint32_t o = B.it_coff[item];
+        if ((uint64_t)o + B.it_ncand[item] > cap_cands) {
             if (lane == 0) atomicOr(&B.tot[TOT_FLAGS], OV_CANDS);
             continue;
         }
-        for (uint32_t j = lane; j < n; j += 32) {
-            B.cc_pos[o + j] = B.cand_ub[e0 + j];
-            B.cc_item[o + j] = item;
+        const uint32_t cb = B.it_choff[item];
+        for (uint32_t b = 0; b < nb; b++) {
+            const uint32_t n = B.bt_cnt[cb + b], e0 = B.bt_e0[cb + b];
+            for (uint32_t j = lane; j < n; j += 32) {
+                B.cc_pos[o + j] = B.cand_ub[e0 + j];
+                B.cc_item[o + j] = item;
+            }
+            o += n;
         }
     }
 }
@@ -689,6 +726,30 @@ __device__ __forceinline__ int put_len(uint8_t *p, uint32_t v) {
     return n;
 }
 
+// Aligned window bit planes of [ws, ws + 32 * SWM_WIN_WORDS): bit b of
+// WL[j] / WH[j] is the lo / hi bit of genome base ws + 32j + b
+// (shift_ref_pos_v, mapper_cpe.c:1509-1586); zero past the index padding.
+__device__ __forceinline__ void load_window(const uint32_t *__restrict__ b2, uint64_t b2_words, uint32_t ws,
+                                            uint32_t L, uint32_t e, uint32_t *WL, uint32_t *WH) {
+    const uint64_t w0 = (uint64_t)(ws >> 5) * 2;
+    const uint32_t sh = ws & 31;
+    const uint32_t nw = (L + 2 * e + 31) / 32 + 2;
+    uint32_t plo = (w0 < b2_words) ? b2[w0] : 0u, phi = (w0 + 1 < b2_words) ? b2[w0 + 1] : 0u;
+#pragma unroll
+    for (uint32_t j = 0; j < SWM_WIN_WORDS; j++) {
+        uint32_t nlo = 0, nhi = 0;
+        if (j < nw) {
+            const uint64_t q = w0 + 2 * j + 2;
+            nlo = q < b2_words ? b2[q] : 0u;
+            nhi = q + 1 < b2_words ? b2[q + 1] : 0u;
+        }
+        WL[j] = swm_fsr(plo, nlo, sh);
+        WH[j] = swm_fsr(phi, nhi, sh);
+        plo = nlo;
+        phi = nhi;
+    }
+}
+
 #define TB_TEXT_MAX 2304 // >= 4 bytes x every route entry a bounded walk can make
 
 __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ lens, const uint32_t *__restrict__ b2,
@@ -710,24 +771,8 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ len
             B.vr_mloc[c] = -1;
             continue;
         }
-        // aligned window planes (shift_ref_pos_v, 1509-1586)
         uint32_t WL[SWM_WIN_WORDS], WH[SWM_WIN_WORDS];
-        const uint64_t w0 = (uint64_t)(ws >> 5) * 2;
-        const uint32_t sh = ws & 31;
-        const uint32_t nw = (L + 2 * e + 31) / 32 + 2;
-        uint32_t plo = (w0 < b2_words) ? b2[w0] : 0u, phi = (w0 + 1 < b2_words) ? b2[w0 + 1] : 0u;
-        for (uint32_t j = 0; j < SWM_WIN_WORDS; j++) {
-            uint32_t nlo = 0, nhi = 0;
-            if (j < nw) {
-                const uint64_t q = w0 + 2 * j + 2;
-                nlo = q < b2_words ? b2[q] : 0u;
-                nhi = q + 1 < b2_words ? b2[q + 1] : 0u;
-            }
-            WL[j] = swm_fsr(plo, nlo, sh);
-            WH[j] = swm_fsr(phi, nhi, sh);
-            plo = nlo;
-            phi = nhi;
-        }
+        load_window(b2, b2_words, ws, L, e, WL, WH);
         const uint32_t *RW = B.it_w + (uint64_t)item * 32;
         uint32_t rw[16];
 #pragma unroll
@@ -766,7 +811,39 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ len
             B.vr_flag[c] = VR_HAM;
             continue;
         }
-        // traceback (align_reads, 288-509)
+        B.vr_loc[c] = ws; // window start, used by the traceback
+        B.vr_flag[c] = VR_NEEDTB;
+    }
+    warp_add_u64(&B.stat[ST_CELLS], cells);
+    warp_add_u64(&B.stat[ST_PASSED], passed);
+}
+
+
+// Traceback of the passing candidates that the Hamming check did not resolve
+// (align_reads, mapper_cpe.c:288-509): re-run Myers keeping D0 / HP per read
+// base, walk back from (L - 1, location), emit the start position and CIGAR.
+__global__ void __launch_bounds__(128) k_traceback(const uint32_t *__restrict__ lens,
+                                                   const uint32_t *__restrict__ b2, uint64_t b2_words,
+                                                   uint64_t ref_length, MapBufs B, uint64_t cap_chunks,
+                                                   uint64_t cap_elems, uint64_t cap_cands, uint64_t cap_arena) {
+    if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint64_t nc = B.tot[TOT_CANDS];
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (uint64_t)gridDim.x * blockDim.x) {
+        if (B.vr_flag[c] != VR_NEEDTB) continue;
+        const uint32_t item = B.cc_item[c];
+        const uint32_t L = lens[item >> 1], e = B.it_e[item];
+        const uint32_t ws = B.vr_loc[c];
+        const int err = B.vr_err[c], loc = B.vr_mloc[c];
+        uint32_t rl;
+        window_start(B.cc_pos[c], L, e, ref_length, &rl);
+        uint32_t WL[SWM_WIN_WORDS], WH[SWM_WIN_WORDS];
+        load_window(b2, b2_words, ws, L, e, WL, WH);
+        const uint32_t *RW = B.it_w + (uint64_t)item * 32;
+        uint32_t rw[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) rw[i] = RW[i];
+        int start = loc - (int)L + 1;
+        uint8_t *slot = B.vr_cig + c * SWM_CIGAR_SLOT;
         uint32_t d0h[SWM_MAX_READ_LEN], hph[SWM_MAX_READ_LEN];
         myers_history(WL, WH, rw, L, e, d0h, hph);
         int match_site = loc;
@@ -855,8 +932,6 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ len
         B.vr_loc[c] = ws + (uint32_t)start + 1;
         B.vr_flag[c] = VR_TB;
     }
-    warp_add_u64(&B.stat[ST_CELLS], cells);
-    warp_add_u64(&B.stat[ST_PASSED], passed);
 }
 
 // ======================================================================
@@ -871,6 +946,7 @@ __global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uin
     unsigned long long locs_total = 0, mapped = 0;
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
         const uint32_t s0 = B.it_choff[item], nb = B.it_nbat[item];
+        uint32_t cnext = B.it_coff[item];
         uint32_t num = 0, len = 0, last = 0, mainf = 1, nrec = 0, nw = 0, nby = 0;
         uint32_t recbase = 0, wbase = 0, bbase = 0;
         bool ok = true;
@@ -903,7 +979,8 @@ __global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uin
             len = 0;
         };
         for (uint32_t s = s0; s < s0 + nb; s++) {
-            const uint32_t cbeg = B.bt_coff[s], cn = B.bt_cnt[s];
+            const uint32_t cbeg = cnext, cn = B.bt_cnt[s];
+            cnext += cn;
             uint32_t g = 0;
             for (uint32_t c = cbeg; c < cbeg + cn; c++) {
                 const uint8_t f = B.vr_flag[c];
@@ -987,19 +1064,15 @@ static int dmalloc(T **p, uint64_t count) {
 
 static void free_bufs(MapBufs &B) {
     void *ps[] = {B.it_w, B.sel_start, B.sel_count, B.sel_meta, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
-                  B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.ch_g,
-                  B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_item, B.bt_cnt, B.bt_coff, B.cand_ub, B.cc_pos,
+                  B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
+                  B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.cand_ub, B.cc_pos,
                   B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena,
                   B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
     for (void *p : ps) cudaFree(p);
     memset(&B, 0, sizeof(B));
 }
 
-static uint64_t scan_cap(const swm_mapper *m) {
-    uint64_t c = m->cap_items + 1;
-    if (m->cap_chunks + 1 > c) c = m->cap_chunks + 1;
-    return c;
-}
+static uint64_t scan_cap(const swm_mapper *m) { return m->cap_items + 1; }
 
 static int alloc_items(swm_mapper *m) {
     MapBufs &B = m->b;
@@ -1022,6 +1095,8 @@ static int alloc_items(swm_mapper *m) {
     rc |= dmalloc(&B.it_recoff, I + 1);
     rc |= dmalloc(&B.it_woff, I + 1);
     rc |= dmalloc(&B.it_boff, I + 1);
+    rc |= dmalloc(&B.it_ncand, I);
+    rc |= dmalloc(&B.it_coff, I + 1);
     rc |= dmalloc(&B.tot, TOT_N);
     rc |= dmalloc(&B.stat, ST_N);
     return rc ? SWM_ERR_OOM : SWM_OK;
@@ -1031,7 +1106,7 @@ static int alloc_work(swm_mapper *m) {
     MapBufs &B = m->b;
     int rc = SWM_OK;
     cudaFree(B.ch_g); cudaFree(B.ch_meta); cudaFree(B.bt_c0); cudaFree(B.bt_c1); cudaFree(B.bt_e0);
-    cudaFree(B.bt_item); cudaFree(B.bt_cnt); cudaFree(B.bt_coff); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
+    cudaFree(B.bt_cnt); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
     cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
     cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
     cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
@@ -1040,9 +1115,7 @@ static int alloc_work(swm_mapper *m) {
     rc |= dmalloc(&B.bt_c0, m->cap_chunks);
     rc |= dmalloc(&B.bt_c1, m->cap_chunks);
     rc |= dmalloc(&B.bt_e0, m->cap_chunks);
-    rc |= dmalloc(&B.bt_item, m->cap_chunks);
     rc |= dmalloc(&B.bt_cnt, m->cap_chunks);
-    rc |= dmalloc(&B.bt_coff, m->cap_chunks + 1);
     rc |= dmalloc(&B.cand_ub, m->cap_elems);
     rc |= dmalloc(&B.cc_pos, m->cap_cands);
     rc |= dmalloc(&B.cc_item, m->cap_cands);
@@ -1160,22 +1233,27 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[2], st));
-    k_cand<<<grid_cap(m->cap_chunks * 32, CAND_WARPS * 32, 8), CAND_WARPS * 32, 0, st>>>(ix->d_pos, ix->d_lseed, B,
-                                                                                           m->cap_chunks);
+    k_cand<<<grid_cap((uint64_t)nitems * 32, CAND_WARPS * 32, 8), CAND_WARPS * 32, 0, st>>>(
+        nitems, ix->d_pos, ix->d_lseed, B, m->cap_chunks, m->cap_elems);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[3], st));
-    rc = swm_exclusive_scan(B.bt_cnt, B.bt_coff, B.tot + TOT_CHUNKS, 0, m->cap_chunks, B.scan_tmp, B.tot + TOT_CANDS,
-                            st);
+    rc = swm_exclusive_scan(B.it_ncand, B.it_coff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_CANDS, st);
     if (rc) return rc;
     m->launches += 3;
-    k_compact<<<grid_cap(m->cap_chunks * 32, 256, 16), 256, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands);
+    k_compact<<<grid_cap((uint64_t)nitems * 32, 256, 16), 256, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems,
+                                                                        m->cap_cands);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[4], st));
     k_verify<<<grid_cap(m->cap_cands, 128, 64), 128, 0, st>>>(d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
                                                                ix->ref_length, B, m->cap_chunks, m->cap_elems,
                                                                m->cap_cands, m->cap_arena);
+    m->launches++;
+    LAUNCH_CHECK();
+    k_traceback<<<grid_cap(m->cap_cands, 128, 64), 128, 0, st>>>(d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
+                                                                  ix->ref_length, B, m->cap_chunks, m->cap_elems,
+                                                                  m->cap_cands, m->cap_arena);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[5], st));
