@@ -224,25 +224,30 @@ def timed_cpu_sample(mix, reads, lens, e, threads, target_s):
 
 # ------------------------------------------------------------ GPU arm
 
-STAGES = ["seed", "plan", "candidates", "compact", "verify", "records"]
+STAGES = ["seed", "plan", "candidates", "compact", "verify", "traceback", "records"]
 
 
 def stage_bytes(stage, st, L, e):
-    """Algorithmic DRAM bytes of one stage over a whole step."""
+    """Algorithmic DRAM bytes of one stage over a whole step: what the stage must
+    read and write once (index entries are 8-byte (position, flank) pairs;
+    `chunks` counts refill chunks)."""
     nl = L // 15
     items = st["items"]
     ns = min(e + 1, nl) * 4
     if stage == "seed":
         return items * (L + nl * 4 * 8 + 128 + ns * 12 + 16)
-    if stage == "plan":
-        return items * (ns * 8 + 16) + st["chunks"] * 8 + st["batches"] * 16
-    if stage == "candidates":
-        return st["fetched"] * 6 + st["chunks"] * 8 + st["batches"] * 20 + st["candidates"] * 4
+    if stage == "plan":   # items with refills only: seed table, refill chunks, batch records
+        return st["chunks"] * (8 + 8) + st["batches"] * 12 + items * 8
+    if stage == "candidates":  # (position, flank) pairs, seed table, refill chunks, candidates
+        return st["fetched"] * 8 + items * ns * 12 + st["chunks"] * 8 + st["candidates"] * 4
     if stage == "compact":
         return st["candidates"] * 12 + st["batches"] * 12
     if stage == "verify":
         win = ((L + 2 * e + 31) // 32 + 1) * 8
-        return st["candidates"] * (win + 64 + 8 + 16) + st["passed"] * 64
+        return st["candidates"] * (win + 64 + 8 + 16)
+    if stage == "traceback":  # flags of every candidate, window + read + CIGAR of the passing ones
+        win = ((L + 2 * e + 31) // 32 + 1) * 8
+        return st["candidates"] * 1 + st["passed"] * (win + 128 + 32)
     if stage == "records":
         return st["candidates"] * 10 + st["locations"] * 12 + items * 24
     return 0
@@ -362,7 +367,7 @@ def run_gpu(args):
                              "bytes_per_step": int(byts)}
     dom = max(STAGES, key=lambda s: per_step["ms_" + s])
     kern = {"seed": "k_seed", "plan": "k_plan", "candidates": "k_cand", "compact": "k_compact",
-            "verify": "k_verify", "records": "k_records"}[dom]
+            "verify": "k_verify", "traceback": "k_traceback", "records": "k_records"}[dom]
     launches_per_step = per_step["blocks"]
     avg_launch_s = per_step["ms_" + dom] / 1e3 / launches_per_step
     alg_bytes_launch = stage_bytes(dom, per_step, L, e) / launches_per_step

@@ -176,7 +176,8 @@ int swm_mapper_stats(const swm_mapper *m, swm_map_stats *s);
 
 /* Per-stage device time of the last block in milliseconds (CUDA events on the
  * mapper's stream); names are "seed", "plan", "candidates", "compact",
- * "verify", "records", "total". Returns SWM_ERR_ARG for an unknown name. */
+ * "verify", "traceback", "records", "total". Returns SWM_ERR_ARG for an
+ * unknown name. */
 int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float *ms);
 
 /* Kernel launches queued for the last block. */
@@ -191,6 +192,12 @@ void *swm_mapper_stream(const swm_mapper *m);
  * location. For tests; n gets the total even when cap is smaller. */
 int swm_mapper_debug_candidates(const swm_mapper *m, uint32_t *item, uint32_t *pos, int32_t *err, int32_t *loc,
                                 uint64_t cap, uint64_t *n);
+
+/* Read encodings of the last block, 32 words per item: [0..15] the bit
+ * planes of the 2-bit packed read that banded Myers scans (lo, hi per 32
+ * bases), [16..31] the planes the Hamming check uses (reads_2bits[16..31] of
+ * get_seed_from_reads, mapper_cpe.c:1246-1364). For tests. */
+int swm_mapper_debug_read_words(const swm_mapper *m, uint32_t *words, uint64_t cap_items);
 
 void swm_mapper_free(swm_mapper *m);
 

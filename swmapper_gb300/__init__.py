@@ -94,6 +94,7 @@ def lib():
         L.swm_mapper_stream.argtypes = [vp]
         L.swm_mapper_stream.restype = vp
         L.swm_mapper_debug_candidates.argtypes = [vp, vp, vp, vp, vp, u64, C.POINTER(u64)]
+        L.swm_mapper_debug_read_words.argtypes = [vp, vp, u64]
         L.swm_mapper_free.argtypes = [vp]
         L.swm_mapper_free.restype = None
         _lib = L
@@ -264,6 +265,11 @@ class Mapper:
         _check(lib().swm_mapper_debug_candidates(self._h, item.ctypes.data, pos.ctypes.data, err.ctypes.data,
                                                  loc.ctypes.data, k, C.byref(n)), "debug")
         return item, pos, err, loc
+
+    def debug_read_words(self, nreads: int) -> np.ndarray:
+        w = np.zeros((2 * nreads, 32), np.uint32)
+        _check(lib().swm_mapper_debug_read_words(self._h, w.ctypes.data, 2 * nreads), "debug_read_words")
+        return w
 
     def close(self) -> None:
         if self._h:

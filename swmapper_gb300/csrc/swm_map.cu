@@ -65,7 +65,8 @@ struct MapBufs {
     uint32_t *it_ncand, *it_coff;            // candidates per item, dense offsets (items + 1)
     // per chunk / batch slot (cap_chunks; batch b of an item sits at slot it_choff + b)
     uint32_t *ch_g, *ch_meta;
-    uint32_t *bt_c0, *bt_c1, *bt_e0, *bt_cnt;
+    uint32_t *bt_c0, *bt_c1, *bt_e0, *bt_cnt; // cap_chunks + cap_items slots
+    uint32_t *sort_scratch; // SWM_BATCH_POSITIONS words per resident k_cand warp
     // upper-bound candidates (cap_elems)
     uint32_t *cand_ub;
     // dense candidates (cap_cands)
@@ -119,8 +120,8 @@ struct swm_mapper {
     int have_result;
     uint32_t tot[TOT_N];
     swm_map_stats stats;
-    cudaEvent_t ev[8];
-    float stage_ms[7];
+    cudaEvent_t ev[9];
+    float stage_ms[8];
     uint64_t launches;
 };
 
@@ -136,39 +137,11 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned l
     if (lane_id() == 0 && v) atomicAdd(dst, v);
 }
 
-// Encode one read base as get_seed_from_reads does (mapper_cpe.c:1260-1305):
-// 2-bit accumulator + lo/hi planes; anything but A/C/G/T encodes as C.
-__device__ __forceinline__ void enc_base(uint32_t *w, uint32_t &acc, uint32_t rp, char ch) {
-    uint32_t code = ch == 'A' ? 0u : ch == 'C' ? 1u : ch == 'G' ? 2u : ch == 'T' ? 3u : 1u;
-    acc |= code << ((rp % 16) * 2);
-    w[16 + (rp >> 5) * 2] |= (code & 1u) << (rp & 31);
-    w[16 + (rp >> 5) * 2 + 1] |= (code >> 1) << (rp & 31);
-    if (rp % 16 == 15) {
-        w[rp / 16] = acc;
-        acc = 0;
-    }
+__device__ __forceinline__ uint32_t base_code_c(char ch) {
+    return ch == 'A' ? 0u : ch == 'C' ? 1u : ch == 'G' ? 2u : ch == 'T' ? 3u : 1u;
 }
 
-// get_seed_from_reads with its tail encoder (mapper_cpe.c:1246-1364).
-__device__ uint32_t read_seed(const char *s, uint32_t *w, uint32_t &acc, uint32_t pre, uint32_t k, uint32_t j,
-                              uint32_t L) {
-    uint32_t i = (j % SWM_SEED_STEP == 0) ? 0 : k - 1;
-    const uint32_t base = (j / SWM_SEED_STEP) * (k + SWM_SEED_STEP - 1) + j % SWM_SEED_STEP;
-    uint32_t seed = pre;
-    uint32_t rp = base + i;
-    for (; i < k; i++) {
-        rp = base + i;
-        char ch = s[rp];
-        uint32_t sc = ch == 'A' ? 0u : ch == 'C' ? 1u : ch == 'G' ? 2u : ch == 'T' ? 3u : (i % 4);
-        seed = (seed >> 2) | (sc << ((k - 1) * 2));
-        enc_base(w, acc, rp, ch);
-    }
-    if (L - rp < k) {
-        for (; rp < L; rp++) enc_base(w, acc, rp, s[rp]);
-        w[(rp - 1) / 16] = acc;
-    }
-    return seed;
-}
+__device__ __forceinline__ bool is_acgt(char ch) { return ch == 'A' || ch == 'C' || ch == 'G' || ch == 'T'; }
 
 __device__ __forceinline__ char comp_base(char c) {
     return c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : c == 'T' ? 'A' : c;
@@ -184,6 +157,40 @@ __device__ __forceinline__ uint32_t even_bits(uint32_t x) {
     return x;
 }
 
+// spread the low 16 bits of x to the even bit positions
+__device__ __forceinline__ uint32_t spread_bits(uint32_t x) {
+    x &= 0x0000ffffu;
+    x = (x | (x << 8)) & 0x00ff00ffu;
+    x = (x | (x << 4)) & 0x0f0f0f0fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+
+struct ReadView { // base i of the strand being mapped (reverse_read, mapper_cpe.c:2429-2450)
+    const char *src;
+    uint32_t L, strand;
+    __device__ __forceinline__ char operator()(uint32_t i) const {
+        return strand ? comp_base(src[L - 1 - i]) : src[i];
+    }
+};
+
+// The rolling seed of long seed l at shift s in closed form: base p of the
+// window enters with its code, or, when it is not A/C/G/T, with d % 4 where
+// d = p - l (k + 3) if d < k (built at shift 0, mapper_cpe.c:1294 with i = d)
+// and (k - 1) % 4 otherwise (added at a later shift with i = k - 1).
+__device__ __forceinline__ uint32_t seed_closed(const ReadView &rv, uint32_t k, uint32_t l, uint32_t s) {
+    const uint32_t p0 = l * (k + SWM_SEED_STEP - 1);
+    uint32_t seed = 0;
+    for (uint32_t t = 0; t < k; t++) {
+        const uint32_t d = s + t;
+        const char ch = rv(p0 + d);
+        const uint32_t c = is_acgt(ch) ? base_code_c(ch) : (d < k ? d % 4 : (k - 1) % 4);
+        seed |= c << (2 * t);
+    }
+    return seed;
+}
+
 // True once any earlier stage of this block ran out of a buffer or met an
 // input outside the envelope: later stages then skip their work (their
 // inputs may be partial) and the host re-runs or rejects the block.
@@ -194,126 +201,239 @@ __device__ __forceinline__ bool block_failed(const MapBufs &B, uint64_t cap_chun
 }
 
 // ======================================================================
-// k_seed: one thread per (read, strand)
+// k_seed: one warp per (read, strand)
 // ======================================================================
+//
+// choose_seed / get_seed_from_reads (mapper_cpe.c:1246-1401) encode the read
+// with a state machine whose main loop visits positions 0, 1, ..., P in
+// order (P = 15 nl - 1, or the last base of the first call whose tail test
+// L - rp < k fires; only calls of the last long seed can fire it). Up to P
+// the bit planes hold the bases' codes and every complete 2-bit word is the
+// interleave of the planes; the partial word is not yet written. The lanes
+// compute that state with ballots; one lane then replays the rest of the
+// state machine literally (the tail encoder re-runs and rewrites the last
+// 2-bit words, mapper_cpe.c:1312-1362) -- at most four tails of < k bases.
 
-__global__ void __launch_bounds__(128) k_seed(const char *__restrict__ reads, const uint32_t *__restrict__ lens,
-                                              uint64_t stride, uint32_t nreads, uint32_t e_glob,
-                                              const uint8_t *__restrict__ e_arr, const uint32_t *__restrict__ off,
-                                              uint32_t k, MapBufs B) {
+#define SEED_WARPS 4
+
+struct SeedSmem {
+    uint32_t pl[16];    // [2b] lo / [2b + 1] hi plane of bases 32b .. 32b + 31
+    uint32_t w2[16];    // 2-bit words, 16 bases each
+    uint32_t cnt[16];   // bucket counts summed per long seed
+    uint32_t idx[16];   // long seed order (exchange sort)
+};
+
+__global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict__ reads,
+                                                          const uint32_t *__restrict__ lens, uint64_t stride,
+                                                          uint32_t nreads, uint32_t e_glob,
+                                                          const uint8_t *__restrict__ e_arr,
+                                                          const uint32_t *__restrict__ off, uint32_t k, MapBufs B) {
+    __shared__ SeedSmem sm_all[SEED_WARPS];
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
+    SeedSmem &S = sm_all[wib];
+    uint32_t *__restrict__ sel_start = B.sel_start;
+    uint32_t *__restrict__ sel_count = B.sel_count;
+    uint32_t *__restrict__ sel_meta = B.sel_meta;
     const uint32_t nitems = 2 * nreads;
-    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
+    const uint32_t klong = k + SWM_SEED_STEP - 1;
+    for (uint32_t item = blockIdx.x * SEED_WARPS + wib; item < nitems; item += gridDim.x * SEED_WARPS) {
         const uint32_t r = item >> 1, strand = item & 1;
         const uint32_t L = lens[r];
         const uint32_t e = e_arr ? e_arr[r] : e_glob;
-        const uint32_t klong0 = k + SWM_SEED_STEP - 1;
-        if (L > SWM_MAX_READ_LEN || L > stride || L / klong0 > 16 || e > SWM_MAX_ERRORS) {
+        if (L > SWM_MAX_READ_LEN || L > stride || L / klong > 16 || e > SWM_MAX_ERRORS) {
             // outside the envelope: no work for this item, and the block fails
-            atomicOr(&B.tot[TOT_FLAGS], OV_BAD);
-            B.it_nsel[item] = 0;
-            B.it_e[item] = 0;
-            B.it_nch[item] = 0;
-            B.it_nel[item] = 0;
+            if (lane == 0) {
+                atomicOr(&B.tot[TOT_FLAGS], OV_BAD);
+                B.it_nsel[item] = 0;
+                B.it_e[item] = 0;
+                B.it_nch[item] = 0;
+                B.it_nel[item] = 0;
+                B.it_nbat[item] = 0;
+            }
             continue;
         }
-        const char *src = reads + (uint64_t)r * stride;
-        char s[SWM_MAX_READ_LEN + 2];
-        if (strand == 0) {
-            for (uint32_t i = 0; i < L; i++) s[i] = src[i];
-        } else {
-            for (uint32_t i = 0; i < L; i++) s[L - 1 - i] = comp_base(src[i]); // reverse_read, 2429-2450
-        }
-        uint32_t w[32];
-#pragma unroll
-        for (int i = 0; i < 32; i++) w[i] = 0;
-        const uint32_t klong = k + SWM_SEED_STEP - 1;
-        const uint32_t nl = L / klong, ns_all = nl * SWM_SEED_STEP;
-        uint32_t cnt[SWM_MAX_SEL], start[SWM_MAX_SEL];
-        uint32_t acc = 0, seed = 0;
-        for (uint32_t j = 0; j < ns_all; j++) { // choose_seed, 1365-1384
-            seed = read_seed(s, w, acc, seed, k, j, L);
-            uint32_t o0 = off[seed], o1 = off[seed + 1];
-            start[j] = o0;
-            cnt[j] = o1 - o0;
-        }
-        uint32_t icount[16], iindex[16];
-        for (uint32_t j = 0; j < 16; j++) {
-            icount[j] = 0;
-            iindex[j] = j;
-        }
-        for (uint32_t j = 0; j < ns_all; j++) icount[j / SWM_SEED_STEP] += cnt[j];
-        for (uint32_t j = 0; j < nl; j++) // exchange sort, 1391-1399
-            for (uint32_t m = j + 1; m < nl; m++)
-                if (icount[j] > icount[m]) {
-                    uint32_t t = icount[j];
-                    icount[j] = icount[m];
-                    icount[m] = t;
-                    t = iindex[j];
-                    iindex[j] = iindex[m];
-                    iindex[m] = t;
+        const ReadView rv{reads + (uint64_t)r * stride, L, strand};
+        const uint32_t nl = L / klong;
+        // first tail trigger (only within the last long seed) and the last
+        // position of the clean visit
+        int jt = -1;
+        uint32_t P = 0;
+        if (nl) {
+            P = nl * klong - 1;
+            for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
+                const uint32_t rp = (nl - 1) * klong + sft + k - 1;
+                if (L - rp < k) {
+                    jt = (int)((nl - 1) * SWM_SEED_STEP + sft);
+                    P = rp;
+                    break;
                 }
-        // flank codes of the read (set_read_long_seeds, 2451-2499)
-        uint8_t res[128];
-        const uint32_t lmask = (1u << klong) - 1, rmask = (1u << (SWM_SEED_STEP - 1)) - 1;
-        for (uint32_t i = 0; i < nl; i++) {
-            uint32_t o = i * klong, wj = o >> 5, sh = o & 31, nx = 16 + (wj + 1) * 2;
-            uint32_t l = swm_fsr(w[16 + wj * 2], nx < 32 ? w[nx] : 0u, sh) & lmask;
-            uint32_t h = swm_fsr(w[16 + wj * 2 + 1], nx + 1 < 32 ? w[nx + 1] : 0u, sh) & lmask;
-            for (uint32_t j = 0; j < SWM_SEED_STEP; j++) {
-                uint32_t sft = k + j, m = (1u << j) - 1;
-                res[2 * (SWM_SEED_STEP * i + j)] = (uint8_t)(((l & m) | ((l >> sft) << j)) & rmask);
-                res[2 * (SWM_SEED_STEP * i + j) + 1] = (uint8_t)(((h & m) | ((h >> sft) << j)) & rmask);
             }
         }
-        // selected seed slots: the (e + 1) rarest long seeds x 4 shifts
+        const uint32_t vis = nl ? (jt >= 0 ? L : nl * klong) : 0u; // bases with plane bits
+        const uint32_t seedspan = nl * klong;                          // bases inside seed windows
+        // planes and the non-ACGT flag by ballots over 32-base groups
+        bool has_n = false;
+        for (uint32_t b = 0; b < 8; b++) {
+            const uint32_t p = 32 * b + lane;
+            uint32_t code = 0;
+            bool n = false;
+            if (p < vis) {
+                const char ch = rv(p);
+                code = base_code_c(ch);
+                n = !is_acgt(ch) && p < seedspan;
+            }
+            const uint32_t lo = __ballot_sync(0xffffffffu, code & 1u), hi = __ballot_sync(0xffffffffu, code >> 1);
+            has_n |= __any_sync(0xffffffffu, n);
+            if (lane == 0) {
+                S.pl[2 * b] = lo;
+                S.pl[2 * b + 1] = hi;
+            }
+        }
+        __syncwarp();
+        // 2-bit words: complete words up to P from the planes, the rest 0
+        if (lane < 16) {
+            uint32_t wv = 0;
+            if (nl && 16 * lane + 15 <= P) {
+                const uint32_t sh = (lane & 1) * 16;
+                const uint32_t lo = (S.pl[2 * (lane >> 1)] >> sh) & 0xffffu, hi = (S.pl[2 * (lane >> 1) + 1] >> sh) & 0xffffu;
+                wv = spread_bits(lo) | (spread_bits(hi) << 1);
+            }
+            S.w2[lane] = wv;
+        }
+        __syncwarp();
+        if (lane == 0 && jt >= 0) {
+            // literal replay of the remaining calls (mapper_cpe.c:1246-1364)
+            auto code_at = [&](uint32_t q) -> uint32_t {
+                return ((S.pl[2 * (q >> 5)] >> (q & 31)) & 1u) | (((S.pl[2 * (q >> 5) + 1] >> (q & 31)) & 1u) << 1);
+            };
+            uint32_t acc = 0;
+            if (P % 16 != 15)
+                for (uint32_t q = P & ~15u; q <= P; q++) acc |= code_at(q) << ((q % 16) * 2);
+            for (uint32_t j = (uint32_t)jt; j < nl * SWM_SEED_STEP; j++) {
+                const uint32_t rp = (j / SWM_SEED_STEP) * klong + j % SWM_SEED_STEP + k - 1;
+                if (j > (uint32_t)jt) { // the one base this call's main loop adds
+                    acc |= code_at(rp) << ((rp % 16) * 2);
+                    if (rp % 16 == 15) {
+                        S.w2[rp / 16] = acc;
+                        acc = 0;
+                    }
+                }
+                for (uint32_t q = rp; q < L; q++) { // tail encoder, re-run from rp
+                    acc |= code_at(q) << ((q % 16) * 2);
+                    if (q % 16 == 15) {
+                        S.w2[q / 16] = acc;
+                        acc = 0;
+                    }
+                }
+                S.w2[(L - 1) / 16] = acc;
+            }
+        }
+        __syncwarp();
+        // bucket counts of every seed, summed per long seed (choose_seed, 1372-1390)
+        const uint32_t ns_all = nl * SWM_SEED_STEP;
+        for (uint32_t j0 = 0; j0 < ns_all; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            uint32_t c = 0;
+            if (j < ns_all) {
+                const uint32_t l = j / SWM_SEED_STEP, sft = j % SWM_SEED_STEP;
+                uint32_t sd;
+                if (!has_n) {
+                    const uint32_t o = l * klong, wj = o >> 5, sh = o & 31;
+                    const uint32_t nlo = wj + 1 < 8 ? S.pl[2 * (wj + 1)] : 0u, nhi = wj + 1 < 8 ? S.pl[2 * (wj + 1) + 1] : 0u;
+                    const uint32_t kmask = (1u << k) - 1;
+                    const uint32_t lo = (swm_fsr(S.pl[2 * wj], nlo, sh) >> sft) & kmask;
+                    const uint32_t hi = (swm_fsr(S.pl[2 * wj + 1], nhi, sh) >> sft) & kmask;
+                    sd = spread_bits(lo) | (spread_bits(hi) << 1);
+                } else {
+                    sd = seed_closed(rv, k, l, sft);
+                }
+                c = off[sd + 1] - off[sd];
+            }
+            c += __shfl_xor_sync(0xffffffffu, c, 1);
+            c += __shfl_xor_sync(0xffffffffu, c, 2);
+            if (j < ns_all && (j % SWM_SEED_STEP) == 0) S.cnt[j / SWM_SEED_STEP] = c;
+        }
+        if (lane < 16) S.idx[lane] = lane;
+        __syncwarp();
+        if (lane == 0) { // exchange sort, 1391-1399
+            for (uint32_t a = 0; a < nl; a++)
+                for (uint32_t m = a + 1; m < nl; m++)
+                    if (S.cnt[a] > S.cnt[m]) {
+                        uint32_t t = S.cnt[a];
+                        S.cnt[a] = S.cnt[m];
+                        S.cnt[m] = t;
+                        t = S.idx[a];
+                        S.idx[a] = S.idx[m];
+                        S.idx[m] = t;
+                    }
+        }
+        __syncwarp();
+        // selected slots: the (e + 1) rarest long seeds x 4 shifts
         // (alignment_rmdup, 2194-2196); slots past nl read count 0
         const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
         const uint32_t ns = nsl * SWM_SEED_STEP;
-        uint32_t nch = 0, nel = 0;
         const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
-        for (uint32_t i = 0; i < ns; i++) {
-            uint32_t sidx = iindex[i / SWM_SEED_STEP] * SWM_SEED_STEP + i % SWM_SEED_STEP;
-            uint32_t c = cnt[sidx];
-            uint32_t base = iindex[i / SWM_SEED_STEP] * klong + i % SWM_SEED_STEP;
-            uint32_t shift = SWM_SEED_STEP - 1 - sidx % SWM_SEED_STEP;
-            B.sel_start[sb + i] = start[sidx];
-            B.sel_count[sb + i] = c;
-            B.sel_meta[sb + i] = base | (shift << 16) | ((uint32_t)res[2 * sidx] << 20) |
-                                 ((uint32_t)res[2 * sidx + 1] << 24);
-            nch += (c + SWM_PER_FETCH - 1) / SWM_PER_FETCH;
-            nel += c;
+        uint32_t nref = 0, nel = 0;
+        for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            if (i < ns) {
+                const uint32_t l = S.idx[i / SWM_SEED_STEP], sft = i % SWM_SEED_STEP;
+                const uint32_t o = l * klong, wj = o >> 5, sh = o & 31;
+                const uint32_t nlo = wj + 1 < 8 ? S.pl[2 * (wj + 1)] : 0u, nhi = wj + 1 < 8 ? S.pl[2 * (wj + 1) + 1] : 0u;
+                const uint32_t lmask = (1u << klong) - 1, kmask = (1u << k) - 1;
+                const uint32_t lr = swm_fsr(S.pl[2 * wj], nlo, sh) & lmask;  // set_read_long_seeds, 2474-2478
+                const uint32_t hr = swm_fsr(S.pl[2 * wj + 1], nhi, sh) & lmask;
+                const uint32_t sd = has_n ? seed_closed(rv, k, l, sft)
+                                          : (spread_bits((lr >> sft) & kmask) | (spread_bits((hr >> sft) & kmask) << 1));
+                const uint32_t o0 = off[sd], c = off[sd + 1] - o0;
+                const uint32_t m = (1u << sft) - 1, kk = k + sft, rmask = (1u << (SWM_SEED_STEP - 1)) - 1;
+                const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & rmask; // 2483-2495
+                const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & rmask;
+                sel_start[sb + i] = o0;
+                sel_count[sb + i] = c;
+                sel_meta[sb + i] = (o + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) | (rh << 24);
+                nref += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
+                nel += c;
+            }
         }
-        // Myers planes from the 2-bit words, Hamming planes as encoded
-        uint32_t *ow = B.it_w + (uint64_t)item * 32;
 #pragma unroll
-        for (int b = 0; b < 8; b++) {
-            uint32_t a0 = w[2 * b], a1 = w[2 * b + 1];
-            ow[2 * b] = even_bits(a0) | (even_bits(a1) << 16);
-            ow[2 * b + 1] = even_bits(a0 >> 1) | (even_bits(a1 >> 1) << 16);
+        for (int d = 16; d > 0; d >>= 1) {
+            nref += __shfl_xor_sync(0xffffffffu, nref, d);
+            nel += __shfl_xor_sync(0xffffffffu, nel, d);
         }
-#pragma unroll
-        for (int i = 16; i < 32; i++) ow[i] = w[i];
-        B.it_nsel[item] = (uint8_t)ns;
-        B.it_e[item] = (uint8_t)e;
-        B.it_nch[item] = nch;
-        B.it_nel[item] = nel;
+        // read words: [0..15] Myers planes from the 2-bit words, [16..31] Hamming planes
+        uint32_t ow;
+        if (lane < 16) {
+            const uint32_t b = lane >> 1, hi = lane & 1;
+            ow = even_bits(S.w2[2 * b] >> hi) | (even_bits(S.w2[2 * b + 1] >> hi) << 16);
+        } else {
+            ow = S.pl[lane - 16];
+        }
+        B.it_w[(uint64_t)item * 32 + lane] = ow;
+        if (lane == 0) {
+            B.it_nsel[item] = (uint8_t)ns;
+            B.it_e[item] = (uint8_t)e;
+            B.it_nch[item] = nref;                  // refill chunks (beyond the first chunk of each seed)
+            B.it_nel[item] = nel;
+            B.it_nbat[item] = (nref == 0 && nel > 0) ? 1u : 0u; // k_plan sets it for items with refills
+        }
+        __syncwarp();
     }
 }
 
 // ======================================================================
-// k_plan: the fetch schedule of alignment_rmdup, one thread per item
+// k_plan: the refill schedule of alignment_rmdup, one thread per item whose
+// buckets need refills (some selected seed has more than 32 positions)
 // ======================================================================
 
-__global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const uint32_t *__restrict__ pos, MapBufs B,
+__global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const unsigned long long *__restrict__ pl, MapBufs B,
                                               uint64_t cap_chunks, uint64_t cap_elems) {
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
-        const uint32_t nch = B.it_nch[item];
-        const uint32_t cb = B.it_choff[item], eb = B.it_eloff[item];
-        if (nch == 0) {
-            B.it_nbat[item] = 0;
-            continue;
-        }
-        if ((uint64_t)cb + nch > cap_chunks) {
+        const uint32_t nref = B.it_nch[item];
+        if (nref == 0) continue; // one batch of initial chunks, set by k_seed
+        const uint32_t rb = B.it_choff[item], eb = B.it_eloff[item];
+        const uint32_t sbase = rb + item;
+        if ((uint64_t)rb + nref > cap_chunks) {
             atomicOr(&B.tot[TOT_FLAGS], OV_CHUNKS);
             B.it_nbat[item] = 0;
             continue;
@@ -327,33 +447,24 @@ __global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const uint32_t *_
         const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
         uint32_t pc[SWM_MAX_SEL], sst[SWM_MAX_SEL], scn[SWM_MAX_SEL];
         uint32_t hloc[SWM_MAX_SEL + 8], hidx[SWM_MAX_SEL + 8];
-        uint32_t hs = 0;
-        uint32_t c = 0, e = 0, b = 0, bc0 = 0, be0 = 0, npos = 0, runs = 0;
-#define EMIT(i_, get_)                                                    \
-    do {                                                                  \
-        B.ch_g[cb + c] = sst[i_] + pc[i_];                                \
-        B.ch_meta[cb + c] = (get_) | ((i_) << 8);                         \
-        c++;                                                              \
-        e += (get_);                                                      \
-        pc[i_] += (get_);                                                 \
-        npos += (get_);                                                   \
-        runs++;                                                           \
-    } while (0)
-        for (uint32_t i = 0; i < ns; i++) { // initial fetch, 2194-2236
+        uint32_t hs = 0, rc = 0, e = 0, b = 0, br0 = 0, be0 = 0, npos = 0, runs = 0;
+        for (uint32_t i = 0; i < ns; i++) { // initial fetch of <= 32 per seed, 2194-2236
             sst[i] = B.sel_start[sb + i];
             scn[i] = B.sel_count[sb + i];
-            pc[i] = 0;
-            uint32_t get = scn[i] > SWM_PER_FETCH ? SWM_PER_FETCH : scn[i];
-            if (get) EMIT(i, get);
+            const uint32_t get = scn[i] > SWM_PER_FETCH ? SWM_PER_FETCH : scn[i];
+            pc[i] = get;
+            e += get;
+            npos += get;
+            runs += get ? 1u : 0u;
         }
-        for (uint32_t i = 0; i < ns; i++) { // seeds_heap_insert, 1919-1935
+        for (uint32_t i = 0; i < ns; i++) { // seeds_heap_insert, 1919-1935 (keys: raw positions)
             if (pc[i] != scn[i]) {
                 hs++;
-                hloc[hs] = pos[sst[i] + pc[i] - 1];
+                hloc[hs] = (uint32_t)(pl[sst[i] + pc[i] - 1] >> 16);
                 hidx[hs] = i;
                 uint32_t q = hs;
                 while (q > 1) {
-                    uint32_t t = q / 2;
+                    const uint32_t t = q / 2;
                     if (hloc[t] > hloc[q]) {
                         uint32_t a = hloc[t];
                         hloc[t] = hloc[q];
@@ -368,17 +479,23 @@ __global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const uint32_t *_
         }
         for (;;) { // 2261-2419
             if (hs > 0 && npos + SWM_PER_FETCH <= SWM_BATCH_POSITIONS && 1 + 2 * runs < SWM_MAX_RUNS_BLOCK) {
-                uint32_t i = hidx[1];
-                uint32_t left = scn[i] - pc[i];
-                uint32_t get = left > SWM_PER_FETCH ? SWM_PER_FETCH : left;
-                EMIT(i, get);
+                const uint32_t i = hidx[1];
+                const uint32_t left = scn[i] - pc[i];
+                const uint32_t get = left > SWM_PER_FETCH ? SWM_PER_FETCH : left;
+                B.ch_g[rb + rc] = sst[i] + pc[i];
+                B.ch_meta[rb + rc] = get | (i << 8);
+                rc++;
+                pc[i] += get;
+                e += get;
+                npos += get;
+                runs++;
                 // seeds_heap_pop_and_insert, 1936-1962 (loop bound i * 2 < size)
                 if (pc[i] == scn[i]) {
                     hloc[1] = hloc[hs];
                     hidx[1] = hidx[hs];
                     hs--;
                 } else {
-                    hloc[1] = pos[sst[i] + pc[i] - 1];
+                    hloc[1] = (uint32_t)(pl[sst[i] + pc[i] - 1] >> 16);
                 }
                 uint32_t q = 1;
                 while (q * 2 < hs) {
@@ -397,20 +514,18 @@ __global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const uint32_t *_
             }
             if (npos + SWM_PER_FETCH > SWM_BATCH_POSITIONS || hs == 0 || 1 + 2 * runs >= SWM_MAX_RUNS_BLOCK) {
                 if (npos > 0) {
-                    const uint32_t slot = cb + b;
-                    B.bt_c0[slot] = cb + bc0;
-                    B.bt_c1[slot] = cb + c;
-                    B.bt_e0[slot] = eb + be0;
+                    B.bt_c0[sbase + b] = rb + br0; // refill chunks of the batch; batch 0 also
+                    B.bt_c1[sbase + b] = rb + rc;  // holds every initial chunk
+                    B.bt_e0[sbase + b] = eb + be0;
                     b++;
                 }
-                bc0 = c;
+                br0 = rc;
                 be0 = e;
                 npos = 0;
                 runs = 0;
                 if (hs == 0) break;
             }
         }
-#undef EMIT
         B.it_nbat[item] = b;
     }
 }
@@ -442,8 +557,8 @@ struct CandSmem {
     uint32_t meta[CAND_MAXCH];   // len | sel << 8
     uint16_t start[CAND_MAXCH + 1];
     uint32_t sel[SWM_MAX_SEL];   // base | shift << 16 | rl << 20 | rh << 24
-    uint8_t cof[SWM_BATCH_POSITIONS];  // element -> chunk
-    uint32_t buf[SWM_BATCH_POSITIONS]; // kept positions
+    uint32_t st[SWM_MAX_SEL];    // bucket start of each selected seed
+    uint32_t cn[SWM_MAX_SEL];    // bucket count of each selected seed
 };
 
 __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
@@ -455,74 +570,108 @@ __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
     return v;
 }
 
-// One warp per item: every batch of the item, element-parallel gather of
-// positions and flank codes, position adjust, flank filter, sort-unique.
-__global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(uint32_t nitems, const uint32_t *__restrict__ pos,
-                                                          const uint16_t *__restrict__ lseed, MapBufs B,
-                                                          uint64_t cap_chunks, uint64_t cap_elems) {
+#define CAND_WARPS 8
+
+// One warp per item, every batch of the item: element-parallel gather of
+// (position, flank code) pairs, position adjust, flank filter, sort-unique.
+__global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(uint32_t nitems, const unsigned long long *__restrict__ pl,
+                                                          MapBufs B, uint64_t cap_chunks, uint64_t cap_elems) {
     __shared__ CandSmem sm_all[CAND_WARPS];
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     CandSmem &S = sm_all[wib];
     const uint32_t lt = (1u << lane) - 1;
+    uint32_t *scratch = B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS;
     for (uint32_t item = blockIdx.x * CAND_WARPS + wib; item < nitems; item += gridDim.x * CAND_WARPS) {
         const uint32_t nb = B.it_nbat[item];
         uint32_t total = 0;
         if (nb) {
             const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
-            const uint32_t ns = B.it_nsel[item];
-            for (uint32_t i = lane; i < ns; i += 32) S.sel[i] = B.sel_meta[sb + i];
-            const uint32_t cb = B.it_choff[item];
+            const uint32_t ns = B.it_nsel[item], nref = B.it_nch[item];
+            const uint32_t sbase = B.it_choff[item] + item;
+            for (uint32_t i = lane; i < ns; i += 32) {
+                S.sel[i] = B.sel_meta[sb + i];
+                S.st[i] = B.sel_start[sb + i];
+                S.cn[i] = B.sel_count[sb + i];
+            }
+            __syncwarp();
             for (uint32_t b = 0; b < nb; b++) {
-                const uint32_t slot = cb + b;
-                const uint32_t c0 = B.bt_c0[slot], nchk = B.bt_c1[slot] - c0, e0 = B.bt_e0[slot];
-                uint32_t carry = 0;
-                for (uint32_t q0 = 0; q0 < nchk; q0 += 32) {
-                    const uint32_t q = q0 + lane;
+                uint32_t c0 = 0, c1 = 0, e0;
+                if (nref == 0) {
+                    e0 = B.it_eloff[item];
+                } else {
+                    c0 = B.bt_c0[sbase + b];
+                    c1 = B.bt_c1[sbase + b];
+                    e0 = B.bt_e0[sbase + b];
+                }
+                // chunk table: the first chunk of every seed (batch 0), then refills
+                uint32_t nchk = 0, carry = 0;
+                if (b == 0) {
+                    for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
+                        const uint32_t i = i0 + lane;
+                        const uint32_t cnt = i < ns ? S.cn[i] : 0u;
+                        const uint32_t len = cnt > SWM_PER_FETCH ? SWM_PER_FETCH : cnt;
+                        const uint32_t m = __ballot_sync(0xffffffffu, len != 0);
+                        const uint32_t inc = warp_scan_incl(len);
+                        if (len) {
+                            const uint32_t q = nchk + __popc(m & lt);
+                            S.g[q] = S.st[i];
+                            S.meta[q] = len | (i << 8);
+                            S.start[q] = (uint16_t)(carry + inc - len);
+                        }
+                        nchk += __popc(m);
+                        carry += __shfl_sync(0xffffffffu, inc, 31);
+                    }
+                }
+                for (uint32_t q0 = c0; q0 < c1; q0 += 32) {
+                    const uint32_t c = q0 + lane;
                     uint32_t len = 0;
-                    if (q < nchk) {
-                        const uint32_t meta = B.ch_meta[c0 + q];
-                        S.g[q] = B.ch_g[c0 + q];
-                        S.meta[q] = meta;
+                    if (c < c1) {
+                        const uint32_t meta = B.ch_meta[c];
                         len = meta & 0xffu;
+                        S.g[nchk + (c - q0)] = B.ch_g[c];
+                        S.meta[nchk + (c - q0)] = meta;
                     }
                     const uint32_t inc = warp_scan_incl(len);
-                    if (q < nchk) S.start[q] = (uint16_t)(carry + inc - len);
+                    if (c < c1) S.start[nchk + (c - q0)] = (uint16_t)(carry + inc - len);
+                    nchk += min(32u, c1 - q0);
                     carry += __shfl_sync(0xffffffffu, inc, 31);
                 }
                 const uint32_t E = carry;
-                __syncwarp();
-                for (uint32_t q = lane; q < nchk; q += 32) {
-                    const uint32_t st = S.start[q], len = S.meta[q] & 0xffu;
-                    for (uint32_t t = 0; t < len; t++) S.cof[st + t] = (uint8_t)q;
-                }
+                if (lane == 0) S.start[nchk] = (uint16_t)E;
                 __syncwarp();
                 uint32_t kept = 0;
                 for (uint32_t eb = 0; eb < E; eb += 32) {
-                    const uint32_t e = eb + lane;
+                    const uint32_t el = eb + lane;
                     bool ok = false;
                     uint32_t p = 0;
-                    if (e < E) {
-                        const uint32_t q = S.cof[e];
-                        const uint32_t g = S.g[q] + (e - S.start[q]);
+                    if (el < E) {
+                        uint32_t lo = 0, hi = nchk; // last chunk with start <= el
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (S.start[mid] <= el) lo = mid;
+                            else hi = mid;
+                        }
+                        const uint32_t q = lo;
+                        const uint32_t g = S.g[q] + (el - S.start[q]);
                         const uint32_t sm = S.sel[S.meta[q] >> 8];
                         const uint32_t base = sm & 0xffffu, shift = (sm >> 16) & 0xfu, rl = (sm >> 20) & 0xfu,
                                        rh = (sm >> 24) & 0xfu;
-                        const uint32_t raw = pos[g];
-                        const uint32_t ls = lseed[g];
+                        const unsigned long long v = pl[g];
+                        const uint32_t raw = (uint32_t)(v >> 16), ls = (uint32_t)(v & 0xffffu);
                         p = raw > base ? raw - base : 0u; // adjust_ref_pos_rmdup, 1893-1917
                         const uint32_t rs = (((ls >> shift) ^ rl) | ((ls >> (6 + shift)) ^ rh)) & 7u; // 2107-2112
-                        ok = (rs == 0) && (e != 0); // element 0 of the batch is dropped (2113)
+                        ok = (rs == 0) && (el != 0); // element 0 of the batch is dropped (2113)
                     }
                     const uint32_t m = __ballot_sync(0xffffffffu, ok);
-                    if (ok) S.buf[kept + __popc(m & lt)] = p;
+                    if (ok) scratch[kept + __popc(m & lt)] = p;
                     kept += __popc(m);
                 }
                 __syncwarp();
                 uint32_t u = 0;
                 uint32_t *dst = B.cand_ub + e0;
                 if (kept <= 32) {
-                    uint32_t v = lane < kept ? S.buf[lane] : 0xffffffffu;
+                    uint32_t v = lane < kept ? scratch[lane] : 0xffffffffu;
                     warp_sort_small(v);
                     const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
                     const bool keep = lane < kept && (lane == 0 || prev != v);
@@ -532,7 +681,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(uint32_t nitems, const
                 } else {
                     uint32_t n2 = 64;
                     while (n2 < kept) n2 <<= 1;
-                    uint32_t *buf = S.buf;
+                    uint32_t *buf = scratch;
                     for (uint32_t i = kept + lane; i < n2; i += 32) buf[i] = 0xffffffffu;
                     __syncwarp();
                     for (uint32_t size = 2; size <= n2; size <<= 1) {
@@ -557,7 +706,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(uint32_t nitems, const
                         u += __popc(m);
                     }
                 }
-                if (lane == 0) B.bt_cnt[slot] = u;
+                if (lane == 0) B.bt_cnt[sbase + b] = u;
                 total += u;
                 __syncwarp();
             }
@@ -579,9 +728,10 @@ __global__ void k_compact(uint32_t nitems, MapBufs B, uint64_t cap_chunks, uint6
             if (lane == 0) atomicOr(&B.tot[TOT_FLAGS], OV_CANDS);
             continue;
         }
-        const uint32_t cb = B.it_choff[item];
+        const uint32_t sbase = B.it_choff[item] + item, nref = B.it_nch[item];
         for (uint32_t b = 0; b < nb; b++) {
-            const uint32_t n = B.bt_cnt[cb + b], e0 = B.bt_e0[cb + b];
+            const uint32_t n = B.bt_cnt[sbase + b];
+            const uint32_t e0 = nref ? B.bt_e0[sbase + b] : B.it_eloff[item];
             for (uint32_t j = lane; j < n; j += 32) {
                 B.cc_pos[o + j] = B.cand_ub[e0 + j];
                 B.cc_item[o + j] = item;
@@ -945,7 +1095,7 @@ __global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uin
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
     unsigned long long locs_total = 0, mapped = 0;
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
-        const uint32_t s0 = B.it_choff[item], nb = B.it_nbat[item];
+        const uint32_t s0 = B.it_choff[item] + item, nb = B.it_nbat[item];
         uint32_t cnext = B.it_coff[item];
         uint32_t num = 0, len = 0, last = 0, mainf = 1, nrec = 0, nw = 0, nby = 0;
         uint32_t recbase = 0, wbase = 0, bbase = 0;
@@ -1065,7 +1215,7 @@ static int dmalloc(T **p, uint64_t count) {
 static void free_bufs(MapBufs &B) {
     void *ps[] = {B.it_w, B.sel_start, B.sel_count, B.sel_meta, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
-                  B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.cand_ub, B.cc_pos,
+                  B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena,
                   B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
     for (void *p : ps) cudaFree(p);
@@ -1073,6 +1223,8 @@ static void free_bufs(MapBufs &B) {
 }
 
 static uint64_t scan_cap(const swm_mapper *m) { return m->cap_items + 1; }
+
+static unsigned cand_grid(const swm_mapper *m) { return grid_cap(m->cap_items * 32, CAND_WARPS * 32, 8); }
 
 static int alloc_items(swm_mapper *m) {
     MapBufs &B = m->b;
@@ -1106,16 +1258,17 @@ static int alloc_work(swm_mapper *m) {
     MapBufs &B = m->b;
     int rc = SWM_OK;
     cudaFree(B.ch_g); cudaFree(B.ch_meta); cudaFree(B.bt_c0); cudaFree(B.bt_c1); cudaFree(B.bt_e0);
-    cudaFree(B.bt_cnt); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
+    cudaFree(B.bt_cnt); cudaFree(B.sort_scratch); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
     cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
     cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
     cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
     rc |= dmalloc(&B.ch_g, m->cap_chunks);
     rc |= dmalloc(&B.ch_meta, m->cap_chunks);
-    rc |= dmalloc(&B.bt_c0, m->cap_chunks);
-    rc |= dmalloc(&B.bt_c1, m->cap_chunks);
-    rc |= dmalloc(&B.bt_e0, m->cap_chunks);
-    rc |= dmalloc(&B.bt_cnt, m->cap_chunks);
+    rc |= dmalloc(&B.bt_c0, m->cap_chunks + m->cap_items);
+    rc |= dmalloc(&B.bt_c1, m->cap_chunks + m->cap_items);
+    rc |= dmalloc(&B.bt_e0, m->cap_chunks + m->cap_items);
+    rc |= dmalloc(&B.bt_cnt, m->cap_chunks + m->cap_items);
+    rc |= dmalloc(&B.sort_scratch, (uint64_t)cand_grid(m) * CAND_WARPS * SWM_BATCH_POSITIONS);
     rc |= dmalloc(&B.cand_ub, m->cap_elems);
     rc |= dmalloc(&B.cc_pos, m->cap_cands);
     rc |= dmalloc(&B.cc_item, m->cap_cands);
@@ -1155,7 +1308,7 @@ extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper *
     m->stride_cap = 0;
     int rc = SWM_OK;
     if (cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking) != cudaSuccess) rc = SWM_ERR_CUDA;
-    for (int i = 0; i < 8 && rc == SWM_OK; i++)
+    for (int i = 0; i < 9 && rc == SWM_OK; i++)
         if (cudaEventCreate(&m->ev[i]) != cudaSuccess) rc = SWM_ERR_CUDA;
     if (rc == SWM_OK) rc = alloc_items(m);
     if (rc == SWM_OK) rc = alloc_work(m);
@@ -1194,7 +1347,7 @@ extern "C" void swm_mapper_free(swm_mapper *m) {
     cudaFreeHost(m->h_nrec);
     cudaFreeHost(m->h_tot);
     cudaFreeHost(m->h_stat);
-    for (int i = 0; i < 8; i++)
+    for (int i = 0; i < 9; i++)
         if (m->ev[i]) cudaEventDestroy(m->ev[i]);
     if (m->st) cudaStreamDestroy(m->st);
     free(m);
@@ -1220,7 +1373,8 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     SWM_CUDA(cudaMemsetAsync(B.tot, 0, TOT_N * 4, st));
     SWM_CUDA(cudaMemsetAsync(B.stat, 0, ST_N * 8, st));
     SWM_CUDA(cudaEventRecord(m->ev[0], st));
-    k_seed<<<grid_cap(nitems, 128, 32), 128, 0, st>>>(d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, ix->k, B);
+    k_seed<<<grid_cap((uint64_t)nitems * 32, SEED_WARPS * 32, 16), SEED_WARPS * 32, 0, st>>>(
+        d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, ix->k, B);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[1], st));
@@ -1229,12 +1383,11 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     rc = swm_exclusive_scan(B.it_nel, B.it_eloff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_ELEMS, st);
     if (rc) return rc;
     m->launches += 6;
-    k_plan<<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, ix->d_pos, B, m->cap_chunks, m->cap_elems);
+    k_plan<<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, ix->d_pl, B, m->cap_chunks, m->cap_elems);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[2], st));
-    k_cand<<<grid_cap((uint64_t)nitems * 32, CAND_WARPS * 32, 8), CAND_WARPS * 32, 0, st>>>(
-        nitems, ix->d_pos, ix->d_lseed, B, m->cap_chunks, m->cap_elems);
+    k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(nitems, ix->d_pl, B, m->cap_chunks, m->cap_elems);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[3], st));
@@ -1251,12 +1404,13 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
                                                                m->cap_cands, m->cap_arena);
     m->launches++;
     LAUNCH_CHECK();
+    SWM_CUDA(cudaEventRecord(m->ev[5], st));
     k_traceback<<<grid_cap(m->cap_cands, 128, 64), 128, 0, st>>>(d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
                                                                   ix->ref_length, B, m->cap_chunks, m->cap_elems,
                                                                   m->cap_cands, m->cap_arena);
     m->launches++;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[5], st));
+    SWM_CUDA(cudaEventRecord(m->ev[6], st));
     k_records<false><<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems, m->cap_cands,
                                                                  m->cap_recs, m->cap_words, m->cap_bytes);
     rc = swm_exclusive_scan(B.it_nrec, B.it_recoff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_RECS, st);
@@ -1270,7 +1424,7 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     k_batches_stat<<<grid_cap(nitems, 256, 8), 256, 0, st>>>(nitems, B);
     m->launches += 12;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[6], st));
+    SWM_CUDA(cudaEventRecord(m->ev[7], st));
     return SWM_OK;
 }
 
@@ -1337,12 +1491,12 @@ static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *a
         return alloc_work(m);
     }
     float t;
-    for (int i = 0; i < 6; i++) {
+    for (int i = 0; i < 7; i++) {
         cudaEventElapsedTime(&t, m->ev[i], m->ev[i + 1]);
         m->stage_ms[i] = t;
     }
-    cudaEventElapsedTime(&t, m->ev[0], m->ev[6]);
-    m->stage_ms[6] = t;
+    cudaEventElapsedTime(&t, m->ev[0], m->ev[7]);
+    m->stage_ms[7] = t;
     const unsigned long long *stat = m->h_stat;
     swm_map_stats &S = m->stats;
     memset(&S, 0, sizeof S);
@@ -1628,9 +1782,10 @@ extern "C" int swm_mapper_stats(const swm_mapper *m, swm_map_stats *s) {
 }
 
 extern "C" int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float *ms) {
-    static const char *names[7] = {"seed", "plan", "candidates", "compact", "verify", "records", "total"};
+    static const char *names[8] = {"seed", "plan", "candidates", "compact", "verify", "traceback", "records",
+                                   "total"};
     if (!m || !stage || !ms) return SWM_ERR_ARG;
-    for (int i = 0; i < 7; i++)
+    for (int i = 0; i < 8; i++)
         if (!strcmp(stage, names[i])) {
             *ms = m->stage_ms[i];
             return SWM_OK;
@@ -1656,5 +1811,15 @@ extern "C" int swm_mapper_debug_candidates(const swm_mapper *m, uint32_t *item, 
         if (err) SWM_CUDA(cudaMemcpy(err, m->b.vr_err, k * 4, cudaMemcpyDeviceToHost));
         if (loc) SWM_CUDA(cudaMemcpy(loc, m->b.vr_mloc, k * 4, cudaMemcpyDeviceToHost));
     }
+    return SWM_OK;
+}
+
+extern "C" int swm_mapper_debug_read_words(const swm_mapper *m, uint32_t *words, uint64_t cap_items) {
+    if (!m || !words) return SWM_ERR_ARG;
+    if (!m->have_result) return SWM_ERR_STATE;
+    SWM_CUDA(cudaSetDevice(m->device));
+    uint64_t n = 2 * m->cur_n;
+    if (n > cap_items) n = cap_items;
+    if (n) SWM_CUDA(cudaMemcpy(words, m->b.it_w, n * 32 * 4, cudaMemcpyDeviceToHost));
     return SWM_OK;
 }

@@ -172,3 +172,50 @@ def test_gpu_packed_pingpong_equals_strided(cuda_lib):
     ms[0].wait_packed(bufs[0])
     got.extend((r[0] + 8000,) + r[1:] for r in bufs[0].records())
     assert got == want
+
+
+def _even(x):
+    x = np.uint64(x) & np.uint64(0x55555555)
+    x = (x | (x >> np.uint64(1))) & np.uint64(0x33333333)
+    x = (x | (x >> np.uint64(2))) & np.uint64(0x0F0F0F0F)
+    x = (x | (x >> np.uint64(4))) & np.uint64(0x00FF00FF)
+    x = (x | (x >> np.uint64(8))) & np.uint64(0x0000FFFF)
+    return int(x)
+
+
+def test_gpu_read_encoding_every_length(cuda_lib):
+    """Per-item read words against the oracle's literal get_seed_from_reads
+    state machine, for every read length 15..254 on both strands, with N and
+    lowercase bases mixed in (covers every tail-encoder case)."""
+    g = genome(300_000, 21)
+    rng = np.random.default_rng(22)
+    lens = np.arange(15, 255, dtype=np.uint32)
+    n = lens.size * 2
+    lens = np.concatenate([lens, lens])
+    reads = np.zeros((n, 254), np.uint8)
+    for i in range(n):
+        L = int(lens[i])
+        st = int(rng.integers(0, g.size - 300))
+        reads[i, :L] = g[st:st + L]
+        if i >= n // 2:
+            for _ in range(int(rng.integers(1, 4))):
+                reads[i, int(rng.integers(0, L))] = ord("N")
+            reads[i, int(rng.integers(0, L))] = ord("c")
+    ix = cuda_lib.Index.build(g)
+    m = cuda_lib.Mapper(ix, max_reads=n)
+    m.map(reads, lens, 4)
+    words = m.debug_read_words(n)
+    comp = bytes.maketrans(b"ACGT", b"TGCA")
+    for it in range(2 * n):
+        r, strand = it >> 1, it & 1
+        s = bytes(reads[r, :lens[r]])
+        if strand:
+            s = s[::-1].translate(comp)
+        w = po.encode_read(s)
+        want = np.zeros(32, np.uint64)
+        for b in range(8):
+            a0, a1 = int(w[2 * b]), int(w[2 * b + 1])
+            want[2 * b] = _even(a0) | (_even(a1) << 16)
+            want[2 * b + 1] = _even(a0 >> 1) | (_even(a1 >> 1) << 16)
+        want[16:] = w[16:]
+        assert np.array_equal(words[it].astype(np.uint64), want), (it, int(lens[r]))
