@@ -47,7 +47,7 @@ enum {
     ST_N
 };
 // device totals (u32), written by the scans
-enum { TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT_ARENA, TOT_FLAGS, TOT_N };
+enum { TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT_ARENA, TOT_FLAGS, TOT_TB, TOT_SLOW, TOT_N };
 
 #define ARENA_CAP_DEFAULT (1u << 20)
 
@@ -78,6 +78,8 @@ struct MapBufs {
     uint8_t *vr_cig;  // cap_cands * SWM_CIGAR_SLOT
     uint32_t *vr_aoff;
     uint8_t *arena;   // long CIGAR texts
+    uint32_t *tb_list;   // candidates that need a traceback (cap_cands)
+    uint32_t *slow_list; // tracebacks whose route outgrew the fast path (cap_cands)
     // records
     uint32_t *out_w;  // cap_words
     uint8_t *out_c;   // cap_bytes
@@ -216,12 +218,17 @@ __device__ __forceinline__ bool block_failed(const MapBufs &B, uint64_t cap_chun
 
 #define SEED_WARPS 4
 
+// Shared state of one warp: 32 items, word w of item t at [w][(t + w) % 32].
+// The skew keeps both access patterns free of bank conflicts: all lanes on
+// one item reading different words (phases A and C), and each lane on its
+// own item (phase B).
 struct SeedSmem {
-    uint32_t pl[16];    // [2b] lo / [2b + 1] hi plane of bases 32b .. 32b + 31
-    uint32_t w2[16];    // 2-bit words, 16 bases each
-    uint32_t cnt[16];   // bucket counts summed per long seed
-    uint32_t idx[16];   // long seed order (exchange sort)
+    uint32_t pl[16][32];   // [2b] lo / [2b + 1] hi plane of bases 32b .. 32b + 31
+    uint32_t w2[16][32];   // 2-bit words, 16 bases each
+    uint32_t cnt[16][32];  // bucket counts summed per long seed
+    uint32_t idx[16][32];  // long seed order (exchange sort)
 };
+#define SK(arr, w, t) S.arr[(w)][((t) + (w)) & 31]
 
 __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict__ reads,
                                                           const uint32_t *__restrict__ lens, uint64_t stride,
@@ -236,186 +243,215 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict
     uint32_t *__restrict__ sel_meta = B.sel_meta;
     const uint32_t nitems = 2 * nreads;
     const uint32_t klong = k + SWM_SEED_STEP - 1;
-    for (uint32_t item = blockIdx.x * SEED_WARPS + wib; item < nitems; item += gridDim.x * SEED_WARPS) {
-        const uint32_t r = item >> 1, strand = item & 1;
-        const uint32_t L = lens[r];
-        const uint32_t e = e_arr ? e_arr[r] : e_glob;
-        if (L > SWM_MAX_READ_LEN || L > stride || L / klong > 16 || e > SWM_MAX_ERRORS) {
-            // outside the envelope: no work for this item, and the block fails
-            if (lane == 0) {
-                atomicOr(&B.tot[TOT_FLAGS], OV_BAD);
-                B.it_nsel[item] = 0;
-                B.it_e[item] = 0;
-                B.it_nch[item] = 0;
-                B.it_nel[item] = 0;
-                B.it_nbat[item] = 0;
+    const uint32_t kmask = (1u << k) - 1, lmask = (1u << klong) - 1, rmask = (1u << (SWM_SEED_STEP - 1)) - 1;
+    for (uint32_t g0 = (blockIdx.x * SEED_WARPS + wib) * 32; g0 < nitems; g0 += gridDim.x * SEED_WARPS * 32) {
+        // ---- phase A, item by item, lanes in parallel: planes, clean 2-bit
+        // words, bucket counts per long seed
+        uint32_t my_P = 0, my_jt = 0xffffffffu, my_nl = 0, my_L = 0, my_ok = 0, my_hasn = 0;
+        for (uint32_t t = 0; t < 32; t++) {
+            const uint32_t item = g0 + t;
+            if (item >= nitems) break;
+            const uint32_t r = item >> 1, strand = item & 1;
+            const uint32_t L = lens[r];
+            const uint32_t e = e_arr ? e_arr[r] : e_glob;
+            const bool ok = !(L > SWM_MAX_READ_LEN || L > stride || L / klong > 16 || e > SWM_MAX_ERRORS);
+            if (!ok) {
+                if (lane == t) my_ok = 0;
+                continue;
             }
-            continue;
-        }
-        const ReadView rv{reads + (uint64_t)r * stride, L, strand};
-        const uint32_t nl = L / klong;
-        // first tail trigger (only within the last long seed) and the last
-        // position of the clean visit
-        int jt = -1;
-        uint32_t P = 0;
-        if (nl) {
-            P = nl * klong - 1;
-            for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
-                const uint32_t rp = (nl - 1) * klong + sft + k - 1;
-                if (L - rp < k) {
-                    jt = (int)((nl - 1) * SWM_SEED_STEP + sft);
-                    P = rp;
-                    break;
-                }
-            }
-        }
-        const uint32_t vis = nl ? (jt >= 0 ? L : nl * klong) : 0u; // bases with plane bits
-        const uint32_t seedspan = nl * klong;                          // bases inside seed windows
-        // planes and the non-ACGT flag by ballots over 32-base groups
-        bool has_n = false;
-        for (uint32_t b = 0; b < 8; b++) {
-            const uint32_t p = 32 * b + lane;
-            uint32_t code = 0;
-            bool n = false;
-            if (p < vis) {
-                const char ch = rv(p);
-                code = base_code_c(ch);
-                n = !is_acgt(ch) && p < seedspan;
-            }
-            const uint32_t lo = __ballot_sync(0xffffffffu, code & 1u), hi = __ballot_sync(0xffffffffu, code >> 1);
-            has_n |= __any_sync(0xffffffffu, n);
-            if (lane == 0) {
-                S.pl[2 * b] = lo;
-                S.pl[2 * b + 1] = hi;
-            }
-        }
-        __syncwarp();
-        // 2-bit words: complete words up to P from the planes, the rest 0
-        if (lane < 16) {
-            uint32_t wv = 0;
-            if (nl && 16 * lane + 15 <= P) {
-                const uint32_t sh = (lane & 1) * 16;
-                const uint32_t lo = (S.pl[2 * (lane >> 1)] >> sh) & 0xffffu, hi = (S.pl[2 * (lane >> 1) + 1] >> sh) & 0xffffu;
-                wv = spread_bits(lo) | (spread_bits(hi) << 1);
-            }
-            S.w2[lane] = wv;
-        }
-        __syncwarp();
-        if (lane == 0 && jt >= 0) {
-            // literal replay of the remaining calls (mapper_cpe.c:1246-1364)
-            auto code_at = [&](uint32_t q) -> uint32_t {
-                return ((S.pl[2 * (q >> 5)] >> (q & 31)) & 1u) | (((S.pl[2 * (q >> 5) + 1] >> (q & 31)) & 1u) << 1);
-            };
-            uint32_t acc = 0;
-            if (P % 16 != 15)
-                for (uint32_t q = P & ~15u; q <= P; q++) acc |= code_at(q) << ((q % 16) * 2);
-            for (uint32_t j = (uint32_t)jt; j < nl * SWM_SEED_STEP; j++) {
-                const uint32_t rp = (j / SWM_SEED_STEP) * klong + j % SWM_SEED_STEP + k - 1;
-                if (j > (uint32_t)jt) { // the one base this call's main loop adds
-                    acc |= code_at(rp) << ((rp % 16) * 2);
-                    if (rp % 16 == 15) {
-                        S.w2[rp / 16] = acc;
-                        acc = 0;
+            const ReadView rv{reads + (uint64_t)r * stride, L, strand};
+            const uint32_t nl = L / klong;
+            // first tail trigger (only calls of the last long seed can fire it)
+            uint32_t jt = 0xffffffffu, P = nl ? nl * klong - 1 : 0u;
+            if (nl) {
+                for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
+                    const uint32_t rp = (nl - 1) * klong + sft + k - 1;
+                    if (L - rp < k) {
+                        jt = (nl - 1) * SWM_SEED_STEP + sft;
+                        P = rp;
+                        break;
                     }
                 }
-                for (uint32_t q = rp; q < L; q++) { // tail encoder, re-run from rp
-                    acc |= code_at(q) << ((q % 16) * 2);
-                    if (q % 16 == 15) {
-                        S.w2[q / 16] = acc;
-                        acc = 0;
+            }
+            const uint32_t vis = nl ? (jt != 0xffffffffu ? L : nl * klong) : 0u;
+            const uint32_t seedspan = nl * klong;
+            bool has_n = false;
+#pragma unroll
+            for (uint32_t b = 0; b < 8; b++) {
+                const uint32_t p = 32 * b + lane;
+                uint32_t code = 0;
+                bool n = false;
+                if (p < vis) {
+                    const char ch = rv(p);
+                    code = base_code_c(ch);
+                    n = !is_acgt(ch) && p < seedspan;
+                }
+                const uint32_t lo = __ballot_sync(0xffffffffu, code & 1u), hi = __ballot_sync(0xffffffffu, code >> 1);
+                has_n |= __any_sync(0xffffffffu, n);
+                if (lane == 2 * b) SK(pl, 2 * b, t) = lo;
+                if (lane == 2 * b + 1) SK(pl, 2 * b + 1, t) = hi;
+            }
+            __syncwarp();
+            if (lane < 16) { // complete words up to P from the planes, the rest 0
+                uint32_t wv = 0;
+                if (nl && 16 * lane + 15 <= P) {
+                    const uint32_t sh = (lane & 1) * 16;
+                    const uint32_t lo = (SK(pl, 2 * (lane >> 1), t) >> sh) & 0xffffu;
+                    const uint32_t hi = (SK(pl, 2 * (lane >> 1) + 1, t) >> sh) & 0xffffu;
+                    wv = spread_bits(lo) | (spread_bits(hi) << 1);
+                }
+                SK(w2, lane, t) = wv;
+            }
+            // bucket counts of every seed, summed per long seed (choose_seed, 1372-1390)
+            const uint32_t ns_all = nl * SWM_SEED_STEP;
+            for (uint32_t j0 = 0; j0 < ns_all; j0 += 32) {
+                const uint32_t j = j0 + lane;
+                uint32_t c = 0;
+                if (j < ns_all) {
+                    const uint32_t l = j / SWM_SEED_STEP, sft = j % SWM_SEED_STEP;
+                    uint32_t sd;
+                    if (!has_n) {
+                        const uint32_t o = l * klong, wj = o >> 5, sh = o & 31;
+                        const uint32_t nlo = wj + 1 < 8 ? SK(pl, 2 * (wj + 1), t) : 0u;
+                        const uint32_t nhi = wj + 1 < 8 ? SK(pl, 2 * (wj + 1) + 1, t) : 0u;
+                        const uint32_t lo = (swm_fsr(SK(pl, 2 * wj, t), nlo, sh) >> sft) & kmask;
+                        const uint32_t hi = (swm_fsr(SK(pl, 2 * wj + 1, t), nhi, sh) >> sft) & kmask;
+                        sd = spread_bits(lo) | (spread_bits(hi) << 1);
+                    } else {
+                        sd = seed_closed(rv, k, l, sft);
                     }
+                    c = off[sd + 1] - off[sd];
                 }
-                S.w2[(L - 1) / 16] = acc;
+                c += __shfl_xor_sync(0xffffffffu, c, 1);
+                c += __shfl_xor_sync(0xffffffffu, c, 2);
+                if (j < ns_all && (j % SWM_SEED_STEP) == 0) SK(cnt, j / SWM_SEED_STEP, t) = c;
+            }
+            if (lane == t) {
+                my_P = P;
+                my_jt = jt;
+                my_nl = nl;
+                my_L = L;
+                my_ok = 1;
+                my_hasn = has_n ? 1u : 0u;
             }
         }
         __syncwarp();
-        // bucket counts of every seed, summed per long seed (choose_seed, 1372-1390)
-        const uint32_t ns_all = nl * SWM_SEED_STEP;
-        for (uint32_t j0 = 0; j0 < ns_all; j0 += 32) {
-            const uint32_t j = j0 + lane;
-            uint32_t c = 0;
-            if (j < ns_all) {
-                const uint32_t l = j / SWM_SEED_STEP, sft = j % SWM_SEED_STEP;
-                uint32_t sd;
-                if (!has_n) {
-                    const uint32_t o = l * klong, wj = o >> 5, sh = o & 31;
-                    const uint32_t nlo = wj + 1 < 8 ? S.pl[2 * (wj + 1)] : 0u, nhi = wj + 1 < 8 ? S.pl[2 * (wj + 1) + 1] : 0u;
-                    const uint32_t kmask = (1u << k) - 1;
-                    const uint32_t lo = (swm_fsr(S.pl[2 * wj], nlo, sh) >> sft) & kmask;
-                    const uint32_t hi = (swm_fsr(S.pl[2 * wj + 1], nhi, sh) >> sft) & kmask;
-                    sd = spread_bits(lo) | (spread_bits(hi) << 1);
-                } else {
-                    sd = seed_closed(rv, k, l, sft);
-                }
-                c = off[sd + 1] - off[sd];
-            }
-            c += __shfl_xor_sync(0xffffffffu, c, 1);
-            c += __shfl_xor_sync(0xffffffffu, c, 2);
-            if (j < ns_all && (j % SWM_SEED_STEP) == 0) S.cnt[j / SWM_SEED_STEP] = c;
-        }
-        if (lane < 16) S.idx[lane] = lane;
-        __syncwarp();
-        if (lane == 0) { // exchange sort, 1391-1399
+        // ---- phase B, lane t works on item t: exchange sort of the long
+        // seeds (1391-1399) and the literal replay of the tail encoder
+        // (1312-1362) from the first call whose tail test fires
+        if (g0 + lane < nitems && my_ok) {
+            const uint32_t t = lane, nl = my_nl, L = my_L, P = my_P;
+            for (uint32_t a = 0; a < 16; a++) SK(idx, a, t) = a;
             for (uint32_t a = 0; a < nl; a++)
                 for (uint32_t m = a + 1; m < nl; m++)
-                    if (S.cnt[a] > S.cnt[m]) {
-                        uint32_t t = S.cnt[a];
-                        S.cnt[a] = S.cnt[m];
-                        S.cnt[m] = t;
-                        t = S.idx[a];
-                        S.idx[a] = S.idx[m];
-                        S.idx[m] = t;
+                    if (SK(cnt, a, t) > SK(cnt, m, t)) {
+                        uint32_t x = SK(cnt, a, t);
+                        SK(cnt, a, t) = SK(cnt, m, t);
+                        SK(cnt, m, t) = x;
+                        x = SK(idx, a, t);
+                        SK(idx, a, t) = SK(idx, m, t);
+                        SK(idx, m, t) = x;
                     }
-        }
-        __syncwarp();
-        // selected slots: the (e + 1) rarest long seeds x 4 shifts
-        // (alignment_rmdup, 2194-2196); slots past nl read count 0
-        const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
-        const uint32_t ns = nsl * SWM_SEED_STEP;
-        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
-        uint32_t nref = 0, nel = 0;
-        for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
-            const uint32_t i = i0 + lane;
-            if (i < ns) {
-                const uint32_t l = S.idx[i / SWM_SEED_STEP], sft = i % SWM_SEED_STEP;
-                const uint32_t o = l * klong, wj = o >> 5, sh = o & 31;
-                const uint32_t nlo = wj + 1 < 8 ? S.pl[2 * (wj + 1)] : 0u, nhi = wj + 1 < 8 ? S.pl[2 * (wj + 1) + 1] : 0u;
-                const uint32_t lmask = (1u << klong) - 1, kmask = (1u << k) - 1;
-                const uint32_t lr = swm_fsr(S.pl[2 * wj], nlo, sh) & lmask;  // set_read_long_seeds, 2474-2478
-                const uint32_t hr = swm_fsr(S.pl[2 * wj + 1], nhi, sh) & lmask;
-                const uint32_t sd = has_n ? seed_closed(rv, k, l, sft)
-                                          : (spread_bits((lr >> sft) & kmask) | (spread_bits((hr >> sft) & kmask) << 1));
-                const uint32_t o0 = off[sd], c = off[sd + 1] - o0;
-                const uint32_t m = (1u << sft) - 1, kk = k + sft, rmask = (1u << (SWM_SEED_STEP - 1)) - 1;
-                const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & rmask; // 2483-2495
-                const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & rmask;
-                sel_start[sb + i] = o0;
-                sel_count[sb + i] = c;
-                sel_meta[sb + i] = (o + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) | (rh << 24);
-                nref += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
-                nel += c;
+            if (my_jt != 0xffffffffu) {
+                auto code_at = [&](uint32_t q) -> uint32_t {
+                    return ((SK(pl, 2 * (q >> 5), t) >> (q & 31)) & 1u) |
+                           (((SK(pl, 2 * (q >> 5) + 1, t) >> (q & 31)) & 1u) << 1);
+                };
+                uint32_t acc = 0;
+                if (P % 16 != 15)
+                    for (uint32_t q = P & ~15u; q <= P; q++) acc |= code_at(q) << ((q % 16) * 2);
+                for (uint32_t j = my_jt; j < nl * SWM_SEED_STEP; j++) {
+                    const uint32_t rp = (j / SWM_SEED_STEP) * klong + j % SWM_SEED_STEP + k - 1;
+                    if (j > my_jt) { // the one base this call's main loop adds
+                        acc |= code_at(rp) << ((rp % 16) * 2);
+                        if (rp % 16 == 15) {
+                            SK(w2, rp / 16, t) = acc;
+                            acc = 0;
+                        }
+                    }
+                    for (uint32_t q = rp; q < L; q++) { // tail encoder, re-run from rp
+                        acc |= code_at(q) << ((q % 16) * 2);
+                        if (q % 16 == 15) {
+                            SK(w2, q / 16, t) = acc;
+                            acc = 0;
+                        }
+                    }
+                    SK(w2, (L - 1) / 16, t) = acc;
+                }
             }
         }
+        __syncwarp();
+        // ---- phase C, item by item, lanes in parallel: selected slots (the
+        // (e + 1) rarest long seeds x 4 shifts, alignment_rmdup 2194-2196;
+        // slots past nl read count 0), bucket ranges, flank codes, read words
+        for (uint32_t t = 0; t < 32; t++) {
+            const uint32_t item = g0 + t;
+            if (item >= nitems) break;
+            const uint32_t ok = __shfl_sync(0xffffffffu, my_ok, t);
+            const uint32_t r = item >> 1, strand = item & 1;
+            const uint32_t e = e_arr ? e_arr[r] : e_glob;
+            if (!ok) {
+                if (lane == 0) {
+                    atomicOr(&B.tot[TOT_FLAGS], OV_BAD);
+                    B.it_nsel[item] = 0;
+                    B.it_e[item] = 0;
+                    B.it_nch[item] = 0;
+                    B.it_nel[item] = 0;
+                    B.it_nbat[item] = 0;
+                }
+                continue;
+            }
+            const uint32_t nl = __shfl_sync(0xffffffffu, my_nl, t);
+            const uint32_t L = __shfl_sync(0xffffffffu, my_L, t);
+            const bool has_n = __shfl_sync(0xffffffffu, my_hasn, t) != 0;
+            const ReadView rv{reads + (uint64_t)r * stride, L, strand};
+            const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
+            const uint32_t ns = nsl * SWM_SEED_STEP;
+            const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+            uint32_t nref = 0, nel = 0;
+            for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
+                const uint32_t i = i0 + lane;
+                if (i < ns) {
+                    const uint32_t l = SK(idx, i / SWM_SEED_STEP, t), sft = i % SWM_SEED_STEP;
+                    const uint32_t o = l * klong, wj = o >> 5, sh = o & 31;
+                    const uint32_t nlo = wj + 1 < 8 ? SK(pl, 2 * (wj + 1), t) : 0u;
+                    const uint32_t nhi = wj + 1 < 8 ? SK(pl, 2 * (wj + 1) + 1, t) : 0u;
+                    const uint32_t lr = swm_fsr(SK(pl, 2 * wj, t), nlo, sh) & lmask; // set_read_long_seeds, 2474-2478
+                    const uint32_t hr = swm_fsr(SK(pl, 2 * wj + 1, t), nhi, sh) & lmask;
+                    const uint32_t sd = has_n ? seed_closed(rv, k, l, sft)
+                                              : (spread_bits((lr >> sft) & kmask) | (spread_bits((hr >> sft) & kmask) << 1));
+                    const uint32_t o0 = off[sd], c = off[sd + 1] - o0;
+                    const uint32_t m = (1u << sft) - 1, kk = k + sft;
+                    const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & rmask; // 2483-2495
+                    const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & rmask;
+                    sel_start[sb + i] = o0;
+                    sel_count[sb + i] = c;
+                    sel_meta[sb + i] = (o + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) | (rh << 24);
+                    nref += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
+                    nel += c;
+                }
+            }
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) {
-            nref += __shfl_xor_sync(0xffffffffu, nref, d);
-            nel += __shfl_xor_sync(0xffffffffu, nel, d);
-        }
-        // read words: [0..15] Myers planes from the 2-bit words, [16..31] Hamming planes
-        uint32_t ow;
-        if (lane < 16) {
-            const uint32_t b = lane >> 1, hi = lane & 1;
-            ow = even_bits(S.w2[2 * b] >> hi) | (even_bits(S.w2[2 * b + 1] >> hi) << 16);
-        } else {
-            ow = S.pl[lane - 16];
-        }
-        B.it_w[(uint64_t)item * 32 + lane] = ow;
-        if (lane == 0) {
-            B.it_nsel[item] = (uint8_t)ns;
-            B.it_e[item] = (uint8_t)e;
-            B.it_nch[item] = nref;                  // refill chunks (beyond the first chunk of each seed)
-            B.it_nel[item] = nel;
-            B.it_nbat[item] = (nref == 0 && nel > 0) ? 1u : 0u; // k_plan sets it for items with refills
+            for (int d = 16; d > 0; d >>= 1) {
+                nref += __shfl_xor_sync(0xffffffffu, nref, d);
+                nel += __shfl_xor_sync(0xffffffffu, nel, d);
+            }
+            // read words: [0..15] Myers planes from the 2-bit words, [16..31] Hamming planes
+            uint32_t ow;
+            if (lane < 16) {
+                const uint32_t b = lane >> 1, hi = lane & 1;
+                ow = even_bits(SK(w2, 2 * b, t) >> hi) | (even_bits(SK(w2, 2 * b + 1, t) >> hi) << 16);
+            } else {
+                ow = SK(pl, lane - 16, t);
+            }
+            B.it_w[(uint64_t)item * 32 + lane] = ow;
+            if (lane == 0) {
+                B.it_nsel[item] = (uint8_t)ns;
+                B.it_e[item] = (uint8_t)e;
+                B.it_nch[item] = nref;                  // refill chunks (beyond the first chunk of each seed)
+                B.it_nel[item] = nel;
+                B.it_nbat[item] = (nref == 0 && nel > 0) ? 1u : 0u; // k_plan sets it for items with refills
+            }
         }
         __syncwarp();
     }
@@ -533,8 +569,6 @@ __global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const unsigned lo
 // ======================================================================
 // k_cand: one warp per batch slot -- gather, adjust, filter, sort-unique
 // ======================================================================
-
-#define CAND_WARPS 4
 
 __device__ __forceinline__ void warp_sort_small(uint32_t &v) {
     const uint32_t lane = lane_id();
@@ -963,6 +997,8 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ len
         }
         B.vr_loc[c] = ws; // window start, used by the traceback
         B.vr_flag[c] = VR_NEEDTB;
+        const uint32_t at = atomicAdd(&B.tot[TOT_TB], 1u);
+        B.tb_list[at] = (uint32_t)c;
     }
     warp_add_u64(&B.stat[ST_CELLS], cells);
     warp_add_u64(&B.stat[ST_PASSED], passed);
@@ -970,16 +1006,227 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ len
 
 
 // Traceback of the passing candidates that the Hamming check did not resolve
-// (align_reads, mapper_cpe.c:288-509): re-run Myers keeping D0 / HP per read
-// base, walk back from (L - 1, location), emit the start position and CIGAR.
-__global__ void __launch_bounds__(128) k_traceback(const uint32_t *__restrict__ lens,
-                                                   const uint32_t *__restrict__ b2, uint64_t b2_words,
-                                                   uint64_t ref_length, MapBufs B, uint64_t cap_chunks,
-                                                   uint64_t cap_elems, uint64_t cap_cands, uint64_t cap_arena) {
+// (align_reads, mapper_cpe.c:288-509): walk back from (L - 1, location)
+// through the D0 / HP words of the Myers run and emit the start position and
+// the CIGAR. The history is rebuilt 32 read bases at a time from (VP, VN)
+// checkpoints into shared memory (the walk only moves towards the read
+// start); the run-length route stays in shared memory too. A walk with more
+// than TB_ROUTE runs is handed to k_traceback_slow.
+#define TB_THREADS 64
+#define TB_ROUTE 48
+
+struct TbSmem {
+    uint32_t cp[8][2][TB_THREADS];   // (VP, VN) before read bases 32b ..
+    uint32_t d0[32][TB_THREADS];     // D0 of the 32 bases of the current block
+    uint32_t hp[32][TB_THREADS];     // HP of the same bases
+    uint16_t route[TB_ROUTE][TB_THREADS]; // size | kind << 12 (M S I D)
+};
+
+// 32 Myers steps of block b from (vp, vn); keeps D0 / HP when `keep`.
+__device__ __forceinline__ void myers_block(const uint32_t *WL, const uint32_t *WH, const uint32_t *rw, uint32_t b,
+                                            uint32_t steps, uint32_t MASK, uint32_t &vp, uint32_t &vn,
+                                            TbSmem *T, bool keep) {
+    const uint32_t wl0 = WL[b], wl1 = WL[b + 1], wh0 = WH[b], wh1 = WH[b + 1];
+    const uint32_t rlw = rw[2 * b], rhw = rw[2 * b + 1];
+    for (uint32_t t = 0; t < steps; t++) {
+        const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
+        const uint32_t mL = 0u - ((rlw >> t) & 1u), mH = 0u - ((rhw >> t) & 1u);
+        const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
+        uint32_t x = eq | vn;
+        const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;
+        const uint32_t hn = vp & d0;
+        const uint32_t hp = vn | ~(vp | d0);
+        x = d0 >> 1;
+        vn = x & hp;
+        vp = hn | ~(x | hp);
+        if (keep) {
+            T->d0[t][threadIdx.x] = d0;
+            T->hp[t][threadIdx.x] = hp;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__restrict__ lens,
+                                                          const uint32_t *__restrict__ b2, uint64_t b2_words,
+                                                          uint64_t ref_length, MapBufs B, uint64_t cap_chunks,
+                                                          uint64_t cap_elems, uint64_t cap_cands, uint64_t cap_arena) {
+    __shared__ TbSmem T;
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
-    const uint64_t nc = B.tot[TOT_CANDS];
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (uint64_t)gridDim.x * blockDim.x) {
-        if (B.vr_flag[c] != VR_NEEDTB) continue;
+    const uint32_t tid = threadIdx.x;
+    const uint64_t ntb = B.tot[TOT_TB];
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + tid; q < ntb; q += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = B.tb_list[q];
+        const uint32_t item = B.cc_item[c];
+        const uint32_t L = lens[item >> 1], e = B.it_e[item];
+        const uint32_t ws = B.vr_loc[c];
+        const int err = B.vr_err[c], loc = B.vr_mloc[c];
+        uint32_t WL[SWM_WIN_WORDS], WH[SWM_WIN_WORDS];
+        load_window(b2, b2_words, ws, L, e, WL, WH);
+        const uint32_t *RW = B.it_w + (uint64_t)item * 32;
+        uint32_t rw[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) rw[i] = RW[i];
+        const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
+        const uint32_t nblk = (L + 31) >> 5;
+        { // checkpoints
+            uint32_t vp = 0, vn = 0;
+            for (uint32_t b = 0; b < nblk; b++) {
+                T.cp[b][0][tid] = vp;
+                T.cp[b][1][tid] = vn;
+                if (b + 1 < nblk) myers_block(WL, WH, rw, b, 32, MASK, vp, vn, &T, false);
+            }
+        }
+        int cur = -1;
+        auto bits = [&](int i, int ss, uint32_t *d0b, uint32_t *hpb) {
+            const int b = i >> 5;
+            if (b != cur) {
+                uint32_t vp = T.cp[b][0][tid], vn = T.cp[b][1][tid];
+                const uint32_t steps = min(32u, L - 32u * (uint32_t)b);
+                myers_block(WL, WH, rw, (uint32_t)b, steps, MASK, vp, vn, &T, true);
+                cur = b;
+            }
+            const uint32_t d0 = T.d0[i & 31][tid], hp = T.hp[i & 31][tid];
+            const bool in = ss >= 0 && ss < 32; // defined read of bits outside 0..31: 0
+            *d0b = in ? ((d0 >> ss) & 1u) : 0u;
+            *hpb = in ? ((hp >> ss) & 1u) : 0u;
+        };
+#define TREF(m_) (((WL[(m_) >> 5] >> ((m_) & 31)) & 1u) | (((WH[(m_) >> 5] >> ((m_) & 31)) & 1u) << 1))
+#define TREAD(r_) (((rw[2 * ((r_) >> 5)] >> ((r_) & 31)) & 1u) | (((rw[2 * ((r_) >> 5) + 1] >> ((r_) & 31)) & 1u) << 1))
+        int start = loc - (int)L + 1;
+        int match_site = loc;
+        int search_site = match_site - ((int)L - 1);
+        int i = (int)L - 1, sum_err = 0;
+        uint32_t nr = 0; // route entries written (index 1 .. nr in the reference's numbering)
+        bool overflow = false;
+        int pre_size = 1;
+        uint32_t pre = 0; // 0 M, 1 S, 2 I, 3 D
+        auto push = [&](uint32_t kind) {
+            if (pre != kind) {
+                if (nr < TB_ROUTE) T.route[nr][tid] = (uint16_t)(pre_size | (pre << 12));
+                else overflow = true;
+                nr++;
+                pre_size = 1;
+                pre = kind;
+            } else {
+                pre_size++;
+            }
+        };
+        { // first step, mapper_cpe.c:380-410
+            uint32_t d0b, hpb;
+            bits(i, search_site, &d0b, &hpb);
+            if (d0b && TREF(match_site) == TREAD(i)) {
+                i--; pre = 0; match_site--;
+            } else if (!d0b && TREF(match_site) != TREAD(i)) {
+                i--; pre = 1; match_site--; sum_err++;
+            } else if (hpb) {
+                i--; search_site++; pre = 1; sum_err++; start++; // labelled S in the reference
+            } else {
+                search_site--; pre = 3; match_site--; sum_err++; start--;
+            }
+        }
+        while (i >= 0) { // mapper_cpe.c:412-466
+            if (sum_err == err) break;
+            if (match_site < 0) break; // defined stop below the window start
+            uint32_t d0b, hpb;
+            bits(i, search_site, &d0b, &hpb);
+            if (d0b && TREF(match_site) == TREAD(i)) {
+                i--; match_site--; push(0);
+            } else if (!d0b && TREF(match_site) != TREAD(i)) {
+                i--; match_site--; sum_err++; push(1);
+            } else if (hpb) {
+                i--; search_site++; sum_err++; push(2); start++;
+            } else {
+                search_site--; match_site--; sum_err++; push(3); start--;
+            }
+        }
+#undef TREF
+#undef TREAD
+        if (nr < TB_ROUTE) T.route[nr][tid] = (uint16_t)(pre_size | (pre << 12));
+        else overflow = true;
+        nr++;
+        if (i >= 0) {
+            if (nr < TB_ROUTE) T.route[nr][tid] = (uint16_t)((i + 1) | (0u << 12));
+            else overflow = true;
+            nr++;
+        }
+        if (overflow) {
+            const uint32_t at = atomicAdd(&B.tot[TOT_SLOW], 1u);
+            B.slow_list[at] = c;
+            continue;
+        }
+        // CIGAR text, read start first: consecutive M / S runs merge into M
+        // (mapper_cpe.c:486-504). First its length, then the bytes.
+        static const char KC[4] = {'M', 'S', 'I', 'D'};
+        auto digits = [](uint32_t v) -> int {
+            int d = 0;
+            for (; v; v /= 10) d++;
+            return d;
+        };
+        int n = 0;
+        for (int j = (int)nr - 1; j >= 0;) {
+            const uint32_t kind = T.route[j][tid] >> 12;
+            if (kind <= 1) {
+                uint32_t smv = 0;
+                while (j >= 0 && (T.route[j][tid] >> 12) <= 1) {
+                    smv += T.route[j][tid] & 0xfffu;
+                    j--;
+                }
+                n += digits(smv) + 1;
+            } else {
+                n += digits(T.route[j][tid] & 0xfffu) + 1;
+                j--;
+            }
+        }
+        uint8_t *slot = B.vr_cig + (uint64_t)c * SWM_CIGAR_SLOT;
+        uint8_t *dst = slot + 2;
+        if (n > SWM_CIGAR_SLOT - 2) {
+            const uint32_t at = atomicAdd(&B.tot[TOT_ARENA], (uint32_t)n);
+            if ((uint64_t)at + n > cap_arena) {
+                atomicOr(&B.tot[TOT_FLAGS], OV_ARENA);
+                continue;
+            }
+            dst = B.arena + at;
+            B.vr_aoff[c] = at;
+        }
+        int w = 0;
+        for (int j = (int)nr - 1; j >= 0;) {
+            const uint32_t kind = T.route[j][tid] >> 12;
+            uint32_t v;
+            char ch;
+            if (kind <= 1) {
+                v = 0;
+                while (j >= 0 && (T.route[j][tid] >> 12) <= 1) {
+                    v += T.route[j][tid] & 0xfffu;
+                    j--;
+                }
+                ch = 'M';
+            } else {
+                v = T.route[j][tid] & 0xfffu;
+                ch = KC[kind];
+                j--;
+            }
+            w += put_len(dst + w, v);
+            dst[w++] = (uint8_t)ch;
+        }
+        slot[0] = (uint8_t)err;
+        slot[1] = (uint8_t)n;
+        B.vr_tlen[c] = (uint16_t)n;
+        B.vr_loc[c] = ws + (uint32_t)start + 1;
+        B.vr_flag[c] = VR_TB;
+    }
+}
+
+// Traceback with the whole D0 / HP history in local memory, for the rare walks
+// whose route outgrows the shared-memory path of k_traceback (align_reads,
+// mapper_cpe.c:288-509).
+__global__ void __launch_bounds__(128) k_traceback_slow(const uint32_t *__restrict__ lens,
+                                                        const uint32_t *__restrict__ b2, uint64_t b2_words,
+                                                        uint64_t ref_length, MapBufs B, uint64_t cap_chunks,
+                                                        uint64_t cap_elems, uint64_t cap_cands, uint64_t cap_arena) {
+    if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint64_t nslow = B.tot[TOT_SLOW];
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nslow; q += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t c = B.slow_list[q];
         const uint32_t item = B.cc_item[c];
         const uint32_t L = lens[item >> 1], e = B.it_e[item];
         const uint32_t ws = B.vr_loc[c];
@@ -1216,7 +1463,8 @@ static void free_bufs(MapBufs &B) {
     void *ps[] = {B.it_w, B.sel_start, B.sel_count, B.sel_meta, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
-                  B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena,
+                  B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
+                  B.slow_list,
                   B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
     for (void *p : ps) cudaFree(p);
     memset(&B, 0, sizeof(B));
@@ -1261,6 +1509,7 @@ static int alloc_work(swm_mapper *m) {
     cudaFree(B.bt_cnt); cudaFree(B.sort_scratch); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
     cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
     cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
+    cudaFree(B.tb_list); cudaFree(B.slow_list);
     cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
     rc |= dmalloc(&B.ch_g, m->cap_chunks);
     rc |= dmalloc(&B.ch_meta, m->cap_chunks);
@@ -1280,6 +1529,8 @@ static int alloc_work(swm_mapper *m) {
     rc |= dmalloc(&B.vr_cig, m->cap_cands * SWM_CIGAR_SLOT);
     rc |= dmalloc(&B.vr_aoff, m->cap_cands);
     rc |= dmalloc(&B.arena, m->cap_arena);
+    rc |= dmalloc(&B.tb_list, m->cap_cands);
+    rc |= dmalloc(&B.slow_list, m->cap_cands);
     rc |= dmalloc(&B.out_w, m->cap_words);
     rc |= dmalloc(&B.out_c, m->cap_bytes);
     rc |= dmalloc(&B.rec_woff, m->cap_recs);
@@ -1373,7 +1624,7 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     SWM_CUDA(cudaMemsetAsync(B.tot, 0, TOT_N * 4, st));
     SWM_CUDA(cudaMemsetAsync(B.stat, 0, ST_N * 8, st));
     SWM_CUDA(cudaEventRecord(m->ev[0], st));
-    k_seed<<<grid_cap((uint64_t)nitems * 32, SEED_WARPS * 32, 16), SEED_WARPS * 32, 0, st>>>(
+    k_seed<<<grid_cap((uint64_t)nitems, SEED_WARPS * 32, 8), SEED_WARPS * 32, 0, st>>>(
         d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, ix->k, B);
     m->launches++;
     LAUNCH_CHECK();
@@ -1405,10 +1656,13 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[5], st));
-    k_traceback<<<grid_cap(m->cap_cands, 128, 64), 128, 0, st>>>(d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
-                                                                  ix->ref_length, B, m->cap_chunks, m->cap_elems,
-                                                                  m->cap_cands, m->cap_arena);
-    m->launches++;
+    k_traceback<<<grid_cap(m->cap_cands, TB_THREADS, 8), TB_THREADS, 0, st>>>(
+        d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
+        m->cap_arena);
+    k_traceback_slow<<<grid_cap(m->cap_cands, 128, 4), 128, 0, st>>>(
+        d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
+        m->cap_arena);
+    m->launches += 2;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[6], st));
     k_records<false><<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems, m->cap_cands,
@@ -1590,6 +1844,15 @@ static int ensure_host(void **p, uint64_t *cap, uint64_t need, size_t elt) {
     return SWM_OK;
 }
 
+static bool is_pinned(const void *p) {
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 // Copy the packed records of the last block to pinned staging.
 static int download_results(swm_mapper *m) {
     if (!m->have_result) return SWM_ERR_STATE;
@@ -1657,9 +1920,40 @@ extern "C" int swm_map_fetch(swm_mapper *m, swm_result *r) {
 
 extern "C" int swm_map_fetch_packed(swm_mapper *m, swm_packed_result *r) {
     if (!m || !r) return SWM_ERR_ARG;
+    if (!m->have_result) return SWM_ERR_STATE;
+    const uint64_t nrec = m->tot[TOT_RECS], nw = m->tot[TOT_WORDS], nby = m->tot[TOT_BYTES];
+    if (nw <= r->words_cap && nby <= r->cigar_cap && nrec <= r->records_cap && is_pinned(r->words) &&
+        is_pinned(r->cigar) && (!r->record_cigar_len || is_pinned(r->record_cigar_len))) {
+        // page-locked caller buffers: copy the packed results straight into them
+        SWM_CUDA(cudaSetDevice(m->device));
+        const uint64_t nitems = 2 * m->cur_n;
+        int rc0 = ensure_host((void **)&m->h_nrec, &m->h_cap_items, nitems, 4);
+        if (rc0) return rc0;
+        cudaStream_t st = m->st;
+        if (nw) SWM_CUDA(cudaMemcpyAsync(r->words, m->b.out_w, nw * 4, cudaMemcpyDeviceToHost, st));
+        if (nby) SWM_CUDA(cudaMemcpyAsync(r->cigar, m->b.out_c, nby, cudaMemcpyDeviceToHost, st));
+        if (nrec && r->record_cigar_len)
+            SWM_CUDA(cudaMemcpyAsync(r->record_cigar_len, m->b.rec_blen, nrec * 4, cudaMemcpyDeviceToHost, st));
+        if (nitems) SWM_CUDA(cudaMemcpyAsync(m->h_nrec, m->b.it_nrec, nitems * 4, cudaMemcpyDeviceToHost, st));
+        SWM_CUDA(cudaStreamSynchronize(st));
+        m->stats.d2h_bytes = nw * 4 + nby + (r->record_cigar_len ? nrec * 4 : 0) + nitems * 4 + TOT_N * 4 + ST_N * 8;
+        r->n_records = nrec;
+        r->n_words = nw;
+        r->n_cigar = nby;
+        int status = SWM_OK;
+        uint64_t nu = 0;
+        for (uint64_t rd = 0; rd < m->cur_n; rd++) {
+            if (m->h_nrec[2 * rd] + m->h_nrec[2 * rd + 1] == 0) {
+                if (nu < r->unmapped_cap && r->unmapped) r->unmapped[nu] = (uint32_t)(2 * rd + 1);
+                else status = SWM_ERR_OVERFLOW;
+                nu++;
+            }
+        }
+        r->n_unmapped = nu;
+        return status;
+    }
     int rc = download_results(m);
     if (rc) return rc;
-    const uint64_t nrec = m->tot[TOT_RECS], nw = m->tot[TOT_WORDS], nby = m->tot[TOT_BYTES];
     r->n_records = nrec;
     r->n_words = nw;
     r->n_cigar = nby;
@@ -1707,12 +2001,24 @@ static int stage_inputs(swm_mapper *m, const swm_batch *b) {
         }
         m->stride_cap = cap;
     }
-    memcpy(m->h_reads, b->reads, bytes);
-    memcpy(m->h_lens, b->reads_len, n * 4);
-    if (b->errors_per_read) memcpy(m->h_e, b->errors_per_read, n);
-    SWM_CUDA(cudaMemcpyAsync(m->d_reads, m->h_reads, bytes, cudaMemcpyHostToDevice, m->st));
-    SWM_CUDA(cudaMemcpyAsync(m->d_lens, m->h_lens, n * 4, cudaMemcpyHostToDevice, m->st));
-    if (b->errors_per_read) SWM_CUDA(cudaMemcpyAsync(m->d_e, m->h_e, n, cudaMemcpyHostToDevice, m->st));
+    // page-locked caller buffers are copied directly; others go through the
+    // mapper's pinned staging so that the copy can run asynchronously
+    const void *src_reads = b->reads, *src_lens = b->reads_len, *src_e = b->errors_per_read;
+    if (!is_pinned(b->reads)) {
+        memcpy(m->h_reads, b->reads, bytes);
+        src_reads = m->h_reads;
+    }
+    if (!is_pinned(b->reads_len)) {
+        memcpy(m->h_lens, b->reads_len, n * 4);
+        src_lens = m->h_lens;
+    }
+    if (b->errors_per_read && !is_pinned(b->errors_per_read)) {
+        memcpy(m->h_e, b->errors_per_read, n);
+        src_e = m->h_e;
+    }
+    SWM_CUDA(cudaMemcpyAsync(m->d_reads, src_reads, bytes, cudaMemcpyHostToDevice, m->st));
+    SWM_CUDA(cudaMemcpyAsync(m->d_lens, src_lens, n * 4, cudaMemcpyHostToDevice, m->st));
+    if (b->errors_per_read) SWM_CUDA(cudaMemcpyAsync(m->d_e, src_e, n, cudaMemcpyHostToDevice, m->st));
     m->h2d_pending = bytes + n * 4 + (b->errors_per_read ? n : 0);
     return SWM_OK;
 }

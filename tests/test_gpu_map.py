@@ -219,3 +219,35 @@ def test_gpu_read_encoding_every_length(cuda_lib):
             want[2 * b + 1] = _even(a0 >> 1) | (_even(a1 >> 1) << 16)
         want[16:] = w[16:]
         assert np.array_equal(words[it].astype(np.uint64), want), (it, int(lens[r]))
+
+
+def test_gpu_pinned_buffers_direct_copy(cuda_lib):
+    """Page-locked caller buffers take the direct-copy path; same records."""
+    import ctypes
+    rt = None
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            rt = ctypes.CDLL(name)
+            break
+        except OSError:
+            pass
+    assert rt is not None
+    rt.cudaHostRegister.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint]
+    rt.cudaHostUnregister.argtypes = [ctypes.c_void_p]
+    g = genome(1_000_000, 23, "repeats100m")
+    reads, lens, _, _ = synth.reads(g, 3000, 150, 150, 0.03, seed=24)
+    ix = cuda_lib.Index.build(g)
+    m = cuda_lib.Mapper(ix, max_reads=3000)
+    want = m.map(reads, lens, 7).records()
+    buf = cuda_lib.PackedBuffers(3000)
+    arrs = [reads, lens, buf.words, buf.cigar, buf.rlen]
+    for a in arrs:
+        assert rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0) == 0
+    try:
+        m.submit(reads, lens, 7)
+        m.wait_packed(buf)
+        got = buf.records()
+    finally:
+        for a in arrs:
+            rt.cudaHostUnregister(a.ctypes.data)
+    assert got == want
