@@ -80,6 +80,20 @@ int swm_index_save(const swm_index *ix, const char *prefix, const char *ref_info
 
 int swm_index_get_info(const swm_index *ix, swm_index_info *info);
 
+/* No counterpart in the reference. The mapper's hash_offset (4^k + 1 start
+ * offsets, rebuilt from .hash_count as mapper_mpe.c:250-255 does) computed
+ * into device memory the caller already owns, for callers that cannot
+ * allocate device memory -- code running where allocation is forbidden or
+ * would stall, such as a serving loop inside another framework's memory pool,
+ * a stream being captured into a CUDA graph, or a host callback. The call
+ * allocates nothing: its scratch is a 128 KB static device array, so k <= 13
+ * (larger k returns SWM_ERR_ARG). The first call on a device looks up that
+ * array's address and should come before any stream capture. All calls on a
+ * device share the array: calls that overlap on the GPU (other streams,
+ * other threads) race; serialise them. stream is a cudaStream_t (NULL =
+ * default stream); the call is asynchronous on it. */
+int swm_hash_offset_noalloc(const uint32_t *d_hash_count, uint32_t *d_hash_offset, uint32_t k, void *stream);
+
 /* Copy the index arrays to host memory in file layout (any pointer may be
  * NULL). hash_offset_end gets the END offsets serial_index writes. */
 int swm_index_download(const swm_index *ix, uint32_t *hash_count, uint32_t *hash_offset_end, uint32_t *positions,

@@ -20,6 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "swm_common.cuh"
@@ -735,4 +736,59 @@ extern "C" void swm_index_free(swm_index *ix) {
     if (!ix) return;
     cudaSetDevice(ix->device);
     index_release(ix);
+}
+
+// ------------------------------------------------ allocation-free offsets
+
+// Scratch of swm_hash_offset_noalloc: the scan's block partial sums, one word
+// per 2048 counts, so 32768 words cover 4^13 buckets (k <= 13). Every device
+// that loads this library holds these 128 KB until the process exits.
+#define NOALLOC_PARTIALS 32768
+static __device__ __align__(256) uint32_t g_noalloc_partials[NOALLOC_PARTIALS + 64];
+
+#define NOALLOC_MAX_DEVICES 64
+static std::mutex g_noalloc_mu;
+static uint32_t *g_noalloc_addr[NOALLOC_MAX_DEVICES]; // device address of the array, per device
+
+// For callers that must not allocate device memory: the caller owns both
+// arrays, and the scan's partial sums go to the static array above instead of
+// a cudaMalloc'ed buffer. Its first call on a device looks up the array's
+// device address (cudaGetSymbolAddress) with that device current; make that
+// first call before any stream capture.
+extern "C" int swm_hash_offset_noalloc(const uint32_t *d_hash_count, uint32_t *d_hash_offset, uint32_t k,
+                                       void *stream) {
+    if (!d_hash_count || !d_hash_offset || k < 1 || k > 16) {
+        swm_set_error("swm_hash_offset_noalloc: null array or k out of range (k=%u)", k);
+        return SWM_ERR_ARG;
+    }
+    const uint64_t n = 1ull << (2 * k);
+    const uint64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nb > NOALLOC_PARTIALS) {
+        swm_set_error("swm_hash_offset_noalloc: k=%u needs %llu partial sums, the static scratch holds %d (k <= 13)",
+                      k, (unsigned long long)nb, NOALLOC_PARTIALS);
+        return SWM_ERR_ARG;
+    }
+    int dev = 0;
+    SWM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        swm_set_error("swm_hash_offset_noalloc: device %d beyond the %d supported", dev, NOALLOC_MAX_DEVICES);
+        return SWM_ERR_ARG;
+    }
+    uint32_t *scratch;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *addr = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_partials);
+            if (e != cudaSuccess || !addr) {
+                swm_set_error("swm_hash_offset_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+                return SWM_ERR_CUDA;
+            }
+            g_noalloc_addr[dev] = (uint32_t *)addr;
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    // every partial the scan reads is written earlier in the same call, so
+    // nothing in the scratch has to be cleared between calls
+    return swm_exclusive_scan(d_hash_count, d_hash_offset, nullptr, n, n, scratch, nullptr, (cudaStream_t)stream);
 }
