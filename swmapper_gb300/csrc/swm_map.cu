@@ -458,6 +458,342 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict
 }
 
 // ======================================================================
+// k_seed12: one thread per (read, strand), k = 12, everything in registers
+// ======================================================================
+//
+// The same outputs as k_seed, with every array indexed at compile time: the
+// read is loaded as aligned words and decoded four bases at a time; the
+// reverse strand is the bit reverse of the forward planes; the literal tail
+// replay touches at most two 2-bit words (P >= L - 11), kept in registers.
+
+#define K12 12u
+#define KL12 15u
+
+// 4 read bytes -> 4 lo bits, 4 hi bits, 4 "is A/C/G/T" bits (base j of the
+// word at bit j). Code ((c >> 1) ^ (c >> 2)) & 3 maps A C G T to 0 1 2 3;
+// anything else encodes as C (lo 1, hi 0), mapper_cpe.c:1293-1300.
+__device__ __forceinline__ void decode4(uint32_t w, uint32_t &lo, uint32_t &hi, uint32_t &ok) {
+    const uint32_t t = (w >> 1) ^ (w >> 2);
+    const uint32_t acgt = __vcmpeq4(w, 0x41414141u) | __vcmpeq4(w, 0x43434343u) | __vcmpeq4(w, 0x47474747u) |
+                          __vcmpeq4(w, 0x54545454u);
+    const uint32_t okb = acgt & 0x01010101u;
+    const uint32_t lob = (t & okb) | (~acgt & 0x01010101u);
+    const uint32_t hib = (t >> 1) & okb;
+    lo = (lob * 0x10204080u) >> 28;
+    hi = (hib * 0x10204080u) >> 28;
+    ok = (okb * 0x10204080u) >> 28;
+}
+
+__device__ __forceinline__ uint32_t spread12(uint32_t x) { return spread_bits(x & 0xfffu); }
+
+__global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, const uint32_t *__restrict__ lens,
+                                                uint64_t stride, uint32_t nreads, uint32_t e_glob,
+                                                const uint8_t *__restrict__ e_arr, const uint32_t *__restrict__ off,
+                                                MapBufs B) {
+    uint32_t *__restrict__ sel_start = B.sel_start;
+    uint32_t *__restrict__ sel_count = B.sel_count;
+    uint32_t *__restrict__ sel_meta = B.sel_meta;
+    uint32_t *__restrict__ it_w = B.it_w;
+    const uint32_t nitems = 2 * nreads;
+    const char *const limit = reads + (uint64_t)nreads * stride;
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
+        const uint32_t r = item >> 1, strand = item & 1;
+        const uint32_t L = lens[r];
+        const uint32_t e = e_arr ? e_arr[r] : e_glob;
+        if (L > SWM_MAX_READ_LEN || L > stride || e > SWM_MAX_ERRORS) {
+            atomicOr(&B.tot[TOT_FLAGS], OV_BAD);
+            B.it_nsel[item] = 0;
+            B.it_e[item] = 0;
+            B.it_nch[item] = 0;
+            B.it_nel[item] = 0;
+            B.it_nbat[item] = 0;
+            continue;
+        }
+        // ---- forward planes of the read bytes
+        uint32_t flo[8], fhi[8], fok[8];
+#pragma unroll
+        for (int b = 0; b < 8; b++) flo[b] = fhi[b] = fok[b] = 0;
+        {
+            const char *a = reads + (uint64_t)r * stride;
+            const uintptr_t ua = (uintptr_t)a;
+            const uint32_t *a0 = (const uint32_t *)(ua & ~(uintptr_t)3);
+            const uint32_t sh = (uint32_t)(ua & 3) * 8;
+            const char *end = a + L;
+            uint32_t prev = ((const char *)a0 < end) ? a0[0] : 0u;
+#pragma unroll
+            for (int j = 0; j < 64; j++) {
+                const char *nxt = (const char *)(a0 + j + 1);
+                const uint32_t cur = (nxt < end && nxt < limit) ? a0[j + 1] : 0u;
+                if (4 * j < (int)L) {
+                    const uint32_t w = sh ? __funnelshift_r(prev, cur, sh) : prev;
+                    uint32_t lo, hi, ok;
+                    decode4(w, lo, hi, ok);
+                    flo[j >> 3] |= lo << (4 * (j & 7));
+                    fhi[j >> 3] |= hi << (4 * (j & 7));
+                    fok[j >> 3] |= ok << (4 * (j & 7));
+                }
+                prev = cur;
+            }
+#pragma unroll
+            for (int b = 0; b < 8; b++) { // bases at or past L are not part of the read
+                const int rem = (int)L - 32 * b;
+                const uint32_t m = rem >= 32 ? 0xffffffffu : rem <= 0 ? 0u : ((1u << rem) - 1u);
+                flo[b] &= m;
+                fhi[b] &= m;
+                fok[b] &= m;
+            }
+        }
+        // ---- planes of the strand: reverse complement for strand 1
+        // (reverse_read, 2429-2450: A<->T, C<->G, anything else kept)
+        uint32_t plo[8], phi[8], pok[8];
+        if (strand == 0) {
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                plo[b] = flo[b];
+                phi[b] = fhi[b];
+                pok[b] = fok[b];
+            }
+        } else {
+            // base i of the strand = base L - 1 - i of the read: bit reverse the
+            // 256-bit planes, then shift right by 256 - L
+            const uint32_t sr = 256u - L, ws = sr >> 5, bs = sr & 31;
+            uint32_t rlo[9], rhi[9], rok[9];
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                rlo[b] = __brev(flo[7 - b]);
+                rhi[b] = __brev(fhi[7 - b]);
+                rok[b] = __brev(fok[7 - b]);
+            }
+            rlo[8] = rhi[8] = rok[8] = 0;
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                uint32_t l0 = 0, l1 = 0, h0 = 0, h1 = 0, o0 = 0, o1 = 0;
+#pragma unroll
+                for (int q = 0; q < 8; q++) { // select words b + ws and b + ws + 1
+                    if ((uint32_t)q == b + ws) {
+                        l0 = rlo[q];
+                        h0 = rhi[q];
+                        o0 = rok[q];
+                    }
+                    if ((uint32_t)q == b + ws + 1) {
+                        l1 = rlo[q];
+                        h1 = rhi[q];
+                        o1 = rok[q];
+                    }
+                }
+                const uint32_t lo = bs ? __funnelshift_r(l0, l1, bs) : l0;
+                const uint32_t hi = bs ? __funnelshift_r(h0, h1, bs) : h0;
+                const uint32_t ok = bs ? __funnelshift_r(o0, o1, bs) : o0;
+                plo[b] = lo ^ ok; // complement flips both bits of A/C/G/T only
+                phi[b] = hi ^ ok;
+                pok[b] = ok;
+            }
+        }
+        const uint32_t nl = L / KL12;
+        uint32_t jt = 0xffffffffu, P = nl ? nl * KL12 - 1 : 0u;
+        if (nl) {
+#pragma unroll
+            for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
+                const uint32_t rp = (nl - 1) * KL12 + sft + K12 - 1;
+                if (jt == 0xffffffffu && L - rp < K12) {
+                    jt = (nl - 1) * SWM_SEED_STEP + sft;
+                    P = rp;
+                }
+            }
+        }
+        const uint32_t vis = nl ? (jt != 0xffffffffu ? L : nl * KL12) : 0u;
+        const uint32_t span = nl * KL12;
+        bool has_n = false;
+#pragma unroll
+        for (int b = 0; b < 8; b++) { // planes hold the visited bases only; N flag over seed windows
+            const int rem = (int)vis - 32 * b;
+            const uint32_t m = rem >= 32 ? 0xffffffffu : rem <= 0 ? 0u : ((1u << rem) - 1u);
+            const int rs = (int)span - 32 * b;
+            const uint32_t ms = rs >= 32 ? 0xffffffffu : rs <= 0 ? 0u : ((1u << rs) - 1u);
+            has_n |= ((~pok[b]) & ms) != 0;
+            plo[b] &= m;
+            phi[b] &= m;
+            pok[b] |= ~m; // positions outside the visit are not N
+        }
+        // ---- long-seed planes (15 bases each) and bucket counts of every seed
+        uint32_t LR[16], HR[16], NR[16], CNT[16], IDX[16];
+#pragma unroll
+        for (int l = 0; l < 16; l++) {
+            const uint32_t o = 15u * l, wj = o >> 5, sh = o & 31;
+            const uint32_t nlo = wj + 1 < 8 ? plo[wj + 1] : 0u, nhi = wj + 1 < 8 ? phi[wj + 1] : 0u;
+            const uint32_t nok = wj + 1 < 8 ? pok[wj + 1] : 0xffffffffu;
+            LR[l] = (sh ? __funnelshift_r(plo[wj], nlo, sh) : plo[wj]) & 0x7fffu;
+            HR[l] = (sh ? __funnelshift_r(phi[wj], nhi, sh) : phi[wj]) & 0x7fffu;
+            NR[l] = ~(sh ? __funnelshift_r(pok[wj], nok, sh) : pok[wj]) & 0x7fffu;
+            IDX[l] = l;
+            CNT[l] = 0;
+        }
+        auto seed_at = [&](int l, uint32_t sft) -> uint32_t {
+            uint32_t sd = spread12(LR[l] >> sft) | (spread12(HR[l] >> sft) << 1);
+            uint32_t nm = (NR[l] >> sft) & 0xfffu;
+            while (nm) { // N bases: d % 4 inside the shift-0 window, else 3 (mapper_cpe.c:1294)
+                const uint32_t t = __ffs(nm) - 1;
+                nm &= nm - 1;
+                const uint32_t d = sft + t;
+                const uint32_t c = d < K12 ? d % 4 : (K12 - 1) % 4;
+                sd = (sd & ~(3u << (2 * t))) | (c << (2 * t));
+            }
+            return sd;
+        };
+#pragma unroll
+        for (int l = 0; l < 16; l++) {
+            if ((uint32_t)l < nl) {
+                uint32_t c = 0;
+#pragma unroll
+                for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
+                    const uint32_t sd = seed_at(l, sft);
+                    c += off[sd + 1] - off[sd];
+                }
+                CNT[l] = c;
+            }
+        }
+        // exchange sort (1391-1399), unrolled
+#pragma unroll
+        for (int a = 0; a < 16; a++) {
+#pragma unroll
+            for (int m2 = a + 1; m2 < 16; m2++) {
+                if ((uint32_t)m2 < nl && CNT[a] > CNT[m2]) {
+                    const uint32_t tc = CNT[a];
+                    CNT[a] = CNT[m2];
+                    CNT[m2] = tc;
+                    const uint32_t ti = IDX[a];
+                    IDX[a] = IDX[m2];
+                    IDX[m2] = ti;
+                }
+            }
+        }
+        const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
+        const uint32_t ns = nsl * SWM_SEED_STEP;
+        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+        uint32_t nref = 0, nel = 0;
+        const uint32_t rmask = (1u << (SWM_SEED_STEP - 1)) - 1;
+#pragma unroll
+        for (int l = 0; l < 16; l++) {
+            uint32_t rank = 0xffffffffu;
+#pragma unroll
+            for (int a = 0; a < 16; a++)
+                if (IDX[a] == (uint32_t)l) rank = a;
+            if ((uint32_t)l < nl && rank < nsl) {
+#pragma unroll
+                for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
+                    const uint32_t sd = seed_at(l, sft);
+                    const uint32_t o0 = off[sd], c = off[sd + 1] - o0;
+                    const uint32_t m = (1u << sft) - 1, kk = K12 + sft;
+                    const uint32_t rl = ((LR[l] & m) | ((LR[l] >> kk) << sft)) & rmask;
+                    const uint32_t rh = ((HR[l] & m) | ((HR[l] >> kk) << sft)) & rmask;
+                    const uint32_t i = rank * SWM_SEED_STEP + sft;
+                    sel_start[sb + i] = o0;
+                    sel_count[sb + i] = c;
+                    sel_meta[sb + i] = (15u * l + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) | (rh << 24);
+                    nref += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
+                    nel += c;
+                }
+            }
+        }
+        // ---- Myers planes: complete 2-bit words up to P are the planes, the
+        // partial word is unwritten; the tail replay rewrites words P/16 and
+        // P/16 + 1 (the only ones it can touch)
+        uint32_t mlo[8], mhi[8];
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            uint32_t m = 0;
+            if (nl) {
+                if (32 * b + 15 <= (int)P) m |= 0x0000ffffu;
+                if (32 * b + 31 <= (int)P) m |= 0xffff0000u;
+            }
+            mlo[b] = plo[b] & m;
+            mhi[b] = phi[b] & m;
+        }
+        if (jt != 0xffffffffu) {
+            const uint32_t w0 = P >> 4;
+            uint32_t wa = 0, wb = 0; // 2-bit words w0 and w0 + 1
+            // the planes of bases 16 w0 .. 16 w0 + 31 (they cover L - 1)
+            uint32_t pl0 = 0, pl1 = 0, ph0 = 0, ph1 = 0;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                if ((uint32_t)q == (w0 >> 1)) {
+                    pl0 = plo[q];
+                    ph0 = phi[q];
+                }
+                if ((uint32_t)q == (w0 >> 1) + 1) {
+                    pl1 = plo[q];
+                    ph1 = phi[q];
+                }
+            }
+            const uint32_t base0 = 16 * w0, sh0 = (w0 & 1) * 16;
+            const uint32_t lwin = __funnelshift_r(pl0, pl1, sh0), hwin = __funnelshift_r(ph0, ph1, sh0);
+            auto code_at = [&](uint32_t q) -> uint32_t { // base q in [16 w0, 16 w0 + 31]
+                const uint32_t t = q - base0;
+                return ((lwin >> t) & 1u) | (((hwin >> t) & 1u) << 1);
+            };
+            auto put = [&](uint32_t q, uint32_t v) {
+                if ((q >> 4) == w0) wa = v;
+                else wb = v;
+            };
+            if (P % 16 == 15) {
+                wa = spread_bits(lwin & 0xffffu) | (spread_bits(hwin & 0xffffu) << 1);
+            }
+            uint32_t acc = 0;
+            if (P % 16 != 15)
+                for (uint32_t q = base0; q <= P; q++) acc |= code_at(q) << ((q % 16) * 2);
+            for (uint32_t j = jt; j < nl * SWM_SEED_STEP; j++) {
+                const uint32_t rp = (j / SWM_SEED_STEP) * KL12 + j % SWM_SEED_STEP + K12 - 1;
+                if (j > jt) { // the one base this call's main loop adds
+                    acc |= code_at(rp) << ((rp % 16) * 2);
+                    if (rp % 16 == 15) {
+                        put(rp, acc);
+                        acc = 0;
+                    }
+                }
+                for (uint32_t q = rp; q < L; q++) { // tail encoder, re-run from rp
+                    acc |= code_at(q) << ((q % 16) * 2);
+                    if (q % 16 == 15) {
+                        put(q, acc);
+                        acc = 0;
+                    }
+                }
+                put(L - 1, acc);
+            }
+            // write words w0 and w0 + 1 back into the Myers planes
+            const uint32_t lo_a = even_bits(wa), hi_a = even_bits(wa >> 1);
+            const uint32_t lo_b = even_bits(wb), hi_b = even_bits(wb >> 1);
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+#pragma unroll
+                for (int hf = 0; hf < 2; hf++) {
+                    const uint32_t q = 2 * b + hf;
+                    if (q == w0 || q == w0 + 1) {
+                        const uint32_t lo = (q == w0) ? lo_a : lo_b, hi = (q == w0) ? hi_a : hi_b;
+                        const uint32_t m = hf ? 0xffff0000u : 0x0000ffffu;
+                        mlo[b] = (mlo[b] & ~m) | ((hf ? (lo << 16) : lo) & m);
+                        mhi[b] = (mhi[b] & ~m) | ((hf ? (hi << 16) : hi) & m);
+                    }
+                }
+            }
+        }
+        uint4 *ow = reinterpret_cast<uint4 *>(it_w + (uint64_t)item * 32);
+        ow[0] = make_uint4(mlo[0], mhi[0], mlo[1], mhi[1]);
+        ow[1] = make_uint4(mlo[2], mhi[2], mlo[3], mhi[3]);
+        ow[2] = make_uint4(mlo[4], mhi[4], mlo[5], mhi[5]);
+        ow[3] = make_uint4(mlo[6], mhi[6], mlo[7], mhi[7]);
+        ow[4] = make_uint4(plo[0], phi[0], plo[1], phi[1]);
+        ow[5] = make_uint4(plo[2], phi[2], plo[3], phi[3]);
+        ow[6] = make_uint4(plo[4], phi[4], plo[5], phi[5]);
+        ow[7] = make_uint4(plo[6], phi[6], plo[7], phi[7]);
+        B.it_nsel[item] = (uint8_t)ns;
+        B.it_e[item] = (uint8_t)e;
+        B.it_nch[item] = nref;
+        B.it_nel[item] = nel;
+        B.it_nbat[item] = (nref == 0 && nel > 0) ? 1u : 0u;
+    }
+}
+
+// ======================================================================
 // k_plan: the refill schedule of alignment_rmdup, one thread per item whose
 // buckets need refills (some selected seed has more than 32 positions)
 // ======================================================================
@@ -1624,8 +1960,11 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     SWM_CUDA(cudaMemsetAsync(B.tot, 0, TOT_N * 4, st));
     SWM_CUDA(cudaMemsetAsync(B.stat, 0, ST_N * 8, st));
     SWM_CUDA(cudaEventRecord(m->ev[0], st));
-    k_seed<<<grid_cap((uint64_t)nitems, SEED_WARPS * 32, 8), SEED_WARPS * 32, 0, st>>>(
-        d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, ix->k, B);
+    if (ix->k == K12)
+        k_seed12<<<grid_cap(nitems, 128, 16), 128, 0, st>>>(d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, B);
+    else
+        k_seed<<<grid_cap((uint64_t)nitems, SEED_WARPS * 32, 8), SEED_WARPS * 32, 0, st>>>(
+            d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, ix->k, B);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[1], st));
