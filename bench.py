@@ -100,6 +100,20 @@ class Dist:
             self.dist.destroy_process_group()
 
 
+def aggregate(dist, elapsed, counts):
+    """Whole-job view of one timed region: the slowest rank's time and the sum of
+    each per-rank count over all ranks."""
+    t, = dist.reduce([float(elapsed)], "max")
+    sums = dist.reduce([float(c) for c in counts], "sum")
+    return (t, *sums)
+
+
+def shard_seed(rank):
+    """Read seed of a rank's shard: every rank maps its own reads against a full
+    index replica (reads are independent; nothing is exchanged)."""
+    return WORKLOAD["read_seed"] + 1000 * rank
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
 
@@ -171,7 +185,7 @@ def make_workload(rank=0):
     w = WORKLOAD
     g = synth.reference(w["genome_bp"], seed=w["genome_seed"], kind=w["genome_kind"])
     reads, lens, _, _ = synth.reads(g, w["reads"], w["read_len"], w["read_len"], w["error_rate"],
-                                    seed=w["read_seed"] + 1000 * rank)
+                                    seed=shard_seed(rank))
     return g, reads, lens
 
 
@@ -310,8 +324,7 @@ def run_gpu(args):
     rt.cudaEventElapsedTime(C.byref(ms), ev0, ev1)
     clk = clocks.stop()
     elapsed = ms.value / 1000.0
-    tot_elapsed, = dist.reduce([elapsed], "max")
-    tot_mapped, tot_cells = dist.reduce([float(acc["mapped_reads"]), float(acc["cells"])], "sum")
+    tot_elapsed, tot_mapped, tot_cells = aggregate(dist, elapsed, [acc["mapped_reads"], acc["cells"]])
     value = tot_mapped / tot_elapsed
     gcups = tot_cells / tot_elapsed / 1e9
 
@@ -353,8 +366,7 @@ def run_gpu(args):
     for _ in range(e2e_steps):
         e2e_step(acc2)
     e2e_t = time.perf_counter() - t0
-    e2e_t, = dist.reduce([e2e_t], "max")
-    e2e_mapped, = dist.reduce([float(acc2["mapped"])], "sum")
+    e2e_t, e2e_mapped = aggregate(dist, e2e_t, [acc2["mapped"]])
     rt.cudaHostUnregister.argtypes = [C.c_void_p]
     for a in pinned:
         rt.cudaHostUnregister(a.ctypes.data)
