@@ -54,9 +54,7 @@ enum { TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT
 struct MapBufs {
     // per item
     uint32_t *it_w;        // items * 32: [0..15] Myers planes, [16..31] Hamming planes
-    uint32_t *sel_start;   // items * 64
-    uint32_t *sel_count;   // items * 64
-    uint32_t *sel_meta;    // items * 64: base | shift << 16 | rl << 20 | rh << 24
+    uint4 *sel;            // items * 64: (bucket start, count, base | shift << 16 | rl << 20 | rh << 24, 0)
     uint8_t *it_nsel, *it_e;
     uint32_t *it_nch, *it_nel, *it_nbat;
     uint32_t *it_choff, *it_eloff; // items + 1
@@ -238,9 +236,7 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict
     __shared__ SeedSmem sm_all[SEED_WARPS];
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     SeedSmem &S = sm_all[wib];
-    uint32_t *__restrict__ sel_start = B.sel_start;
-    uint32_t *__restrict__ sel_count = B.sel_count;
-    uint32_t *__restrict__ sel_meta = B.sel_meta;
+    uint4 *__restrict__ sel = B.sel;
     const uint32_t nitems = 2 * nreads;
     const uint32_t klong = k + SWM_SEED_STEP - 1;
     const uint32_t kmask = (1u << k) - 1, lmask = (1u << klong) - 1, rmask = (1u << (SWM_SEED_STEP - 1)) - 1;
@@ -424,9 +420,8 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict
                     const uint32_t m = (1u << sft) - 1, kk = k + sft;
                     const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & rmask; // 2483-2495
                     const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & rmask;
-                    sel_start[sb + i] = o0;
-                    sel_count[sb + i] = c;
-                    sel_meta[sb + i] = (o + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) | (rh << 24);
+                    sel[sb + i] = make_uint4(o0, c, (o + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) |
+                                                          (rh << 24), 0u);
                     nref += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
                     nel += c;
                 }
@@ -458,16 +453,21 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict
 }
 
 // ======================================================================
-// k_seed12: one thread per (read, strand), k = 12, everything in registers
+// k_seed12: one thread per (read, strand), k = 12
 // ======================================================================
 //
-// The same outputs as k_seed, with every array indexed at compile time: the
-// read is loaded as aligned words and decoded four bases at a time; the
-// reverse strand is the bit reverse of the forward planes; the literal tail
-// replay touches at most two 2-bit words (P >= L - 11), kept in registers.
+// The same outputs as k_seed with every register array indexed at compile
+// time. The two threads of a read (strands 0 and 1 are adjacent lanes) decode
+// alternate words of it and exchange the halves; the reverse strand is the
+// bit reverse of the forward planes. Seed codes come from interleaved 2-bit
+// words of the strand (one funnel shift per seed), so every bucket lookup of
+// a read issues back to back; the (start, count) pairs wait in shared memory
+// for the selection. The literal tail replay touches at most two 2-bit words
+// (P >= L - 11), kept in registers.
 
 #define K12 12u
 #define KL12 15u
+#define SEED12_THREADS 64
 
 // 4 read bytes -> 4 lo bits, 4 hi bits, 4 "is A/C/G/T" bits (base j of the
 // word at bit j). Code ((c >> 1) ^ (c >> 2)) & 3 maps A C G T to 0 1 2 3;
@@ -484,23 +484,84 @@ __device__ __forceinline__ void decode4(uint32_t w, uint32_t &lo, uint32_t &hi, 
     ok = (okb * 0x10204080u) >> 28;
 }
 
-__device__ __forceinline__ uint32_t spread12(uint32_t x) { return spread_bits(x & 0xfffu); }
+// 2-bit codes an N takes at each position of the seed at shift sft: d % 4
+// for d = sft + t inside the first k bases, (k - 1) % 4 past them
+// (mapper_cpe.c:1294).
+__host__ __device__ constexpr uint32_t nfill12(uint32_t sft) {
+    uint32_t w = 0;
+    for (uint32_t t = 0; t < K12; t++) {
+        const uint32_t d = sft + t;
+        w |= (d < K12 ? d % 4u : (K12 - 1u) % 4u) << (2u * t);
+    }
+    return w;
+}
 
-__global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, const uint32_t *__restrict__ lens,
-                                                uint64_t stride, uint32_t nreads, uint32_t e_glob,
-                                                const uint8_t *__restrict__ e_arr, const uint32_t *__restrict__ off,
-                                                MapBufs B) {
-    uint32_t *__restrict__ sel_start = B.sel_start;
-    uint32_t *__restrict__ sel_count = B.sel_count;
-    uint32_t *__restrict__ sel_meta = B.sel_meta;
+// L2-resident loads of the bucket offsets (hint: keep them over streamed data)
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ uint32_t ld_keep(const uint32_t *p, uint64_t pol) {
+    uint32_t v;
+    asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+// Bucket (start, count) of every seed of long seeds 0 .. NL-1 into shared
+// memory, slot 4 l + sft; returns the per-long-seed sums in cnt.
+template <int NL, bool HASN>
+__device__ __forceinline__ void seed12_lookup(const uint32_t (&iw)[NL], const uint32_t (&pok)[8], uint32_t nl,
+                                              const uint32_t *__restrict__ off, uint64_t pol, uint2 *oc,
+                                              uint32_t (&cnt)[NL]) {
+    const uint32_t tid = threadIdx.x;
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+        uint32_t csum = 0;
+#pragma unroll
+        for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
+            const uint32_t o = KL12 * l + sft, w = o >> 4, sh = 2 * (o & 15);
+            const uint32_t hi = (w + 1 < (uint32_t)NL) ? iw[w + 1] : 0u;
+            uint32_t sd = (sh ? __funnelshift_r(iw[w], hi, sh) : iw[w]) & 0xffffffu;
+            if (HASN) {
+                const uint32_t wj = o >> 5, s5 = o & 31;
+                const uint32_t nx = wj + 1 < 8 ? pok[wj + 1] : 0xffffffffu;
+                const uint32_t nm = ~(s5 ? __funnelshift_r(pok[wj], nx, s5) : pok[wj]) & 0xfffu;
+                const uint32_t M = spread_bits(nm) * 3u;
+                sd = (sd & ~M) | (nfill12(sft) & M);
+            }
+            sd = ((uint32_t)l < nl) ? sd : 0u;
+            const uint32_t o0 = ld_keep(off + sd, pol), o1 = ld_keep(off + sd + 1, pol);
+            const uint32_t c = o1 - o0;
+            oc[(4 * l + sft) * SEED12_THREADS + tid] = make_uint2(o0, c);
+            csum += c;
+        }
+        cnt[l] = ((uint32_t)l < nl) ? csum : 0u;
+    }
+}
+
+template <int NL>
+__global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const char *__restrict__ reads,
+                                                           const uint32_t *__restrict__ lens, uint64_t stride,
+                                                           uint32_t nreads, uint32_t e_glob,
+                                                           const uint8_t *__restrict__ e_arr,
+                                                           const uint32_t *__restrict__ off, MapBufs B) {
+    extern __shared__ uint2 s12[];
+    uint2 *oc = s12;                                                          // [4 NL][threads]
+    uint32_t *fl = reinterpret_cast<uint32_t *>(s12 + 4 * NL * SEED12_THREADS); // [NL][threads]
+    uint4 *__restrict__ sel = B.sel;
     uint32_t *__restrict__ it_w = B.it_w;
+    const uint32_t tid = threadIdx.x;
     const uint32_t nitems = 2 * nreads;
     const char *const limit = reads + (uint64_t)nreads * stride;
-    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
+    const uint64_t pol = l2_keep_policy();
+    for (uint32_t item = blockIdx.x * blockDim.x + tid; item < nitems; item += gridDim.x * blockDim.x) {
+        // items 2r and 2r + 1 sit in adjacent lanes (even block size and stride)
+        const uint32_t pair = 3u << (lane_id() & ~1u);
         const uint32_t r = item >> 1, strand = item & 1;
         const uint32_t L = lens[r];
         const uint32_t e = e_arr ? e_arr[r] : e_glob;
-        if (L > SWM_MAX_READ_LEN || L > stride || e > SWM_MAX_ERRORS) {
+        if (L > SWM_MAX_READ_LEN || L > stride || e > SWM_MAX_ERRORS || L > NL * KL12 + KL12 - 1) {
             atomicOr(&B.tot[TOT_FLAGS], OV_BAD);
             B.it_nsel[item] = 0;
             B.it_e[item] = 0;
@@ -509,7 +570,8 @@ __global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, 
             B.it_nbat[item] = 0;
             continue;
         }
-        // ---- forward planes of the read bytes
+        // ---- forward planes of the read bytes: this lane decodes words
+        // 2 jj + strand, the other lane of the pair the rest
         uint32_t flo[8], fhi[8], fok[8];
 #pragma unroll
         for (int b = 0; b < 8; b++) flo[b] = fhi[b] = fok[b] = 0;
@@ -519,23 +581,31 @@ __global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, 
             const uint32_t *a0 = (const uint32_t *)(ua & ~(uintptr_t)3);
             const uint32_t sh = (uint32_t)(ua & 3) * 8;
             const char *end = a + L;
-            uint32_t prev = ((const char *)a0 < end) ? a0[0] : 0u;
 #pragma unroll
-            for (int j = 0; j < 64; j++) {
-                const char *nxt = (const char *)(a0 + j + 1);
-                const uint32_t cur = (nxt < end && nxt < limit) ? a0[j + 1] : 0u;
-                if (4 * j < (int)L) {
-                    const uint32_t w = sh ? __funnelshift_r(prev, cur, sh) : prev;
-                    uint32_t lo, hi, ok;
-                    decode4(w, lo, hi, ok);
-                    flo[j >> 3] |= lo << (4 * (j & 7));
-                    fhi[j >> 3] |= hi << (4 * (j & 7));
-                    fok[j >> 3] |= ok << (4 * (j & 7));
+            for (int b = 0; b < 8; b++) {
+                if (32 * b < (int)L) {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const uint32_t j = 8 * b + 2 * q + strand; // word j: bytes 4j .. 4j + 3 of the read
+                        const char *p0 = (const char *)(a0 + j), *p1 = (const char *)(a0 + j + 1);
+                        const uint32_t w0 = (p0 < end && p0 < limit) ? __ldcs(a0 + j) : 0u;
+                        const uint32_t w1 = (p1 < end && p1 < limit) ? __ldcs(a0 + j + 1) : 0u;
+                        const uint32_t w = sh ? __funnelshift_r(w0, w1, sh) : w0;
+                        uint32_t lo, hi, ok;
+                        decode4(w, lo, hi, ok);
+                        const uint32_t s = 4 * (2 * q + strand);
+                        flo[b] |= lo << s;
+                        fhi[b] |= hi << s;
+                        fok[b] |= ok << s;
+                    }
                 }
-                prev = cur;
             }
 #pragma unroll
-            for (int b = 0; b < 8; b++) { // bases at or past L are not part of the read
+            for (int b = 0; b < 8; b++) {
+                flo[b] |= __shfl_xor_sync(pair, flo[b], 1);
+                fhi[b] |= __shfl_xor_sync(pair, fhi[b], 1);
+                fok[b] |= __shfl_xor_sync(pair, fok[b], 1);
+                // bases at or past L are not part of the read
                 const int rem = (int)L - 32 * b;
                 const uint32_t m = rem >= 32 ? 0xffffffffu : rem <= 0 ? 0u : ((1u << rem) - 1u);
                 flo[b] &= m;
@@ -555,35 +625,36 @@ __global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, 
             }
         } else {
             // base i of the strand = base L - 1 - i of the read: bit reverse the
-            // 256-bit planes, then shift right by 256 - L
+            // 256-bit planes, then shift right by 256 - L (word steps of 4, 2,
+            // 1 words as selects, then a funnel shift)
             const uint32_t sr = 256u - L, ws = sr >> 5, bs = sr & 31;
-            uint32_t rlo[9], rhi[9], rok[9];
 #pragma unroll
             for (int b = 0; b < 8; b++) {
-                rlo[b] = __brev(flo[7 - b]);
-                rhi[b] = __brev(fhi[7 - b]);
-                rok[b] = __brev(fok[7 - b]);
+                plo[b] = __brev(flo[7 - b]);
+                phi[b] = __brev(fhi[7 - b]);
+                pok[b] = __brev(fok[7 - b]);
             }
-            rlo[8] = rhi[8] = rok[8] = 0;
+#pragma unroll
+            for (int step = 4; step >= 1; step >>= 1) {
+                const bool mv = (ws & step) != 0;
+#pragma unroll
+                for (int b = 0; b < 8; b++) {
+                    const uint32_t nlo = b + step < 8 ? plo[b + step] : 0u;
+                    const uint32_t nhi = b + step < 8 ? phi[b + step] : 0u;
+                    const uint32_t nok = b + step < 8 ? pok[b + step] : 0u;
+                    plo[b] = mv ? nlo : plo[b];
+                    phi[b] = mv ? nhi : phi[b];
+                    pok[b] = mv ? nok : pok[b];
+                }
+            }
 #pragma unroll
             for (int b = 0; b < 8; b++) {
-                uint32_t l0 = 0, l1 = 0, h0 = 0, h1 = 0, o0 = 0, o1 = 0;
-#pragma unroll
-                for (int q = 0; q < 8; q++) { // select words b + ws and b + ws + 1
-                    if ((uint32_t)q == b + ws) {
-                        l0 = rlo[q];
-                        h0 = rhi[q];
-                        o0 = rok[q];
-                    }
-                    if ((uint32_t)q == b + ws + 1) {
-                        l1 = rlo[q];
-                        h1 = rhi[q];
-                        o1 = rok[q];
-                    }
-                }
-                const uint32_t lo = bs ? __funnelshift_r(l0, l1, bs) : l0;
-                const uint32_t hi = bs ? __funnelshift_r(h0, h1, bs) : h0;
-                const uint32_t ok = bs ? __funnelshift_r(o0, o1, bs) : o0;
+                const uint32_t nlo = b + 1 < 8 ? plo[b + 1] : 0u;
+                const uint32_t nhi = b + 1 < 8 ? phi[b + 1] : 0u;
+                const uint32_t nok = b + 1 < 8 ? pok[b + 1] : 0u;
+                const uint32_t lo = bs ? __funnelshift_r(plo[b], nlo, bs) : plo[b];
+                const uint32_t hi = bs ? __funnelshift_r(phi[b], nhi, bs) : phi[b];
+                const uint32_t ok = bs ? __funnelshift_r(pok[b], nok, bs) : pok[b];
                 plo[b] = lo ^ ok; // complement flips both bits of A/C/G/T only
                 phi[b] = hi ^ ok;
                 pok[b] = ok;
@@ -615,85 +686,30 @@ __global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, 
             phi[b] &= m;
             pok[b] |= ~m; // positions outside the visit are not N
         }
-        // ---- long-seed planes (15 bases each) and bucket counts of every seed
-        uint32_t LR[16], HR[16], NR[16], CNT[16], IDX[16];
+        // ---- interleaved 2-bit words of the strand (base 16 w + i at bits
+        // 2i, 2i + 1) and the flank bits of every long seed
+        uint32_t iw[NL];
 #pragma unroll
-        for (int l = 0; l < 16; l++) {
-            const uint32_t o = 15u * l, wj = o >> 5, sh = o & 31;
+        for (int w = 0; w < NL; w++) {
+            const uint32_t l16 = (w & 1) ? (plo[w >> 1] >> 16) : plo[w >> 1];
+            const uint32_t h16 = (w & 1) ? (phi[w >> 1] >> 16) : phi[w >> 1];
+            iw[w] = spread_bits(l16) | (spread_bits(h16) << 1);
+        }
+#pragma unroll
+        for (int l = 0; l < NL; l++) {
+            const uint32_t o = KL12 * l, wj = o >> 5, sh = o & 31;
             const uint32_t nlo = wj + 1 < 8 ? plo[wj + 1] : 0u, nhi = wj + 1 < 8 ? phi[wj + 1] : 0u;
-            const uint32_t nok = wj + 1 < 8 ? pok[wj + 1] : 0xffffffffu;
-            LR[l] = (sh ? __funnelshift_r(plo[wj], nlo, sh) : plo[wj]) & 0x7fffu;
-            HR[l] = (sh ? __funnelshift_r(phi[wj], nhi, sh) : phi[wj]) & 0x7fffu;
-            NR[l] = ~(sh ? __funnelshift_r(pok[wj], nok, sh) : pok[wj]) & 0x7fffu;
-            IDX[l] = l;
-            CNT[l] = 0;
-        }
-        auto seed_at = [&](int l, uint32_t sft) -> uint32_t {
-            uint32_t sd = spread12(LR[l] >> sft) | (spread12(HR[l] >> sft) << 1);
-            uint32_t nm = (NR[l] >> sft) & 0xfffu;
-            while (nm) { // N bases: d % 4 inside the shift-0 window, else 3 (mapper_cpe.c:1294)
-                const uint32_t t = __ffs(nm) - 1;
-                nm &= nm - 1;
-                const uint32_t d = sft + t;
-                const uint32_t c = d < K12 ? d % 4 : (K12 - 1) % 4;
-                sd = (sd & ~(3u << (2 * t))) | (c << (2 * t));
+            const uint32_t lr = (sh ? __funnelshift_r(plo[wj], nlo, sh) : plo[wj]) & 0x7fffu;
+            const uint32_t hr = (sh ? __funnelshift_r(phi[wj], nhi, sh) : phi[wj]) & 0x7fffu;
+            uint32_t f = 0;
+#pragma unroll
+            for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) { // the 3 bases around the 12-mer
+                const uint32_t m = (1u << sft) - 1, kk = K12 + sft;
+                const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & 7u;
+                const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & 7u;
+                f |= (rl | (rh << 3)) << (6 * sft);
             }
-            return sd;
-        };
-#pragma unroll
-        for (int l = 0; l < 16; l++) {
-            if ((uint32_t)l < nl) {
-                uint32_t c = 0;
-#pragma unroll
-                for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
-                    const uint32_t sd = seed_at(l, sft);
-                    c += off[sd + 1] - off[sd];
-                }
-                CNT[l] = c;
-            }
-        }
-        // exchange sort (1391-1399), unrolled
-#pragma unroll
-        for (int a = 0; a < 16; a++) {
-#pragma unroll
-            for (int m2 = a + 1; m2 < 16; m2++) {
-                if ((uint32_t)m2 < nl && CNT[a] > CNT[m2]) {
-                    const uint32_t tc = CNT[a];
-                    CNT[a] = CNT[m2];
-                    CNT[m2] = tc;
-                    const uint32_t ti = IDX[a];
-                    IDX[a] = IDX[m2];
-                    IDX[m2] = ti;
-                }
-            }
-        }
-        const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
-        const uint32_t ns = nsl * SWM_SEED_STEP;
-        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
-        uint32_t nref = 0, nel = 0;
-        const uint32_t rmask = (1u << (SWM_SEED_STEP - 1)) - 1;
-#pragma unroll
-        for (int l = 0; l < 16; l++) {
-            uint32_t rank = 0xffffffffu;
-#pragma unroll
-            for (int a = 0; a < 16; a++)
-                if (IDX[a] == (uint32_t)l) rank = a;
-            if ((uint32_t)l < nl && rank < nsl) {
-#pragma unroll
-                for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
-                    const uint32_t sd = seed_at(l, sft);
-                    const uint32_t o0 = off[sd], c = off[sd + 1] - o0;
-                    const uint32_t m = (1u << sft) - 1, kk = K12 + sft;
-                    const uint32_t rl = ((LR[l] & m) | ((LR[l] >> kk) << sft)) & rmask;
-                    const uint32_t rh = ((HR[l] & m) | ((HR[l] >> kk) << sft)) & rmask;
-                    const uint32_t i = rank * SWM_SEED_STEP + sft;
-                    sel_start[sb + i] = o0;
-                    sel_count[sb + i] = c;
-                    sel_meta[sb + i] = (15u * l + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) | (rh << 24);
-                    nref += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
-                    nel += c;
-                }
-            }
+            fl[l * SEED12_THREADS + tid] = f;
         }
         // ---- Myers planes: complete 2-bit words up to P are the planes, the
         // partial word is unwritten; the tail replay rewrites words P/16 and
@@ -715,15 +731,13 @@ __global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, 
             // the planes of bases 16 w0 .. 16 w0 + 31 (they cover L - 1)
             uint32_t pl0 = 0, pl1 = 0, ph0 = 0, ph1 = 0;
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                if ((uint32_t)q == (w0 >> 1)) {
-                    pl0 = plo[q];
-                    ph0 = phi[q];
-                }
-                if ((uint32_t)q == (w0 >> 1) + 1) {
-                    pl1 = plo[q];
-                    ph1 = phi[q];
-                }
+            for (int q = 0; q < 8; q++) { // masks, not indexing by w0
+                const uint32_t m0 = ((uint32_t)q == (w0 >> 1)) ? 0xffffffffu : 0u;
+                const uint32_t m1 = ((uint32_t)q == (w0 >> 1) + 1) ? 0xffffffffu : 0u;
+                pl0 |= plo[q] & m0;
+                ph0 |= phi[q] & m0;
+                pl1 |= plo[q] & m1;
+                ph1 |= phi[q] & m1;
             }
             const uint32_t base0 = 16 * w0, sh0 = (w0 & 1) * 16;
             const uint32_t lwin = __funnelshift_r(pl0, pl1, sh0), hwin = __funnelshift_r(ph0, ph1, sh0);
@@ -763,17 +777,14 @@ __global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, 
             const uint32_t lo_a = even_bits(wa), hi_a = even_bits(wa >> 1);
             const uint32_t lo_b = even_bits(wb), hi_b = even_bits(wb >> 1);
 #pragma unroll
-            for (int b = 0; b < 8; b++) {
-#pragma unroll
-                for (int hf = 0; hf < 2; hf++) {
-                    const uint32_t q = 2 * b + hf;
-                    if (q == w0 || q == w0 + 1) {
-                        const uint32_t lo = (q == w0) ? lo_a : lo_b, hi = (q == w0) ? hi_a : hi_b;
-                        const uint32_t m = hf ? 0xffff0000u : 0x0000ffffu;
-                        mlo[b] = (mlo[b] & ~m) | ((hf ? (lo << 16) : lo) & m);
-                        mhi[b] = (mhi[b] & ~m) | ((hf ? (hi << 16) : hi) & m);
-                    }
-                }
+            for (int b = 0; b < 8; b++) { // blend, no indexing by w0
+                const uint32_t q0 = 2 * b, q1 = 2 * b + 1;
+                const uint32_t ma = ((q0 == w0) ? 0x0000ffffu : 0u) | ((q1 == w0) ? 0xffff0000u : 0u);
+                const uint32_t mb = ((q0 == w0 + 1) ? 0x0000ffffu : 0u) | ((q1 == w0 + 1) ? 0xffff0000u : 0u);
+                const uint32_t la = lo_a | (lo_a << 16), ha = hi_a | (hi_a << 16);
+                const uint32_t lb = lo_b | (lo_b << 16), hb = hi_b | (hi_b << 16);
+                mlo[b] = (mlo[b] & ~(ma | mb)) | (la & ma) | (lb & mb);
+                mhi[b] = (mhi[b] & ~(ma | mb)) | (ha & ma) | (hb & mb);
             }
         }
         uint4 *ow = reinterpret_cast<uint4 *>(it_w + (uint64_t)item * 32);
@@ -785,6 +796,47 @@ __global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, 
         ow[5] = make_uint4(plo[2], phi[2], plo[3], phi[3]);
         ow[6] = make_uint4(plo[4], phi[4], plo[5], phi[5]);
         ow[7] = make_uint4(plo[6], phi[6], plo[7], phi[7]);
+        // ---- bucket counts of every seed, all lookups in flight together
+        uint32_t CNT[NL], IDX[NL];
+        if (has_n) seed12_lookup<NL, true>(iw, pok, nl, off, pol, oc, CNT);
+        else seed12_lookup<NL, false>(iw, pok, nl, off, pol, oc, CNT);
+#pragma unroll
+        for (int l = 0; l < NL; l++) IDX[l] = l;
+        // exchange sort (1391-1399), unrolled
+#pragma unroll
+        for (int a = 0; a < NL; a++) {
+#pragma unroll
+            for (int m2 = a + 1; m2 < NL; m2++) {
+                const bool sw = ((uint32_t)m2 < nl) & (CNT[a] > CNT[m2]);
+                const uint32_t ca = CNT[a], cm = CNT[m2], ia = IDX[a], im = IDX[m2];
+                CNT[a] = sw ? cm : ca;
+                CNT[m2] = sw ? ca : cm;
+                IDX[a] = sw ? im : ia;
+                IDX[m2] = sw ? ia : im;
+            }
+        }
+        // ---- the (e + 1) rarest long seeds x 4 shifts, rank by rank
+        // (alignment_rmdup 2194-2196)
+        const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
+        const uint32_t ns = nsl * SWM_SEED_STEP;
+        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+        uint32_t nref = 0, nel = 0;
+#pragma unroll
+        for (int a = 0; a < NL; a++) {
+            if ((uint32_t)a < nsl) {
+                const uint32_t l = IDX[a];
+                const uint32_t f = fl[l * SEED12_THREADS + tid];
+#pragma unroll
+                for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
+                    const uint2 v = oc[(4 * l + sft) * SEED12_THREADS + tid];
+                    const uint32_t rl = (f >> (6 * sft)) & 7u, rh = (f >> (6 * sft + 3)) & 7u;
+                    const uint32_t meta = (KL12 * l + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) | (rh << 24);
+                    sel[sb + a * SWM_SEED_STEP + sft] = make_uint4(v.x, v.y, meta, 0u);
+                    nref += v.y > SWM_PER_FETCH ? (v.y - 1) / SWM_PER_FETCH : 0u;
+                    nel += v.y;
+                }
+            }
+        }
         B.it_nsel[item] = (uint8_t)ns;
         B.it_e[item] = (uint8_t)e;
         B.it_nch[item] = nref;
@@ -792,6 +844,8 @@ __global__ void __launch_bounds__(128) k_seed12(const char *__restrict__ reads, 
         B.it_nbat[item] = (nref == 0 && nel > 0) ? 1u : 0u;
     }
 }
+
+static size_t seed12_smem(int nl) { return (size_t)nl * SEED12_THREADS * (4 * sizeof(uint2) + sizeof(uint32_t)); }
 
 // ======================================================================
 // k_plan: the refill schedule of alignment_rmdup, one thread per item whose
@@ -821,8 +875,9 @@ __global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const unsigned lo
         uint32_t hloc[SWM_MAX_SEL + 8], hidx[SWM_MAX_SEL + 8];
         uint32_t hs = 0, rc = 0, e = 0, b = 0, br0 = 0, be0 = 0, npos = 0, runs = 0;
         for (uint32_t i = 0; i < ns; i++) { // initial fetch of <= 32 per seed, 2194-2236
-            sst[i] = B.sel_start[sb + i];
-            scn[i] = B.sel_count[sb + i];
+            const uint4 sv = B.sel[sb + i];
+            sst[i] = sv.x;
+            scn[i] = sv.y;
             const uint32_t get = scn[i] > SWM_PER_FETCH ? SWM_PER_FETCH : scn[i];
             pc[i] = get;
             e += get;
@@ -960,9 +1015,10 @@ __global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(uint32_t nitems, const
             const uint32_t ns = B.it_nsel[item], nref = B.it_nch[item];
             const uint32_t sbase = B.it_choff[item] + item;
             for (uint32_t i = lane; i < ns; i += 32) {
-                S.sel[i] = B.sel_meta[sb + i];
-                S.st[i] = B.sel_start[sb + i];
-                S.cn[i] = B.sel_count[sb + i];
+                const uint4 sv = B.sel[sb + i];
+                S.sel[i] = sv.z;
+                S.st[i] = sv.x;
+                S.cn[i] = sv.y;
             }
             __syncwarp();
             for (uint32_t b = 0; b < nb; b++) {
@@ -1796,7 +1852,7 @@ static int dmalloc(T **p, uint64_t count) {
 }
 
 static void free_bufs(MapBufs &B) {
-    void *ps[] = {B.it_w, B.sel_start, B.sel_count, B.sel_meta, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
+    void *ps[] = {B.it_w, B.sel, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
@@ -1815,9 +1871,7 @@ static int alloc_items(swm_mapper *m) {
     const uint64_t I = m->cap_items;
     int rc = SWM_OK;
     rc |= dmalloc(&B.it_w, I * 32);
-    rc |= dmalloc(&B.sel_start, I * SWM_MAX_SEL);
-    rc |= dmalloc(&B.sel_count, I * SWM_MAX_SEL);
-    rc |= dmalloc(&B.sel_meta, I * SWM_MAX_SEL);
+    rc |= dmalloc(&B.sel, I * SWM_MAX_SEL);
     rc |= dmalloc(&B.it_nsel, I);
     rc |= dmalloc(&B.it_e, I);
     rc |= dmalloc(&B.it_nch, I);
@@ -1960,8 +2014,12 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     SWM_CUDA(cudaMemsetAsync(B.tot, 0, TOT_N * 4, st));
     SWM_CUDA(cudaMemsetAsync(B.stat, 0, ST_N * 8, st));
     SWM_CUDA(cudaEventRecord(m->ev[0], st));
-    if (ix->k == K12)
-        k_seed12<<<grid_cap(nitems, 128, 16), 128, 0, st>>>(d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, B);
+    if (ix->k == K12 && stride <= 10 * KL12 + KL12 - 1)
+        k_seed12<10><<<grid_cap(nitems, SEED12_THREADS, 8), SEED12_THREADS, seed12_smem(10), st>>>(
+            d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, B);
+    else if (ix->k == K12)
+        k_seed12<16><<<grid_cap(nitems, SEED12_THREADS, 6), SEED12_THREADS, seed12_smem(16), st>>>(
+            d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, B);
     else
         k_seed<<<grid_cap((uint64_t)nitems, SEED_WARPS * 32, 8), SEED_WARPS * 32, 0, st>>>(
             d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, ix->k, B);
