@@ -77,6 +77,7 @@ struct MapBufs {
     uint32_t *vr_aoff;
     uint8_t *arena;   // long CIGAR texts
     uint32_t *tb_list;   // candidates that need a traceback (cap_cands)
+    uint32_t *tb_cp;     // (VP, VN) at every 32-base block of each of them (cap_cands * 16)
     uint32_t *slow_list; // tracebacks whose route outgrew the fast path (cap_cands)
     // records
     uint32_t *out_w;  // cap_words
@@ -1200,9 +1201,10 @@ __device__ __forceinline__ uint32_t window_start(uint32_t base_pos, uint32_t L, 
 // with the pattern-match word built from window bit planes: at read base i
 // bit j of eq is [window[i + j] == read[i]] for j <= 2e, the same word the
 // reference keeps in peq[read[i]]. Returns (error, location) exactly as the
-// reference's final scan (634-650).
+// reference's final scan (634-650). cp gets (VP, VN) at the start of every
+// 32-base block.
 __device__ __forceinline__ int myers_scan(const uint32_t *WL, const uint32_t *WH, const uint32_t *RW, uint32_t L,
-                                          uint32_t e, uint32_t rl, int *loc_out) {
+                                          uint32_t e, uint32_t rl, int *loc_out, uint32_t *cp) {
     const uint32_t band = 2 * e + 1;
     const uint32_t MASK = (1u << band) - 1u;
     uint32_t vp = 0, vn = 0, ones = 0;
@@ -1211,6 +1213,8 @@ __device__ __forceinline__ int myers_scan(const uint32_t *WL, const uint32_t *WH
         const uint32_t wl0 = WL[b], wl1 = WL[b + 1], wh0 = WH[b], wh1 = WH[b + 1];
         const uint32_t rlw = RW[2 * b], rhw = RW[2 * b + 1];
         const uint32_t steps = min(32u, L - 32 * b);
+        cp[2 * b] = vp; // (VP, VN) before block b, for the traceback
+        cp[2 * b + 1] = vn;
         uint32_t acc = 0;
         if (steps == 32) {
 #pragma unroll
@@ -1354,7 +1358,8 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ len
 #pragma unroll
         for (int i = 0; i < 16; i++) rw[i] = RW[i];
         int loc;
-        const int err = myers_scan(WL, WH, rw, L, e, rl, &loc);
+        uint32_t cp[16];
+        const int err = myers_scan(WL, WH, rw, L, e, rl, &loc, cp);
         cells += (unsigned long long)L * (2 * e + 1);
         B.vr_err[c] = err;
         B.vr_mloc[c] = loc;
@@ -1391,6 +1396,11 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ len
         B.vr_flag[c] = VR_NEEDTB;
         const uint32_t at = atomicAdd(&B.tot[TOT_TB], 1u);
         B.tb_list[at] = (uint32_t)c;
+        uint4 *cpo = reinterpret_cast<uint4 *>(B.tb_cp + (uint64_t)at * 16);
+        const uint32_t nblk = (L + 31) >> 5;
+#pragma unroll
+        for (uint32_t k = 0; k < 4; k++)
+            if (4 * k < 2 * nblk) cpo[k] = make_uint4(cp[4 * k], cp[4 * k + 1], cp[4 * k + 2], cp[4 * k + 3]);
     }
     warp_add_u64(&B.stat[ST_CELLS], cells);
     warp_add_u64(&B.stat[ST_PASSED], passed);
@@ -1400,42 +1410,69 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ len
 // Traceback of the passing candidates that the Hamming check did not resolve
 // (align_reads, mapper_cpe.c:288-509): walk back from (L - 1, location)
 // through the D0 / HP words of the Myers run and emit the start position and
-// the CIGAR. The history is rebuilt 32 read bases at a time from (VP, VN)
-// checkpoints into shared memory (the walk only moves towards the read
-// start); the run-length route stays in shared memory too. A walk with more
-// than TB_ROUTE runs is handed to k_traceback_slow.
+// the CIGAR.
+//
+// The walk keeps match_site = i + search_site. While 0 <= search_site <= 2e
+// the pattern bit of step i at search_site is [ref(match_site) == read(i)]
+// and D0 contains it, so a step whose bases agree is always an M step: runs
+// of agreeing bases along the diagonal are taken 32 at a time from the bit
+// planes. Only the other steps (errors, or walks outside the band) need D0 /
+// HP, which are recomputed from the (VP, VN) checkpoint k_verify left at the
+// start of their 32-base block. The run-length route stays in shared memory;
+// a walk with more than TB_ROUTE runs is handed to k_traceback_slow.
 #define TB_THREADS 64
 #define TB_ROUTE 48
 
 struct TbSmem {
-    uint32_t cp[8][2][TB_THREADS];   // (VP, VN) before read bases 32b ..
-    uint32_t d0[32][TB_THREADS];     // D0 of the 32 bases of the current block
-    uint32_t hp[32][TB_THREADS];     // HP of the same bases
     uint16_t route[TB_ROUTE][TB_THREADS]; // size | kind << 12 (M S I D)
 };
 
-// 32 Myers steps of block b from (vp, vn); keeps D0 / HP when `keep`.
-__device__ __forceinline__ void myers_block(const uint32_t *WL, const uint32_t *WH, const uint32_t *rw, uint32_t b,
-                                            uint32_t steps, uint32_t MASK, uint32_t &vp, uint32_t &vn,
-                                            TbSmem *T, bool keep) {
+// D0 and HP of read base i: Myers steps from the checkpoint of its block.
+__device__ __forceinline__ void myers_at(const uint32_t *WL, const uint32_t *WH, const uint32_t *rw,
+                                         const uint32_t *cp, int i, uint32_t MASK, uint32_t &d0o, uint32_t &hpo) {
+    const uint32_t b = (uint32_t)i >> 5, tend = (uint32_t)i & 31;
+    uint32_t vp = cp[2 * b], vn = cp[2 * b + 1];
     const uint32_t wl0 = WL[b], wl1 = WL[b + 1], wh0 = WH[b], wh1 = WH[b + 1];
     const uint32_t rlw = rw[2 * b], rhw = rw[2 * b + 1];
-    for (uint32_t t = 0; t < steps; t++) {
+    uint32_t d0 = 0, hp = 0;
+    for (uint32_t t = 0; t <= tend; t++) {
         const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
         const uint32_t mL = 0u - ((rlw >> t) & 1u), mH = 0u - ((rhw >> t) & 1u);
         const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
         uint32_t x = eq | vn;
-        const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;
+        d0 = ((vp + (x & vp)) ^ vp) | x;
         const uint32_t hn = vp & d0;
-        const uint32_t hp = vn | ~(vp | d0);
+        hp = vn | ~(vp | d0);
         x = d0 >> 1;
         vn = x & hp;
         vp = hn | ~(x | hp);
-        if (keep) {
-            T->d0[t][threadIdx.x] = d0;
-            T->hp[t][threadIdx.x] = hp;
-        }
     }
+    d0o = d0;
+    hpo = hp;
+}
+
+// Bits start .. start + 31 of a bit array held as words P[0], P[st], P[2 st]
+// ...; positions below 0 read 0.
+__device__ __forceinline__ uint32_t bits32(const uint32_t *P, int st, int start) {
+    const int wi = start >> 5; // floor
+    const uint32_t a = wi >= 0 ? P[wi * st] : 0u, b = wi + 1 >= 0 ? P[(wi + 1) * st] : 0u;
+    return __funnelshift_r(a, b, (uint32_t)start & 31);
+}
+
+// Number of steps i, i - 1, ... (at most i + 1) whose read base equals the
+// window base at the same offset s.
+__device__ __forceinline__ int match_run(const uint32_t *WL, const uint32_t *WH, const uint32_t *rw, int i, int s) {
+    int run = 0, pos = i;
+    while (pos >= 0) {
+        const int lo = pos - 31;
+        const uint32_t x = (bits32(rw, 2, lo) ^ bits32(WL, 1, lo + s)) | (bits32(rw + 1, 2, lo) ^ bits32(WH, 1, lo + s));
+        const int k = x ? __clz(x) : 32;
+        if (k >= pos + 1) return run + pos + 1;
+        run += k;
+        if (k < 32) break;
+        pos -= 32;
+    }
+    return run;
 }
 
 __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__restrict__ lens,
@@ -1455,29 +1492,25 @@ __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__rest
         uint32_t WL[SWM_WIN_WORDS], WH[SWM_WIN_WORDS];
         load_window(b2, b2_words, ws, L, e, WL, WH);
         const uint32_t *RW = B.it_w + (uint64_t)item * 32;
-        uint32_t rw[16];
+        uint32_t rw[16], cp[16];
+        const uint4 *cps = reinterpret_cast<const uint4 *>(B.tb_cp + q * 16);
 #pragma unroll
-        for (int i = 0; i < 16; i++) rw[i] = RW[i];
-        const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
-        const uint32_t nblk = (L + 31) >> 5;
-        { // checkpoints
-            uint32_t vp = 0, vn = 0;
-            for (uint32_t b = 0; b < nblk; b++) {
-                T.cp[b][0][tid] = vp;
-                T.cp[b][1][tid] = vn;
-                if (b + 1 < nblk) myers_block(WL, WH, rw, b, 32, MASK, vp, vn, &T, false);
-            }
+        for (int k = 0; k < 4; k++) {
+            const uint4 r4 = reinterpret_cast<const uint4 *>(RW)[k];
+            rw[4 * k] = r4.x;
+            rw[4 * k + 1] = r4.y;
+            rw[4 * k + 2] = r4.z;
+            rw[4 * k + 3] = r4.w;
+            const uint4 c4 = cps[k];
+            cp[4 * k] = c4.x;
+            cp[4 * k + 1] = c4.y;
+            cp[4 * k + 2] = c4.z;
+            cp[4 * k + 3] = c4.w;
         }
-        int cur = -1;
+        const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
         auto bits = [&](int i, int ss, uint32_t *d0b, uint32_t *hpb) {
-            const int b = i >> 5;
-            if (b != cur) {
-                uint32_t vp = T.cp[b][0][tid], vn = T.cp[b][1][tid];
-                const uint32_t steps = min(32u, L - 32u * (uint32_t)b);
-                myers_block(WL, WH, rw, (uint32_t)b, steps, MASK, vp, vn, &T, true);
-                cur = b;
-            }
-            const uint32_t d0 = T.d0[i & 31][tid], hp = T.hp[i & 31][tid];
+            uint32_t d0, hp;
+            myers_at(WL, WH, rw, cp, i, MASK, d0, hp);
             const bool in = ss >= 0 && ss < 32; // defined read of bits outside 0..31: 0
             *d0b = in ? ((d0 >> ss) & 1u) : 0u;
             *hpb = in ? ((hp >> ss) & 1u) : 0u;
@@ -1492,16 +1525,16 @@ __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__rest
         bool overflow = false;
         int pre_size = 1;
         uint32_t pre = 0; // 0 M, 1 S, 2 I, 3 D
+        auto flush_run = [&](uint32_t kind) { // a new run of `kind` starts
+            if (nr < TB_ROUTE) T.route[nr][tid] = (uint16_t)(pre_size | (pre << 12));
+            else overflow = true;
+            nr++;
+            pre_size = 1;
+            pre = kind;
+        };
         auto push = [&](uint32_t kind) {
-            if (pre != kind) {
-                if (nr < TB_ROUTE) T.route[nr][tid] = (uint16_t)(pre_size | (pre << 12));
-                else overflow = true;
-                nr++;
-                pre_size = 1;
-                pre = kind;
-            } else {
-                pre_size++;
-            }
+            if (pre != kind) flush_run(kind);
+            else pre_size++;
         };
         { // first step, mapper_cpe.c:380-410
             uint32_t d0b, hpb;
@@ -1519,6 +1552,20 @@ __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__rest
         while (i >= 0) { // mapper_cpe.c:412-466
             if (sum_err == err) break;
             if (match_site < 0) break; // defined stop below the window start
+            if (search_site >= 0 && search_site <= 2 * (int)e) {
+                const int run = match_run(WL, WH, rw, i, search_site);
+                if (run > 0) { // run M steps
+                    if (pre != 0) {
+                        flush_run(0);
+                        pre_size = run;
+                    } else {
+                        pre_size += run;
+                    }
+                    i -= run;
+                    match_site -= run;
+                    continue;
+                }
+            }
             uint32_t d0b, hpb;
             bits(i, search_site, &d0b, &hpb);
             if (d0b && TREF(match_site) == TREAD(i)) {
@@ -1856,7 +1903,7 @@ static void free_bufs(MapBufs &B) {
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
-                  B.slow_list,
+                  B.tb_cp, B.slow_list,
                   B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
     for (void *p : ps) cudaFree(p);
     memset(&B, 0, sizeof(B));
@@ -1899,7 +1946,7 @@ static int alloc_work(swm_mapper *m) {
     cudaFree(B.bt_cnt); cudaFree(B.sort_scratch); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
     cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
     cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
-    cudaFree(B.tb_list); cudaFree(B.slow_list);
+    cudaFree(B.tb_list); cudaFree(B.tb_cp); cudaFree(B.slow_list);
     cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
     rc |= dmalloc(&B.ch_g, m->cap_chunks);
     rc |= dmalloc(&B.ch_meta, m->cap_chunks);
@@ -1920,6 +1967,7 @@ static int alloc_work(swm_mapper *m) {
     rc |= dmalloc(&B.vr_aoff, m->cap_cands);
     rc |= dmalloc(&B.arena, m->cap_arena);
     rc |= dmalloc(&B.tb_list, m->cap_cands);
+    rc |= dmalloc(&B.tb_cp, m->cap_cands * 16);
     rc |= dmalloc(&B.slow_list, m->cap_cands);
     rc |= dmalloc(&B.out_w, m->cap_words);
     rc |= dmalloc(&B.out_c, m->cap_bytes);
@@ -2053,7 +2101,7 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[5], st));
-    k_traceback<<<grid_cap(m->cap_cands, TB_THREADS, 8), TB_THREADS, 0, st>>>(
+    k_traceback<<<grid_cap(m->cap_cands, TB_THREADS, 16), TB_THREADS, 0, st>>>(
         d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
         m->cap_arena);
     k_traceback_slow<<<grid_cap(m->cap_cands, 128, 4), 128, 0, st>>>(
