@@ -54,7 +54,9 @@ enum { TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT
 struct MapBufs {
     // per item
     uint32_t *it_w;        // items * 32: [0..15] Myers planes, [16..31] Hamming planes
-    uint4 *sel;            // items * 64: (bucket start, count, base | shift << 16 | rl << 20 | rh << 24, 0)
+    uint2 *sel;            // items * 64: (bucket start, count) of the seed of long seed l, shift t at 4 l + t
+    uint8_t *sel_fl;       // items * 64: its read flank bits rl | rh << 3 (rl, rh: 3 bits each)
+    unsigned long long *it_perm; // items: selected slot i is record 4 * nibble(i / 4) + i % 4
     uint8_t *it_nsel, *it_e;
     uint32_t *it_nch, *it_nel, *it_nbat;
     uint32_t *it_choff, *it_eloff; // items + 1
@@ -237,7 +239,7 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict
     __shared__ SeedSmem sm_all[SEED_WARPS];
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     SeedSmem &S = sm_all[wib];
-    uint4 *__restrict__ sel = B.sel;
+    uint2 *__restrict__ sel = B.sel;
     const uint32_t nitems = 2 * nreads;
     const uint32_t klong = k + SWM_SEED_STEP - 1;
     const uint32_t kmask = (1u << k) - 1, lmask = (1u << klong) - 1, rmask = (1u << (SWM_SEED_STEP - 1)) - 1;
@@ -421,8 +423,8 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict
                     const uint32_t m = (1u << sft) - 1, kk = k + sft;
                     const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & rmask; // 2483-2495
                     const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & rmask;
-                    sel[sb + i] = make_uint4(o0, c, (o + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) |
-                                                          (rh << 24), 0u);
+                    sel[sb + SWM_SEED_STEP * l + sft] = make_uint2(o0, c);
+                    B.sel_fl[sb + SWM_SEED_STEP * l + sft] = (uint8_t)(rl | (rh << 3));
                     nref += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
                     nel += c;
                 }
@@ -443,6 +445,9 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict
             B.it_w[(uint64_t)item * 32 + lane] = ow;
             if (lane == 0) {
                 B.it_nsel[item] = (uint8_t)ns;
+                unsigned long long perm = 0;
+                for (uint32_t a = 0; a < nsl; a++) perm |= (unsigned long long)SK(idx, a, t) << (4 * a);
+                B.it_perm[item] = perm;
                 B.it_e[item] = (uint8_t)e;
                 B.it_nch[item] = nref;                  // refill chunks (beyond the first chunk of each seed)
                 B.it_nel[item] = nel;
@@ -462,9 +467,12 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict
 // alternate words of it and exchange the halves; the reverse strand is the
 // bit reverse of the forward planes. Seed codes come from interleaved 2-bit
 // words of the strand (one funnel shift per seed), so every bucket lookup of
-// a read issues back to back; the (start, count) pairs wait in shared memory
-// for the selection. The literal tail replay touches at most two 2-bit words
-// (P >= L - 11), kept in registers.
+// a read issues back to back. Every seed's record (bucket start, count,
+// flank bits) is written at slot 4 l + shift as soon as its lookup returns;
+// the selection is then only the rank order of the long seeds, stored as a
+// permutation (sel_slot), so no lookup is repeated and no shared memory
+// limits the occupancy. The literal tail replay touches at most two 2-bit
+// words (P >= L - 11), kept in registers.
 
 #define K12 12u
 #define KL12 15u
@@ -497,7 +505,8 @@ __host__ __device__ constexpr uint32_t nfill12(uint32_t sft) {
     return w;
 }
 
-// L2-resident loads of the bucket offsets (hint: keep them over streamed data)
+// Bucket offsets are read through an L2 evict-last policy: the 64 MB table
+// stays in L2 while reads and records stream past it.
 __device__ __forceinline__ uint64_t l2_keep_policy() {
     uint64_t pol;
     asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
@@ -509,35 +518,62 @@ __device__ __forceinline__ uint32_t ld_keep(const uint32_t *p, uint64_t pol) {
     return v;
 }
 
-// Bucket (start, count) of every seed of long seeds 0 .. NL-1 into shared
-// memory, slot 4 l + sft; returns the per-long-seed sums in cnt.
+// Seed code of the seed at read offset o (12 bases from o) from the
+// interleaved words w0 = word o / 16 and w1 = the next one; with N bases
+// (nk = the "not A/C/G/T" bits of bases o .. o + 11) the N positions take
+// their code nfill12(sft).
+__device__ __forceinline__ uint32_t seed12_code(uint32_t w0, uint32_t w1, uint32_t o) {
+    const uint32_t sh = 2 * (o & 15);
+    return (sh ? __funnelshift_r(w0, w1, sh) : w0) & 0xffffffu;
+}
+__device__ __forceinline__ uint32_t seed12_nfix(uint32_t sd, uint32_t nk, uint32_t sft) {
+    const uint32_t M = spread_bits(nk & 0xfffu) * 3u;
+    return (sd & ~M) | (nfill12(sft) & M);
+}
+
+// Record of every seed of long seeds 0 .. NL-1 at slot 4 l + shift: (bucket
+// start, count) in rec and the flank byte rl | rh << 3 in byte 4 l + shift of
+// flw, where rl / rh are the lo / hi bits of the 3 long-seed bases outside
+// the 12-mer (set_read_long_seeds, 2474-2478). cnt gets the bucket counts summed per
+// long seed (choose_seed, 1372-1390), nref the refill chunks. Every lookup is
+// independent, so they all issue back to back.
 template <int NL, bool HASN>
-__device__ __forceinline__ void seed12_lookup(const uint32_t (&iw)[NL], const uint32_t (&pok)[8], uint32_t nl,
-                                              const uint32_t *__restrict__ off, uint64_t pol, uint2 *oc,
-                                              uint32_t (&cnt)[NL]) {
-    const uint32_t tid = threadIdx.x;
+__device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const uint32_t (&plo)[8],
+                                               const uint32_t (&phi)[8], const uint32_t (&pok)[8], uint32_t nl,
+                                               const uint32_t *__restrict__ off, uint64_t pol,
+                                               uint2 *__restrict__ rec, uint32_t *__restrict__ flw,
+                                               uint32_t (&cnt)[NL], uint32_t (&nref)[NL]) {
 #pragma unroll
     for (int l = 0; l < NL; l++) {
-        uint32_t csum = 0;
+        const bool act = (uint32_t)l < nl;
+        const uint32_t ob = KL12 * l, wj0 = ob >> 5, sh0 = ob & 31;
+        const uint32_t nlo = wj0 + 1 < 8 ? plo[wj0 + 1] : 0u, nhi = wj0 + 1 < 8 ? phi[wj0 + 1] : 0u;
+        const uint32_t lr = (sh0 ? __funnelshift_r(plo[wj0], nlo, sh0) : plo[wj0]) & 0x7fffu;
+        const uint32_t hr = (sh0 ? __funnelshift_r(phi[wj0], nhi, sh0) : phi[wj0]) & 0x7fffu;
+        uint32_t csum = 0, rsum = 0, f = 0;
 #pragma unroll
         for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
-            const uint32_t o = KL12 * l + sft, w = o >> 4, sh = 2 * (o & 15);
-            const uint32_t hi = (w + 1 < (uint32_t)NL) ? iw[w + 1] : 0u;
-            uint32_t sd = (sh ? __funnelshift_r(iw[w], hi, sh) : iw[w]) & 0xffffffu;
+            const uint32_t o = ob + sft, w = o >> 4;
+            uint32_t sd = seed12_code(iw[w], (w + 1 < (uint32_t)NL) ? iw[w + 1] : 0u, o);
             if (HASN) {
                 const uint32_t wj = o >> 5, s5 = o & 31;
                 const uint32_t nx = wj + 1 < 8 ? pok[wj + 1] : 0xffffffffu;
-                const uint32_t nm = ~(s5 ? __funnelshift_r(pok[wj], nx, s5) : pok[wj]) & 0xfffu;
-                const uint32_t M = spread_bits(nm) * 3u;
-                sd = (sd & ~M) | (nfill12(sft) & M);
+                sd = seed12_nfix(sd, ~(s5 ? __funnelshift_r(pok[wj], nx, s5) : pok[wj]), sft);
             }
-            sd = ((uint32_t)l < nl) ? sd : 0u;
-            const uint32_t o0 = ld_keep(off + sd, pol), o1 = ld_keep(off + sd + 1, pol);
-            const uint32_t c = o1 - o0;
-            oc[(4 * l + sft) * SEED12_THREADS + tid] = make_uint2(o0, c);
+            sd = act ? sd : 0u;
+            const uint32_t o0 = ld_keep(off + sd, pol);
+            const uint32_t c = ld_keep(off + sd + 1, pol) - o0;
+            const uint32_t m = (1u << sft) - 1, kk = K12 + sft;
+            const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & 7u;
+            const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & 7u;
+            rec[SWM_SEED_STEP * l + sft] = make_uint2(o0, c);
+            f |= (rl | (rh << 3)) << (8 * sft);
             csum += c;
+            rsum += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
         }
-        cnt[l] = ((uint32_t)l < nl) ? csum : 0u;
+        flw[l] = f;
+        cnt[l] = act ? csum : 0u;
+        nref[l] = act ? rsum : 0u;
     }
 }
 
@@ -547,10 +583,7 @@ __global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const char *__restric
                                                            uint32_t nreads, uint32_t e_glob,
                                                            const uint8_t *__restrict__ e_arr,
                                                            const uint32_t *__restrict__ off, MapBufs B) {
-    extern __shared__ uint2 s12[];
-    uint2 *oc = s12;                                                          // [4 NL][threads]
-    uint32_t *fl = reinterpret_cast<uint32_t *>(s12 + 4 * NL * SEED12_THREADS); // [NL][threads]
-    uint4 *__restrict__ sel = B.sel;
+    uint2 *__restrict__ sel = B.sel;
     uint32_t *__restrict__ it_w = B.it_w;
     const uint32_t tid = threadIdx.x;
     const uint32_t nitems = 2 * nreads;
@@ -688,29 +721,13 @@ __global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const char *__restric
             pok[b] |= ~m; // positions outside the visit are not N
         }
         // ---- interleaved 2-bit words of the strand (base 16 w + i at bits
-        // 2i, 2i + 1) and the flank bits of every long seed
+        // 2i, 2i + 1)
         uint32_t iw[NL];
 #pragma unroll
         for (int w = 0; w < NL; w++) {
             const uint32_t l16 = (w & 1) ? (plo[w >> 1] >> 16) : plo[w >> 1];
             const uint32_t h16 = (w & 1) ? (phi[w >> 1] >> 16) : phi[w >> 1];
             iw[w] = spread_bits(l16) | (spread_bits(h16) << 1);
-        }
-#pragma unroll
-        for (int l = 0; l < NL; l++) {
-            const uint32_t o = KL12 * l, wj = o >> 5, sh = o & 31;
-            const uint32_t nlo = wj + 1 < 8 ? plo[wj + 1] : 0u, nhi = wj + 1 < 8 ? phi[wj + 1] : 0u;
-            const uint32_t lr = (sh ? __funnelshift_r(plo[wj], nlo, sh) : plo[wj]) & 0x7fffu;
-            const uint32_t hr = (sh ? __funnelshift_r(phi[wj], nhi, sh) : phi[wj]) & 0x7fffu;
-            uint32_t f = 0;
-#pragma unroll
-            for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) { // the 3 bases around the 12-mer
-                const uint32_t m = (1u << sft) - 1, kk = K12 + sft;
-                const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & 7u;
-                const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & 7u;
-                f |= (rl | (rh << 3)) << (6 * sft);
-            }
-            fl[l * SEED12_THREADS + tid] = f;
         }
         // ---- Myers planes: complete 2-bit words up to P are the planes, the
         // partial word is unwritten; the tail replay rewrites words P/16 and
@@ -797,10 +814,12 @@ __global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const char *__restric
         ow[5] = make_uint4(plo[2], phi[2], plo[3], phi[3]);
         ow[6] = make_uint4(plo[4], phi[4], plo[5], phi[5]);
         ow[7] = make_uint4(plo[6], phi[6], plo[7], phi[7]);
-        // ---- bucket counts of every seed, all lookups in flight together
-        uint32_t CNT[NL], IDX[NL];
-        if (has_n) seed12_lookup<NL, true>(iw, pok, nl, off, pol, oc, CNT);
-        else seed12_lookup<NL, false>(iw, pok, nl, off, pol, oc, CNT);
+        // ---- every seed's record, all lookups in flight together
+        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+        uint32_t CNT[NL], IDX[NL], REF[NL];
+        uint32_t *flw = reinterpret_cast<uint32_t *>(B.sel_fl + sb);
+        if (has_n) seed12_records<NL, true>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, CNT, REF);
+        else seed12_records<NL, false>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, CNT, REF);
 #pragma unroll
         for (int l = 0; l < NL; l++) IDX[l] = l;
         // exchange sort (1391-1399), unrolled
@@ -809,35 +828,28 @@ __global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const char *__restric
 #pragma unroll
             for (int m2 = a + 1; m2 < NL; m2++) {
                 const bool sw = ((uint32_t)m2 < nl) & (CNT[a] > CNT[m2]);
-                const uint32_t ca = CNT[a], cm = CNT[m2], ia = IDX[a], im = IDX[m2];
+                const uint32_t ca = CNT[a], cm = CNT[m2], ia = IDX[a], im = IDX[m2], ra = REF[a], rm = REF[m2];
                 CNT[a] = sw ? cm : ca;
                 CNT[m2] = sw ? ca : cm;
                 IDX[a] = sw ? im : ia;
                 IDX[m2] = sw ? ia : im;
+                REF[a] = sw ? rm : ra;
+                REF[m2] = sw ? ra : rm;
             }
         }
-        // ---- the (e + 1) rarest long seeds x 4 shifts, rank by rank
-        // (alignment_rmdup 2194-2196)
+        // ---- the (e + 1) rarest long seeds x 4 shifts (alignment_rmdup
+        // 2194-2196): ranks 0 .. nsl - 1 of the sorted order
         const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
         const uint32_t ns = nsl * SWM_SEED_STEP;
-        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
         uint32_t nref = 0, nel = 0;
+        unsigned long long perm = 0;
 #pragma unroll
         for (int a = 0; a < NL; a++) {
-            if ((uint32_t)a < nsl) {
-                const uint32_t l = IDX[a];
-                const uint32_t f = fl[l * SEED12_THREADS + tid];
-#pragma unroll
-                for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
-                    const uint2 v = oc[(4 * l + sft) * SEED12_THREADS + tid];
-                    const uint32_t rl = (f >> (6 * sft)) & 7u, rh = (f >> (6 * sft + 3)) & 7u;
-                    const uint32_t meta = (KL12 * l + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | (rl << 20) | (rh << 24);
-                    sel[sb + a * SWM_SEED_STEP + sft] = make_uint4(v.x, v.y, meta, 0u);
-                    nref += v.y > SWM_PER_FETCH ? (v.y - 1) / SWM_PER_FETCH : 0u;
-                    nel += v.y;
-                }
-            }
+            nref += (uint32_t)a < nsl ? REF[a] : 0u;
+            nel += (uint32_t)a < nsl ? CNT[a] : 0u;
+            perm |= (unsigned long long)IDX[a] << (4 * a);
         }
+        B.it_perm[item] = perm;
         B.it_nsel[item] = (uint8_t)ns;
         B.it_e[item] = (uint8_t)e;
         B.it_nch[item] = nref;
@@ -846,7 +858,13 @@ __global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const char *__restric
     }
 }
 
-static size_t seed12_smem(int nl) { return (size_t)nl * SEED12_THREADS * (4 * sizeof(uint2) + sizeof(uint32_t)); }
+
+// Record of selected slot i (rank i / 4, shift i % 4) in the item's sel
+// records: k_seed12 writes every seed at 4 l + shift and the ranks as a
+// permutation of the long seeds l.
+__device__ __forceinline__ uint32_t sel_slot(unsigned long long perm, uint32_t i) {
+    return (uint32_t)((perm >> (4 * (i >> 2))) & 15u) * SWM_SEED_STEP + (i & 3u);
+}
 
 // ======================================================================
 // k_plan: the refill schedule of alignment_rmdup, one thread per item whose
@@ -872,11 +890,12 @@ __global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const unsigned lo
         }
         const uint32_t ns = B.it_nsel[item];
         const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+        const unsigned long long perm = B.it_perm[item];
         uint32_t pc[SWM_MAX_SEL], sst[SWM_MAX_SEL], scn[SWM_MAX_SEL];
         uint32_t hloc[SWM_MAX_SEL + 8], hidx[SWM_MAX_SEL + 8];
         uint32_t hs = 0, rc = 0, e = 0, b = 0, br0 = 0, be0 = 0, npos = 0, runs = 0;
         for (uint32_t i = 0; i < ns; i++) { // initial fetch of <= 32 per seed, 2194-2236
-            const uint4 sv = B.sel[sb + i];
+            const uint2 sv = B.sel[sb + sel_slot(perm, i)];
             sst[i] = sv.x;
             scn[i] = sv.y;
             const uint32_t get = scn[i] > SWM_PER_FETCH ? SWM_PER_FETCH : scn[i];
@@ -1000,8 +1019,9 @@ __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
 
 // One warp per item, every batch of the item: element-parallel gather of
 // (position, flank code) pairs, position adjust, flank filter, sort-unique.
-__global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(uint32_t nitems, const unsigned long long *__restrict__ pl,
-                                                          MapBufs B, uint64_t cap_chunks, uint64_t cap_elems) {
+__global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(uint32_t nitems, const unsigned long long *__restrict__ pl,
+                                                             MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
+                                                             uint32_t klong) {
     __shared__ CandSmem sm_all[CAND_WARPS];
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
@@ -1014,10 +1034,14 @@ __global__ void __launch_bounds__(CAND_WARPS * 32) k_cand(uint32_t nitems, const
         if (nb) {
             const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
             const uint32_t ns = B.it_nsel[item], nref = B.it_nch[item];
+            const unsigned long long perm = B.it_perm[item];
             const uint32_t sbase = B.it_choff[item] + item;
             for (uint32_t i = lane; i < ns; i += 32) {
-                const uint4 sv = B.sel[sb + i];
-                S.sel[i] = sv.z;
+                const uint32_t rs = sel_slot(perm, i), l = rs / SWM_SEED_STEP, sft = rs % SWM_SEED_STEP;
+                const uint2 sv = B.sel[sb + rs];
+                const uint32_t fb = B.sel_fl[sb + rs];
+                // base | shift << 16 | rl << 20 | rh << 24
+                S.sel[i] = (l * klong + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | ((fb & 7u) << 20) | ((fb >> 3) << 24);
                 S.st[i] = sv.x;
                 S.cn[i] = sv.y;
             }
@@ -1899,7 +1923,7 @@ static int dmalloc(T **p, uint64_t count) {
 }
 
 static void free_bufs(MapBufs &B) {
-    void *ps[] = {B.it_w, B.sel, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
+    void *ps[] = {B.it_w, B.sel, B.sel_fl, B.it_perm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
@@ -1919,6 +1943,8 @@ static int alloc_items(swm_mapper *m) {
     int rc = SWM_OK;
     rc |= dmalloc(&B.it_w, I * 32);
     rc |= dmalloc(&B.sel, I * SWM_MAX_SEL);
+    rc |= dmalloc(&B.sel_fl, I * SWM_MAX_SEL);
+    rc |= dmalloc(&B.it_perm, I);
     rc |= dmalloc(&B.it_nsel, I);
     rc |= dmalloc(&B.it_e, I);
     rc |= dmalloc(&B.it_nch, I);
@@ -2063,10 +2089,10 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     SWM_CUDA(cudaMemsetAsync(B.stat, 0, ST_N * 8, st));
     SWM_CUDA(cudaEventRecord(m->ev[0], st));
     if (ix->k == K12 && stride <= 10 * KL12 + KL12 - 1)
-        k_seed12<10><<<grid_cap(nitems, SEED12_THREADS, 8), SEED12_THREADS, seed12_smem(10), st>>>(
+        k_seed12<10><<<grid_cap(nitems, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(
             d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, B);
     else if (ix->k == K12)
-        k_seed12<16><<<grid_cap(nitems, SEED12_THREADS, 6), SEED12_THREADS, seed12_smem(16), st>>>(
+        k_seed12<16><<<grid_cap(nitems, SEED12_THREADS, 8), SEED12_THREADS, 0, st>>>(
             d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, B);
     else
         k_seed<<<grid_cap((uint64_t)nitems, SEED_WARPS * 32, 8), SEED_WARPS * 32, 0, st>>>(
@@ -2083,7 +2109,8 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[2], st));
-    k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(nitems, ix->d_pl, B, m->cap_chunks, m->cap_elems);
+    k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(nitems, ix->d_pl, B, m->cap_chunks, m->cap_elems,
+                                                     ix->k + SWM_SEED_STEP - 1);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[3], st));
