@@ -1167,23 +1167,25 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(uint32_t nitems, co
 }
 
 // Dense candidate list: item by item, batch by batch, in verification order.
-__global__ void k_compact(uint32_t nitems, MapBufs B, uint64_t cap_chunks, uint64_t cap_elems, uint64_t cap_cands) {
+__global__ void __launch_bounds__(256) k_compact(uint32_t nitems, MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
+                                                 uint64_t cap_cands) {
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
-    const uint32_t lane = lane_id();
-    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < nitems; item += nwarps) {
-        const uint32_t nb = B.it_nbat[item];
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
+        // one thread per item: its scalars in one round trip, then its few
+        // candidates batch by batch
+        const uint32_t nb = B.it_nbat[item], nref = B.it_nch[item];
+        const uint32_t o0 = B.it_coff[item], nc = B.it_ncand[item];
+        const uint32_t sbase = B.it_choff[item] + item, eloff = B.it_eloff[item];
         if (!nb) continue;
-        uint32_t o = B.it_coff[item];
-        if ((uint64_t)o + B.it_ncand[item] > cap_cands) {
-            if (lane == 0) atomicOr(&B.tot[TOT_FLAGS], OV_CANDS);
+        if ((uint64_t)o0 + nc > cap_cands) {
+            atomicOr(&B.tot[TOT_FLAGS], OV_CANDS);
             continue;
         }
-        const uint32_t sbase = B.it_choff[item] + item, nref = B.it_nch[item];
+        uint32_t o = o0;
         for (uint32_t b = 0; b < nb; b++) {
-            const uint32_t n = B.bt_cnt[sbase + b];
-            const uint32_t e0 = nref ? B.bt_e0[sbase + b] : B.it_eloff[item];
-            for (uint32_t j = lane; j < n; j += 32) {
+            const uint32_t n = nref ? B.bt_cnt[sbase + b] : nc; // one batch when there are no refills
+            const uint32_t e0 = nref ? B.bt_e0[sbase + b] : eloff;
+            for (uint32_t j = 0; j < n; j++) {
                 B.cc_pos[o + j] = B.cand_ub[e0 + j];
                 B.cc_item[o + j] = item;
             }
@@ -2117,8 +2119,7 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     rc = swm_exclusive_scan(B.it_ncand, B.it_coff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_CANDS, st);
     if (rc) return rc;
     m->launches += 3;
-    k_compact<<<grid_cap((uint64_t)nitems * 32, 256, 16), 256, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems,
-                                                                        m->cap_cands);
+    k_compact<<<grid_cap(nitems, 256, 8), 256, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems, m->cap_cands);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[4], st));
