@@ -78,6 +78,7 @@ struct MapBufs {
     uint8_t *vr_cig;  // cap_cands * SWM_CIGAR_SLOT
     uint32_t *vr_aoff;
     uint8_t *arena;   // long CIGAR texts
+    uint16_t *unm;       // bit j of halfword w: read 16 w + j has no location (cap_items / 32 + 1)
     uint32_t *tb_list;   // candidates that need a traceback (cap_cands)
     uint32_t *tb_cp;     // (VP, VN) at every 32-base block of each of them (cap_cands * 16)
     uint32_t *slow_list; // tracebacks whose route outgrew the fast path (cap_cands)
@@ -107,7 +108,8 @@ struct swm_mapper {
     uint32_t *h_lens;
     uint8_t *h_e;
     // pinned result staging
-    uint32_t *h_w, *h_rw, *h_rb, *h_rl, *h_nrec;
+    uint32_t *h_w, *h_rw, *h_rb, *h_rl;
+    uint16_t *h_unm;
     uint8_t *h_c;
     uint64_t h_cap_w, h_cap_c, h_cap_rw, h_cap_rb, h_cap_rl, h_cap_items;
     uint32_t *h_tot;           // pinned copy of B.tot
@@ -1805,6 +1807,13 @@ __global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uin
                                                  uint64_t cap_cands, uint64_t cap_recs, uint64_t cap_words,
                                                  uint64_t cap_bytes) {
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    // distinct arrays: loads of later candidates may pass earlier stores
+    const uint8_t *__restrict__ vflag = B.vr_flag;
+    const uint32_t *__restrict__ vloc = B.vr_loc;
+    const uint16_t *__restrict__ vtlen = B.vr_tlen;
+    const uint8_t *__restrict__ vcig = B.vr_cig;
+    uint8_t *__restrict__ out_c = B.out_c;
+    uint32_t *__restrict__ out_w = B.out_w;
     unsigned long long locs_total = 0, mapped = 0;
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
         const uint32_t s0 = B.it_choff[item] + item, nb = B.it_nbat[item];
@@ -1824,8 +1833,8 @@ __global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uin
         auto put = [&]() { // put_cigar, 1437-1507
             if (num > 0) {
                 if (WRITE && ok) {
-                    B.out_w[wrec] = item;
-                    B.out_w[wrec + 1] = num | (mainf ? (1u << 31) : 0u);
+                    out_w[wrec] = item;
+                    out_w[wrec + 1] = num | (mainf ? (1u << 31) : 0u);
                     B.rec_woff[recbase + nrec] = wrec;
                     B.rec_boff[recbase + nrec] = bcur - len;
                     B.rec_blen[recbase + nrec] = len;
@@ -1845,19 +1854,28 @@ __global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uin
             cnext += cn;
             uint32_t g = 0;
             for (uint32_t c = cbeg; c < cbeg + cn; c++) {
-                const uint8_t f = B.vr_flag[c];
+                const uint8_t f = vflag[c];
                 if (f == VR_INVALID) continue;
                 if (f == VR_HAM || f == VR_TB) {
-                    const uint32_t loc = B.vr_loc[c];
+                    const uint32_t loc = vloc[c];
                     if (f == VR_HAM || !(num > 0 && last == loc)) { // 475-477
-                        const uint32_t tl = B.vr_tlen[c];
+                        const uint32_t tl = vtlen[c];
                         if (WRITE && ok) {
-                            B.out_w[wrec + 2 + num] = loc;
-                            const uint8_t *sl = B.vr_cig + (uint64_t)c * SWM_CIGAR_SLOT;
-                            B.out_c[bcur] = sl[0];
-                            B.out_c[bcur + 1] = sl[1];
-                            const uint8_t *tx = (tl <= SWM_CIGAR_SLOT - 2) ? sl + 2 : B.arena + B.vr_aoff[c];
-                            for (uint32_t q = 0; q < tl; q++) B.out_c[bcur + 2 + q] = tx[q];
+                            out_w[wrec + 2 + num] = loc;
+                            // [NM, len, text]: the slot's first 16 bytes in one load
+                            const uint4 h = *reinterpret_cast<const uint4 *>(vcig + (uint64_t)c * SWM_CIGAR_SLOT);
+                            const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
+                            if (tl + 2 <= 16) {
+#pragma unroll
+                                for (uint32_t q = 0; q < 16; q++)
+                                    if (q < tl + 2) out_c[bcur + q] = (uint8_t)(hw[q >> 2] >> (8 * (q & 3)));
+                            } else {
+                                out_c[bcur] = (uint8_t)h.x;
+                                out_c[bcur + 1] = (uint8_t)(h.x >> 8);
+                                const uint8_t *tx = (tl <= SWM_CIGAR_SLOT - 2) ? vcig + (uint64_t)c * SWM_CIGAR_SLOT + 2
+                                                                              : B.arena + B.vr_aoff[c];
+                                for (uint32_t q = 0; q < tl; q++) out_c[bcur + 2 + q] = tx[q];
+                            }
                         }
                         bcur += 2 + tl;
                         num++;
@@ -1877,8 +1895,14 @@ __global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uin
             B.it_nrec[item] = nrec;
             B.it_nw[item] = nw;
             B.it_nb[item] = nby;
-        } else if ((item & 1) && (nrec + B.it_nrec[item - 1]) > 0) {
-            mapped++;
+        } else {
+            const bool mp = (item & 1) && (nrec + B.it_nrec[item - 1]) > 0;
+            mapped += mp ? 1u : 0u;
+            // unmapped reads as bits, 16 reads (one warp of items) per halfword
+            const uint32_t item0 = item & ~31u, left = nitems - item0;
+            const uint32_t wm = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
+            const uint32_t bal = __ballot_sync(wm, (item & 1) && !mp);
+            if ((item & 31) == 0) B.unm[item0 >> 5] = (uint16_t)even_bits(bal >> 1);
         }
     }
     if (WRITE) {
@@ -1925,7 +1949,7 @@ static int dmalloc(T **p, uint64_t count) {
 }
 
 static void free_bufs(MapBufs &B) {
-    void *ps[] = {B.it_w, B.sel, B.sel_fl, B.it_perm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
+    void *ps[] = {B.it_w, B.sel, B.sel_fl, B.it_perm, B.unm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
@@ -1947,6 +1971,7 @@ static int alloc_items(swm_mapper *m) {
     rc |= dmalloc(&B.sel, I * SWM_MAX_SEL);
     rc |= dmalloc(&B.sel_fl, I * SWM_MAX_SEL);
     rc |= dmalloc(&B.it_perm, I);
+    rc |= dmalloc(&B.unm, I / 32 + 1);
     rc |= dmalloc(&B.it_nsel, I);
     rc |= dmalloc(&B.it_e, I);
     rc |= dmalloc(&B.it_nch, I);
@@ -2032,7 +2057,7 @@ extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper *
     if (rc == SWM_OK && (dmalloc(&m->d_lens, max_reads) || dmalloc(&m->d_e, max_reads))) rc = SWM_ERR_OOM;
     if (rc == SWM_OK && (cudaHostAlloc((void **)&m->h_lens, max_reads * 4, 0) != cudaSuccess ||
                          cudaHostAlloc((void **)&m->h_e, max_reads, 0) != cudaSuccess ||
-                         cudaHostAlloc((void **)&m->h_nrec, m->cap_items * 4, 0) != cudaSuccess ||
+                         cudaHostAlloc((void **)&m->h_unm, (m->cap_items / 32 + 1) * 2, 0) != cudaSuccess ||
                          cudaHostAlloc((void **)&m->h_tot, TOT_N * 4, 0) != cudaSuccess ||
                          cudaHostAlloc((void **)&m->h_stat, ST_N * 8, 0) != cudaSuccess))
         rc = SWM_ERR_OOM;
@@ -2040,7 +2065,7 @@ extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper *
         swm_mapper_free(m);
         return rc;
     }
-    m->h_cap_items = m->cap_items;
+    m->h_cap_items = m->cap_items / 32 + 1;
     *out = m;
     return SWM_OK;
 }
@@ -2061,7 +2086,7 @@ extern "C" void swm_mapper_free(swm_mapper *m) {
     cudaFreeHost(m->h_rw);
     cudaFreeHost(m->h_rb);
     cudaFreeHost(m->h_rl);
-    cudaFreeHost(m->h_nrec);
+    cudaFreeHost(m->h_unm);
     cudaFreeHost(m->h_tot);
     cudaFreeHost(m->h_stat);
     for (int i = 0; i < 9; i++)
@@ -2327,6 +2352,26 @@ static bool is_pinned(const void *p) {
 }
 
 // Copy the packed records of the last block to pinned staging.
+// cur_read ids (2 * read + 1) of the reads without a location, in read
+// order, from the device's bit list (mapper_cpe.c:1455-1458).
+static uint64_t unmapped_list(const swm_mapper *m, uint32_t *out, uint64_t cap, int *status) {
+    uint64_t nu = 0;
+    const uint64_t nh = (m->cur_n + 15) / 16;
+    for (uint64_t w = 0; w < nh; w++) {
+        uint32_t bits = m->h_unm[w];
+        while (bits) {
+            const uint32_t j = (uint32_t)__builtin_ctz(bits);
+            bits &= bits - 1;
+            const uint64_t rd = 16 * w + j;
+            if (rd >= m->cur_n) break;
+            if (nu < cap && out) out[nu] = (uint32_t)(2 * rd + 1);
+            else *status = SWM_ERR_OVERFLOW;
+            nu++;
+        }
+    }
+    return nu;
+}
+
 static int download_results(swm_mapper *m) {
     if (!m->have_result) return SWM_ERR_STATE;
     SWM_CUDA(cudaSetDevice(m->device));
@@ -2337,7 +2382,7 @@ static int download_results(swm_mapper *m) {
     if (!rc) rc = ensure_host((void **)&m->h_rw, &m->h_cap_rw, nrec, 4);
     if (!rc) rc = ensure_host((void **)&m->h_rb, &m->h_cap_rb, nrec, 4);
     if (!rc) rc = ensure_host((void **)&m->h_rl, &m->h_cap_rl, nrec, 4);
-    if (!rc) rc = ensure_host((void **)&m->h_nrec, &m->h_cap_items, nitems, 4);
+    if (!rc) rc = ensure_host((void **)&m->h_unm, &m->h_cap_items, nitems / 32 + 1, 2);
     if (rc) return rc;
     cudaStream_t st = m->st;
     if (nw) SWM_CUDA(cudaMemcpyAsync(m->h_w, m->b.out_w, nw * 4, cudaMemcpyDeviceToHost, st));
@@ -2347,9 +2392,10 @@ static int download_results(swm_mapper *m) {
         SWM_CUDA(cudaMemcpyAsync(m->h_rb, m->b.rec_boff, nrec * 4, cudaMemcpyDeviceToHost, st));
         SWM_CUDA(cudaMemcpyAsync(m->h_rl, m->b.rec_blen, nrec * 4, cudaMemcpyDeviceToHost, st));
     }
-    if (nitems) SWM_CUDA(cudaMemcpyAsync(m->h_nrec, m->b.it_nrec, nitems * 4, cudaMemcpyDeviceToHost, st));
+    const uint64_t nunm = (m->cur_n + 15) / 16;
+    if (nunm) SWM_CUDA(cudaMemcpyAsync(m->h_unm, m->b.unm, nunm * 2, cudaMemcpyDeviceToHost, st));
     SWM_CUDA(cudaStreamSynchronize(st));
-    m->stats.d2h_bytes = nw * 4 + nby + nrec * 12 + nitems * 4 + TOT_N * 4 + ST_N * 8;
+    m->stats.d2h_bytes = nw * 4 + nby + nrec * 12 + nunm * 2 + TOT_N * 4 + ST_N * 8;
     return SWM_OK;
 }
 
@@ -2377,17 +2423,9 @@ extern "C" int swm_map_fetch(swm_mapper *m, swm_result *r) {
             status = SWM_ERR_OVERFLOW;
         }
     }
-    uint64_t nu = 0;
-    for (uint64_t rd = 0; rd < m->cur_n; rd++) {
-        if (m->h_nrec[2 * rd] + m->h_nrec[2 * rd + 1] == 0) {
-            if (nu < r->unmapped_cap && r->unmapped) r->unmapped[nu] = (uint32_t)(2 * rd + 1);
-            else status = SWM_ERR_OVERFLOW;
-            nu++;
-        }
-    }
-    r->n_unmapped = nu;
+    r->n_unmapped = unmapped_list(m, r->unmapped, r->unmapped_cap, &status);
     if (status) swm_set_error("result buffers too small (records %llu, unmapped %llu)", (unsigned long long)nrec,
-                              (unsigned long long)nu);
+                              (unsigned long long)r->n_unmapped);
     return status;
 }
 
@@ -2400,29 +2438,22 @@ extern "C" int swm_map_fetch_packed(swm_mapper *m, swm_packed_result *r) {
         // page-locked caller buffers: copy the packed results straight into them
         SWM_CUDA(cudaSetDevice(m->device));
         const uint64_t nitems = 2 * m->cur_n;
-        int rc0 = ensure_host((void **)&m->h_nrec, &m->h_cap_items, nitems, 4);
+        int rc0 = ensure_host((void **)&m->h_unm, &m->h_cap_items, nitems / 32 + 1, 2);
         if (rc0) return rc0;
         cudaStream_t st = m->st;
         if (nw) SWM_CUDA(cudaMemcpyAsync(r->words, m->b.out_w, nw * 4, cudaMemcpyDeviceToHost, st));
         if (nby) SWM_CUDA(cudaMemcpyAsync(r->cigar, m->b.out_c, nby, cudaMemcpyDeviceToHost, st));
         if (nrec && r->record_cigar_len)
             SWM_CUDA(cudaMemcpyAsync(r->record_cigar_len, m->b.rec_blen, nrec * 4, cudaMemcpyDeviceToHost, st));
-        if (nitems) SWM_CUDA(cudaMemcpyAsync(m->h_nrec, m->b.it_nrec, nitems * 4, cudaMemcpyDeviceToHost, st));
+        const uint64_t nunm = (m->cur_n + 15) / 16;
+        if (nunm) SWM_CUDA(cudaMemcpyAsync(m->h_unm, m->b.unm, nunm * 2, cudaMemcpyDeviceToHost, st));
         SWM_CUDA(cudaStreamSynchronize(st));
-        m->stats.d2h_bytes = nw * 4 + nby + (r->record_cigar_len ? nrec * 4 : 0) + nitems * 4 + TOT_N * 4 + ST_N * 8;
+        m->stats.d2h_bytes = nw * 4 + nby + (r->record_cigar_len ? nrec * 4 : 0) + nunm * 2 + TOT_N * 4 + ST_N * 8;
         r->n_records = nrec;
         r->n_words = nw;
         r->n_cigar = nby;
         int status = SWM_OK;
-        uint64_t nu = 0;
-        for (uint64_t rd = 0; rd < m->cur_n; rd++) {
-            if (m->h_nrec[2 * rd] + m->h_nrec[2 * rd + 1] == 0) {
-                if (nu < r->unmapped_cap && r->unmapped) r->unmapped[nu] = (uint32_t)(2 * rd + 1);
-                else status = SWM_ERR_OVERFLOW;
-                nu++;
-            }
-        }
-        r->n_unmapped = nu;
+        r->n_unmapped = unmapped_list(m, r->unmapped, r->unmapped_cap, &status);
         return status;
     }
     int rc = download_results(m);
@@ -2440,15 +2471,7 @@ extern "C" int swm_map_fetch_packed(swm_mapper *m, swm_packed_result *r) {
         if (nby) memcpy(r->cigar, m->h_c, nby);
         if (r->record_cigar_len && nrec) memcpy(r->record_cigar_len, m->h_rl, nrec * 4);
     }
-    uint64_t nu = 0;
-    for (uint64_t rd = 0; rd < m->cur_n; rd++) {
-        if (m->h_nrec[2 * rd] + m->h_nrec[2 * rd + 1] == 0) {
-            if (nu < r->unmapped_cap && r->unmapped) r->unmapped[nu] = (uint32_t)(2 * rd + 1);
-            else status = SWM_ERR_OVERFLOW;
-            nu++;
-        }
-    }
-    r->n_unmapped = nu;
+    r->n_unmapped = unmapped_list(m, r->unmapped, r->unmapped_cap, &status);
     if (status) swm_set_error("packed result buffers too small (words %llu, bytes %llu, records %llu)",
                               (unsigned long long)nw, (unsigned long long)nby, (unsigned long long)nrec);
     return status;
