@@ -169,6 +169,16 @@ int swm_map_device(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
                    uint64_t reads_num, uint32_t errors, const uint8_t *d_errors);
 int swm_map_fetch(swm_mapper *m, swm_result *r);
 
+/* Asynchronous form of swm_map_device (no reference counterpart: the
+ * reference's reads are always host buffers): submit queues the block on the
+ * mapper's stream and returns; wait blocks until it is mapped (results stay
+ * on the device until swm_map_fetch). The device inputs must stay valid until
+ * wait returns. Two mappers used in turn keep the GPU busy while the host
+ * handles the other's results. */
+int swm_map_device_submit(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, uint64_t stride,
+                          uint64_t reads_num, uint32_t errors, const uint8_t *d_errors);
+int swm_map_device_wait(swm_mapper *m);
+
 /* Packed results: the same records without the reference's fixed strides
  * (record q's words follow record q - 1's; its CIGAR bytes likewise), for
  * callers that do not need the ref_info_t layout. */

@@ -84,6 +84,8 @@ def lib():
         L.swm_map_submit.argtypes = [vp, C.POINTER(Batch)]
         L.swm_map_wait.argtypes = [vp, C.POINTER(Result)]
         L.swm_map_device.argtypes = [vp, vp, vp, u64, u64, u32, vp]
+        L.swm_map_device_submit.argtypes = [vp, vp, vp, u64, u64, u32, vp]
+        L.swm_map_device_wait.argtypes = [vp]
         L.swm_map_fetch.argtypes = [vp, C.POINTER(Result)]
         L.swm_map_fetch_packed.argtypes = [vp, C.POINTER(PackedResult)]
         L.swm_map_wait_packed.argtypes = [vp, C.POINTER(PackedResult)]
@@ -232,6 +234,16 @@ class Mapper:
         """Map reads already resident in device memory (pointers as ints)."""
         _check(lib().swm_map_device(self._h, d_reads, d_lens, stride, nreads, errors, d_errors),
                "swm_map_device")
+
+    def submit_device(self, d_reads: int, d_lens: int, stride: int, nreads: int, errors: int,
+                      d_errors: int | None = None):
+        """Queue a block of device-resident reads and return (swm_map_device_submit)."""
+        _check(lib().swm_map_device_submit(self._h, d_reads, d_lens, stride, nreads, errors, d_errors),
+               "swm_map_device_submit")
+
+    def wait_device(self):
+        """Wait for the block queued by submit_device (swm_map_device_wait)."""
+        _check(lib().swm_map_device_wait(self._h), "swm_map_device_wait")
 
     def fetch(self, nreads: int, records_cap: int | None = None) -> MapOutput:
         res, ref_pos, cigar, unm = self._result(nreads, records_cap)

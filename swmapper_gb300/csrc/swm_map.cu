@@ -120,7 +120,10 @@ struct swm_mapper {
     const uint8_t *cur_e;
     uint64_t cur_stride, cur_n;
     uint32_t cur_errors;
-    int pending; // submitted, not yet waited
+    int pending; // submitted, not yet waited: 1 host inputs, 2 device inputs
+    const char *dev_reads;     // device inputs of a pending swm_map_device_submit
+    const uint32_t *dev_lens;
+    const uint8_t *dev_e;
     uint64_t h2d_pending; // bytes copied in for the block being mapped
     int have_result;
     uint32_t tot[TOT_N];
@@ -2327,6 +2330,40 @@ extern "C" int swm_map_device(swm_mapper *m, const char *d_reads, const uint32_t
     return run_block(m, d_reads, d_lens, stride, (uint32_t)reads_num, errors, d_errors, 0);
 }
 
+extern "C" int swm_map_device_submit(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, uint64_t stride,
+                                     uint64_t reads_num, uint32_t errors, const uint8_t *d_errors) {
+    if (!m || (!d_reads && reads_num) || (!d_lens && reads_num)) return SWM_ERR_ARG;
+    int rc = check_batch(m, reads_num, stride, errors);
+    if (rc) return rc;
+    SWM_CUDA(cudaSetDevice(m->device));
+    if (m->pending) return SWM_ERR_STATE;
+    m->have_result = 0;
+    m->dev_reads = d_reads;
+    m->dev_lens = d_lens;
+    m->dev_e = d_errors;
+    m->cur_stride = stride;
+    m->cur_n = reads_num;
+    m->cur_errors = errors;
+    rc = enqueue(m, d_reads, d_lens, stride, (uint32_t)reads_num, errors, d_errors);
+    if (!rc) rc = queue_totals(m);
+    if (rc) return rc;
+    m->pending = 2;
+    return SWM_OK;
+}
+
+extern "C" int swm_map_device_wait(swm_mapper *m) {
+    if (!m) return SWM_ERR_ARG;
+    if (m->pending != 2) return SWM_ERR_STATE;
+    SWM_CUDA(cudaSetDevice(m->device));
+    m->pending = 0;
+    int again = 0;
+    int rc = finish_block(m, (uint32_t)m->cur_n, 0, &again);
+    if (rc) return rc;
+    if (again) // a work buffer was too small: repeat the block
+        rc = run_block(m, m->dev_reads, m->dev_lens, m->cur_stride, (uint32_t)m->cur_n, m->cur_errors, m->dev_e, 1);
+    return rc;
+}
+
 static int ensure_host(void **p, uint64_t *cap, uint64_t need, size_t elt) {
     if (need <= *cap && *p) return SWM_OK;
     uint64_t n = need + need / 4 + 1024;
@@ -2540,7 +2577,7 @@ extern "C" int swm_map_submit(swm_mapper *m, const swm_batch *b) {
 
 extern "C" int swm_map_wait(swm_mapper *m, swm_result *r) {
     if (!m || !r) return SWM_ERR_ARG;
-    if (!m->pending) return SWM_ERR_STATE;
+    if (m->pending != 1) return SWM_ERR_STATE;
     SWM_CUDA(cudaSetDevice(m->device));
     m->pending = 0;
     int again = 0;
@@ -2557,7 +2594,7 @@ extern "C" int swm_map_wait(swm_mapper *m, swm_result *r) {
 
 extern "C" int swm_map_wait_packed(swm_mapper *m, swm_packed_result *r) {
     if (!m || !r) return SWM_ERR_ARG;
-    if (!m->pending) return SWM_ERR_STATE;
+    if (m->pending != 1) return SWM_ERR_STATE;
     SWM_CUDA(cudaSetDevice(m->device));
     m->pending = 0;
     int again = 0;

@@ -251,3 +251,58 @@ def test_gpu_pinned_buffers_direct_copy(cuda_lib):
         for a in arrs:
             rt.cudaHostUnregister(a.ctypes.data)
     assert got == want
+
+
+def test_gpu_device_submit_two_mappers(cuda_lib):
+    """swm_map_device_submit / swm_map_device_wait on two mappers in turn
+    (blocks overlapping on the GPU) give the same records and unmapped ids as
+    swm_map_device one block at a time."""
+    import ctypes
+    rt = None
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            rt = ctypes.CDLL(name)
+            break
+        except OSError:
+            pass
+    assert rt is not None
+    rt.cudaMalloc.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]
+    rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    rt.cudaFree.argtypes = [ctypes.c_void_p]
+    g = genome(3_000_000, 31, "human", nrun_min=2000, nrun_max=20000, copies_per_family=300)
+    reads, lens, _, _ = synth.reads(g, 6000, 150, 150, 0.03, seed=32)
+    ix = cuda_lib.Index.build(g)
+    d_reads, d_lens = ctypes.c_void_p(), ctypes.c_void_p()
+    assert rt.cudaMalloc(ctypes.byref(d_reads), reads.nbytes) == 0
+    assert rt.cudaMalloc(ctypes.byref(d_lens), lens.nbytes) == 0
+    try:
+        assert rt.cudaMemcpy(d_reads, reads.ctypes.data, reads.nbytes, 1) == 0
+        assert rt.cudaMemcpy(d_lens, lens.ctypes.data, lens.nbytes, 1) == 0
+        stride = reads.shape[1]
+        blk = [(b0, d_reads.value + b0 * stride, d_lens.value + b0 * 4) for b0 in (0, 2000, 4000)]
+
+        def out_of(m):
+            o = m.fetch(2000)
+            return o.records(), [int(x) for x in o.unmapped]
+
+        ref = cuda_lib.Mapper(ix, max_reads=2000)
+        want = []
+        for _, dr, dl in blk:
+            ref.map_device(dr, dl, stride, 2000, 7)
+            want.append(out_of(ref))
+        ma, mb = cuda_lib.Mapper(ix, max_reads=2000), cuda_lib.Mapper(ix, max_reads=2000)
+        got = [None] * 3
+        ma.submit_device(blk[0][1], blk[0][2], stride, 2000, 7)
+        mb.submit_device(blk[1][1], blk[1][2], stride, 2000, 7)
+        ma.wait_device()
+        got[0] = out_of(ma)
+        ma.submit_device(blk[2][1], blk[2][2], stride, 2000, 7)
+        mb.wait_device()
+        got[1] = out_of(mb)
+        ma.wait_device()
+        got[2] = out_of(ma)
+        assert got == want
+        assert any(u for _, u in want) and all(r for r, _ in want)
+    finally:
+        rt.cudaFree(d_reads)
+        rt.cudaFree(d_lens)
