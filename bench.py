@@ -40,11 +40,38 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-WORKLOAD = dict(workload="batched: 100 Mbp genome (41% GC, 10% repeat copies 300 bp-6 kb at 1% divergence), "
-                         "1,000,000 x 150 bp reads at 3% error, e=7, k=12",
-                genome_bp=100_000_000, genome_kind="repeats100m", genome_seed=20261203,
-                reads=1_000_000, read_len=150, error_rate=0.03, e=7, k=12, read_seed=7)
+# The reference's benchmark configurations (synthetic stand-ins with the same
+# shapes). "batched" is the headline line; the others are parity-test shapes
+# that bench.py can also time with --workload.
+WORKLOADS = {
+    "batched": dict(workload="batched: 100 Mbp genome (41% GC, 10% repeat copies 300 bp-6 kb at 1% divergence), "
+                             "1,000,000 x 150 bp reads at 3% error, e=7, k=12",
+                    genome_bp=100_000_000, genome_kind="repeats100m", genome_seed=20261203,
+                    reads=1_000_000, len_min=150, len_max=150, error_rate=0.03, e=7, k=12, read_seed=7,
+                    block=262144),
+    "plain": dict(workload="plain: 1 Mbp uniform genome, 10,000 x 100 bp reads at 2% error, e=5, k=12, "
+                           "blocks of 4,096 reads",
+                  genome_bp=1_000_000, genome_kind="uniform", genome_seed=1,
+                  reads=10_000, len_min=100, len_max=100, error_rate=0.02, e=5, k=12, read_seed=2, block=4096),
+    "uneven": dict(workload="uneven: 100 Mbp genome as batched, 2,000,000 reads of 50-250 bp at 4% error, "
+                            "per-read e=ceil(0.05 L), k=12",
+                   genome_bp=100_000_000, genome_kind="repeats100m", genome_seed=20261203,
+                   reads=2_000_000, len_min=50, len_max=250, error_rate=0.04, e=None, e_frac=0.05, k=12,
+                   read_seed=11, block=262144),
+    "human": dict(workload="human-scale: 3.1 Gbp genome (41% GC, 5% N in runs of 10 kb-1 Mb, 50% repeat families "
+                           "at 2-15% divergence), 10,000,000 x 150 bp reads at 3% error, e=7, k=12",
+                  genome_bp=3_100_000_000, genome_kind="human", genome_seed=31,
+                  reads=10_000_000, len_min=150, len_max=150, error_rate=0.03, e=7, k=12, read_seed=13,
+                  block=262144),
+}
+WORKLOADS["serving"] = dict(
+    workload="serving: index of the human-scale genome resident; Poisson arrivals of requests of log-uniform "
+             "[1, 4096] reads, 50-250 bp at 3% error, e=ceil(0.05 L); offered load 25/50/90% of the measured peak",
+    genome_bp=3_100_000_000, genome_kind="human", genome_seed=31, reads=1_000_000, len_min=50, len_max=250,
+    error_rate=0.03, e=None, e_frac=0.05, k=12, read_seed=17, block=65536, requests=3000)
+WORKLOAD = dict(WORKLOADS["batched"])
 METRIC = "mapped reads/s"
+L2_FLUSH_BYTES = 512 << 20   # > the 129 MB L2
 UNIT = "reads/s"
 
 
@@ -185,12 +212,21 @@ def profile_traffic(kernel):
 
 
 def make_workload(rank=0):
+    """Genome, reads, lengths and per-read thresholds (None: one e for all)."""
     from swmapper_gb300 import synth
     w = WORKLOAD
     g = synth.reference(w["genome_bp"], seed=w["genome_seed"], kind=w["genome_kind"])
-    reads, lens, _, _ = synth.reads(g, w["reads"], w["read_len"], w["read_len"], w["error_rate"],
+    reads, lens, _, _ = synth.reads(g, w["reads"], w["len_min"], w["len_max"], w["error_rate"],
                                     seed=shard_seed(rank))
-    return g, reads, lens
+    eper = None
+    if w.get("e") is None: # e = ceil(frac * L), at most the envelope's 15
+        eper = np.minimum(np.ceil(w["e_frac"] * lens.astype(np.float64) - 1e-9), 15).astype(np.uint8)
+    return g, reads, lens, eper
+
+
+def e_arg(eper):
+    """Scalar threshold passed with per-read ones (their maximum)."""
+    return int(eper.max()) if eper is not None and eper.size else int(WORKLOAD.get("e") or 0)
 
 
 # ------------------------------------------------------------ CPU legs
@@ -204,18 +240,32 @@ def host_map_index(arrays, k):
 
 
 CPU_BLOCK = 10_000   # reads per block of the reference's host loop (mapper_mpe.c:727)
+REF_WINDOW_BASES = 224  # 7 x 32 bases: the 16-word window slot of the reference verifier
 _cpu_bufs = {}
 
 
-def cpu_map(mix, reads, lens, e, threads):
+def cpu_map(mix, reads, lens, e, threads, eper=None):
     """Map on the host in blocks of 10,000 reads: the reference's own
     get_positions() when it was compiled here (kind 'reference'), else the
-    oracle restatement (kind 'port'). Returns (mapped reads, kind)."""
+    oracle restatement (kind 'port'). Per-read thresholds map each e group
+    on its own (the reference takes one e per call). Returns (mapped reads,
+    kind)."""
     from oracle import pyoracle as po
+    if eper is not None:
+        mapped, kinds = 0, set()
+        for ev in np.unique(eper):
+            idx = np.nonzero(eper == ev)[0]
+            mg, kd = cpu_map(mix, reads[idx], lens[idx], int(ev), threads)
+            mapped += mg
+            kinds.add(kd)
+        return mapped, "reference" if kinds == {"reference"} else "port"
     if "out" not in _cpu_bufs:
         _cpu_bufs["out"] = po.out_buffers(CPU_BLOCK)
     mapped = 0
-    kind = "reference" if po.have_ref() else "port"
+    # the reference's 16-word window slot holds L + 2e <= 224 (mapper_cpe.c:1600,1613); longer
+    # windows overflow it, so such reads run on the oracle restatement
+    in_env = reads.shape[0] == 0 or int(lens.max()) + 2 * e <= REF_WINDOW_BASES
+    kind = "reference" if po.have_ref() and in_env else "port"
     for b0 in range(0, reads.shape[0], CPU_BLOCK):
         r, ln = reads[b0:b0 + CPU_BLOCK], lens[b0:b0 + CPU_BLOCK]
         if kind == "reference":
@@ -227,15 +277,15 @@ def cpu_map(mix, reads, lens, e, threads):
     return mapped, kind
 
 
-def timed_cpu_sample(mix, reads, lens, e, threads, target_s):
+def timed_cpu_sample(mix, reads, lens, e, threads, target_s, eper=None):
     """Time a bounded sample sized to take about target_s seconds."""
     n = min(2048, reads.shape[0])
     t0 = time.perf_counter()
-    cpu_map(mix, reads[:n], lens[:n], e, threads)
+    cpu_map(mix, reads[:n], lens[:n], e, threads, None if eper is None else eper[:n])
     dt = max(time.perf_counter() - t0, 1e-3)
     n = int(min(reads.shape[0], max(n, n * target_s / dt)))
     t0 = time.perf_counter()
-    mapped, kind = cpu_map(mix, reads[:n], lens[:n], e, threads)
+    mapped, kind = cpu_map(mix, reads[:n], lens[:n], e, threads, None if eper is None else eper[:n])
     dt = time.perf_counter() - t0
     return mapped / dt, n, dt, kind
 
@@ -278,7 +328,8 @@ def run_gpu(args):
     rt = cudart()
     rt.cudaSetDevice(local)
     w = WORKLOAD
-    g, reads, lens = make_workload(rank)
+    g, reads, lens, eper = make_workload(rank)
+    E = e_arg(eper)
     t0 = time.perf_counter()
     ix = swm.Index.build(g, k=w["k"], device=local)
     index_build_s = time.perf_counter() - t0
@@ -290,6 +341,10 @@ def run_gpu(args):
     assert rt.cudaMalloc(C.byref(d_lens), lens.nbytes) == 0
     rt.cudaMemcpy(d_reads, reads.ctypes.data, reads.nbytes, 1)
     rt.cudaMemcpy(d_lens, lens.ctypes.data, lens.nbytes, 1)
+    d_e = C.c_void_p()
+    if eper is not None:
+        assert rt.cudaMalloc(C.byref(d_e), eper.nbytes) == 0
+        rt.cudaMemcpy(d_e, eper.ctypes.data, eper.nbytes, 1)
     # NMAP mappers (own stream and buffers each) take the blocks in turn, so
     # one block's gather-bound stages overlap another's ALU-bound ones
     mappers = [swm.Mapper(ix, max_reads=block) for _ in range(args.mappers)]
@@ -322,40 +377,60 @@ def run_gpu(args):
             if len(pend) == len(mappers):
                 drain()
             mm = mappers[i % len(mappers)]
-            mm.submit_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, nb, w["e"])
+            mm.submit_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, nb, E,
+                             d_e.value + b0 if eper is not None else None)
             pend.append(mm)
         while pend:
             drain()
+
+    inf = ix.info()
+    index_bytes = (2 * (4 << (2 * inf.k)) + 8 * inf.n_seeds + 4 * (inf.n_words2 + inf.n_words3))
+    input_bytes = reads.nbytes + lens.nbytes + index_bytes
+    flush = input_bytes < L2_FLUSH_BYTES  # small inputs: flush L2 between timed steps
+    d_flush = C.c_void_p()
+    if flush:
+        assert rt.cudaMalloc(C.byref(d_flush), L2_FLUSH_BYTES) == 0
+    rt.cudaMemsetAsync.argtypes = [C.c_void_p, C.c_int, C.c_size_t, C.c_void_p]
+
+    def timed(nsteps, acc):
+        """Device time of nsteps passes: ev0 on the first stream, which every
+        other stream waits for; ev1 after every stream's last block."""
+        rt.cudaDeviceSynchronize()
+        rt.cudaEventRecord(ev0, streams[0])
+        for sm in streams[1:]:
+            rt.cudaStreamWaitEvent(sm, ev0, 0)
+        run_steps(nsteps, acc)
+        for sm in streams[1:]:
+            rt.cudaEventRecord(evq, sm)
+            rt.cudaStreamWaitEvent(streams[0], evq, 0)
+        rt.cudaEventRecord(ev1, streams[0])
+        rt.cudaEventSynchronize(ev1)
+        rt.cudaDeviceSynchronize()
+        ms = C.c_float()
+        rt.cudaEventElapsedTime(C.byref(ms), ev0, ev1)
+        return ms.value / 1000.0
 
     run_steps(args.warmup, None)
     acc = {}
     clocks = ClockSampler(local)
     clocks.start()
     dist.barrier()
-    rt.cudaDeviceSynchronize()
-    # ev0 on the first stream, which every other stream waits for; ev1 after
-    # every stream's last block
-    rt.cudaEventRecord(ev0, streams[0])
-    for sm in streams[1:]:
-        rt.cudaStreamWaitEvent(sm, ev0, 0)
-    run_steps(args.steps, acc)
-    for sm in streams[1:]:
-        rt.cudaEventRecord(evq, sm)
-        rt.cudaStreamWaitEvent(streams[0], evq, 0)
-    rt.cudaEventRecord(ev1, streams[0])
-    rt.cudaEventSynchronize(ev1)
-    rt.cudaDeviceSynchronize()
+    if flush: # one step at a time, L2 flushed (outside the events) before each
+        elapsed = 0.0
+        for _ in range(args.steps):
+            rt.cudaMemsetAsync(d_flush, 1, L2_FLUSH_BYTES, streams[0])
+            elapsed += timed(1, acc)
+    else:
+        elapsed = timed(args.steps, acc)
     dist.barrier()
-    ms = C.c_float()
-    rt.cudaEventElapsedTime(C.byref(ms), ev0, ev1)
     clk = clocks.stop()
-    elapsed = ms.value / 1000.0
     tot_elapsed, tot_mapped, tot_cells = aggregate(dist, elapsed, [acc["mapped_reads"], acc["cells"]])
     value = tot_mapped / tot_elapsed
     # kernel times in isolation (one mapper, one block at a time) for the
     # stage breakdown and the roofline: one untimed pass over the reads
     for b0, nb in blocks:
-        m.map_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, nb, w["e"])
+        m.map_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, nb, E,
+                     d_e.value + b0 if eper is not None else None)
         for sname in STAGES:
             acc["ms_" + sname] = acc.get("ms_" + sname, 0.0) + m.stage_ms(sname) * args.steps
     gcups = tot_cells / tot_elapsed / 1e9
@@ -387,7 +462,8 @@ def run_gpu(args):
             b0, nb = blocks[i % len(blocks)]
             if len(pend) == 2:
                 drain()
-            mappers[i % 2].submit(reads[b0:b0 + nb], lens[b0:b0 + nb], w["e"])
+            mappers[i % 2].submit(reads[b0:b0 + nb], lens[b0:b0 + nb], E,
+                                  None if eper is None else eper[b0:b0 + nb])
             pend.append((i, mappers[i % 2]))
         while pend:
             drain()
@@ -410,7 +486,8 @@ def run_gpu(args):
 
     # roofline of the dominant kernel
     peak, peak_kind, peaks = measured_peaks()
-    L, e = w["read_len"], w["e"]
+    L = float(lens.mean())
+    e = E if eper is None else float(eper.mean())
     per_step = {k: v / args.steps for k, v in acc.items()}
     stage_rows = {}
     for sname in STAGES:
@@ -455,7 +532,10 @@ def run_gpu(args):
             "data": "synthetic (seeded genome and reads of the workload's shapes; no public dataset)",
             "config": {**WORKLOAD, "block_reads": block, "mappers": args.mappers,
                        "parallelism": f"replicas x{ws} (reads sharded by rank)",
-                       "l2": "inputs larger than L2 (reads 150 MB, index ~0.2 GB); no flush"},
+                       "l2": (f"inputs {input_bytes / 1e6:.0f} MB < L2: L2 flushed ({L2_FLUSH_BYTES >> 20} MiB write) "
+                              f"before each timed step" if flush else
+                              f"inputs larger than L2 (reads {reads.nbytes / 1e6:.0f} MB, index "
+                              f"{index_bytes / 1e9:.2f} GB); no flush")},
             "gcups": round(gcups, 2), "index_build_s": round(index_build_s, 3),
             "per_step": {k: int(v) if not k.startswith("ms_") else round(v, 3) for k, v in per_step.items()},
             "stages": stage_rows, "stage_timing": "kernel times of one mapper alone (untimed pass)",
@@ -465,7 +545,7 @@ def run_gpu(args):
         arrays = ix.download()
         mix = host_map_index(arrays, w["k"])
         threads = os.cpu_count() or 1
-        v, n, dt, kind = timed_cpu_sample(mix, reads, lens, w["e"], threads, args.cpu_seconds)
+        v, n, dt, kind = timed_cpu_sample(mix, reads, lens, E, threads, args.cpu_seconds, eper)
         line["cpu_baseline"] = {"value": round(v, 1), "unit": UNIT, "cores": threads, "kind": kind,
                                 "sample": f"first {n} reads of the workload, {dt:.1f} s, {threads} threads"}
     if rank == 0:
@@ -477,6 +557,94 @@ def count_mapped(buf, nreads):
     return nreads - int(buf.c.n_unmapped)
 
 
+# ------------------------------------------------------------ serving
+
+def run_serving(args):
+    """Batch latency under Poisson arrivals: one host thread coalesces the
+    requests that have arrived (up to one block of reads) and hands them to two
+    mappers in turn (swm_map_submit / swm_map_wait_packed); a request's latency
+    runs from its arrival to the return of the wait that delivers its records."""
+    import swmapper_gb300 as swm
+    ws, rank, local = dist_env()
+    rt = cudart()
+    rt.cudaSetDevice(local)
+    w = WORKLOAD
+    rng = np.random.default_rng(w["read_seed"])
+    g, reads, lens, eper = make_workload(rank)
+    t0 = time.perf_counter()
+    ix = swm.Index.build(g, k=w["k"], device=local)
+    index_build_s = time.perf_counter() - t0
+    del g
+    nreq = args.requests or w["requests"]
+    sizes = np.minimum(np.exp(rng.uniform(0.0, math.log(4096.0), nreq)).astype(np.int64), 4096)
+    sizes = np.maximum(sizes, 1)
+    starts = np.concatenate([[0], np.cumsum(sizes)[:-1]]) % max(1, reads.shape[0] - 4096)
+    block = args.block
+    mappers = [swm.Mapper(ix, max_reads=block) for _ in range(2)]
+    bufs = [swm.PackedBuffers(block) for _ in range(2)]
+
+    streams = [C.c_void_p(mm.stream()) for mm in mappers]
+    rt.cudaStreamQuery.argtypes = [C.c_void_p]
+
+    def serve(arrivals):
+        """Serve the requests at the given arrival offsets (s); returns the
+        latency of each and the span from the first arrival to the last reply."""
+        nq = len(arrivals)
+        lat = np.zeros(nq)
+        pend = []   # (mapper index, [request ids]), oldest first
+        nxt = 0
+        slot = 0
+        t_start = time.perf_counter()
+        done_t = t_start
+
+        def complete():
+            nonlocal done_t
+            j, ids = pend.pop(0)
+            mappers[j].wait_packed(bufs[j])
+            done_t = time.perf_counter()
+            for q in ids:
+                lat[q] = done_t - (t_start + arrivals[q])
+
+        while nxt < nq or pend:
+            now = time.perf_counter() - t_start
+            if nxt < nq and arrivals[nxt] <= now and len(pend) < 2:
+                # coalesce what has arrived, up to one block of reads
+                ids, n = [], 0
+                while nxt < nq and arrivals[nxt] <= now and n + sizes[nxt] <= block:
+                    ids.append(nxt)
+                    n += int(sizes[nxt])
+                    nxt += 1
+                sel = np.concatenate([np.arange(starts[q], starts[q] + sizes[q]) for q in ids])
+                mappers[slot].submit(reads[sel], lens[sel], e_arg(eper), None if eper is None else eper[sel])
+                pend.append((slot, ids))
+                slot ^= 1
+            elif pend and (len(pend) == 2 or nxt >= nq or rt.cudaStreamQuery(streams[pend[0][0]]) == 0):
+                complete()
+            elif not pend:
+                time.sleep(max(0.0, min(arrivals[nxt] - now, 0.0005)))
+        return lat, done_t - t_start
+
+    serve(np.zeros(min(nreq, 50)))  # warm-up
+    total_reads = int(sizes.sum())
+    _, span = serve(np.zeros(nreq))  # all requests at once: the peak
+    peak = total_reads / span
+    rows = []
+    for load in (0.25, 0.5, 0.9):
+        rate = load * peak / float(sizes.mean())           # requests per second
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+        lat, span = serve(arrivals)
+        rows.append({"load": load, "offered_reads_per_s": round(load * peak, 1),
+                     "sustained_reads_per_s": round(total_reads / span, 1),
+                     "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                     "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)})
+    line = {"metric": "batch latency p99 (serving)", "value": rows[-1]["p99_ms"], "unit": "ms", "n_gpus": 1,
+            "higher_is_better": False, "peak_reads_per_s": round(peak, 1), "loads": rows,
+            "requests": nreq, "reads_per_request_mean": round(float(sizes.mean()), 1),
+            "index_build_s": round(index_build_s, 3), "data": "synthetic",
+            "config": {**WORKLOAD, "block_reads": block, "mappers": 2}}
+    print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------ reference arm
 
 def run_reference(args):
@@ -486,7 +654,8 @@ def run_reference(args):
     from oracle import build as obuild
     from oracle import pyoracle as po
     w = WORKLOAD
-    g, reads, lens = make_workload(0)
+    g, reads, lens, eper = make_workload(0)
+    E = e_arg(eper)
     kind = "reference"
     t0 = time.perf_counter()
     exe = os.path.join(obuild.REF_DIR, "serial_index")
@@ -512,7 +681,7 @@ def run_reference(args):
     mix = host_map_index(arrays, w["k"])
     threads = os.cpu_count() or 1
     # size one step to ~args.ref_step_seconds
-    rate, n, _, kind2 = timed_cpu_sample(mix, reads, lens, w["e"], threads, 1.0)
+    rate, n, _, kind2 = timed_cpu_sample(mix, reads, lens, E, threads, 1.0, eper)
     kind = kind if kind2 == "reference" else "port"
     per_step = int(min(reads.shape[0], max(1024, rate * args.ref_step_seconds)))
     total_mapped = 0
@@ -522,7 +691,7 @@ def run_reference(args):
         lo = off % reads.shape[0]
         hi = min(reads.shape[0], lo + per_step)
         t0 = time.perf_counter()
-        mapped, _ = cpu_map(mix, reads[lo:hi], lens[lo:hi], w["e"], threads)
+        mapped, _ = cpu_map(mix, reads[lo:hi], lens[lo:hi], E, threads, None if eper is None else eper[lo:hi])
         dt = time.perf_counter() - t0
         off = hi
         if s >= args.warmup:
@@ -547,22 +716,32 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--block", type=int, default=262144, help="reads per mapping block")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batched",
+                    help="benchmark configuration (default: batched, the headline line)")
+    ap.add_argument("--block", type=int, default=None, help="reads per mapping block (default: the workload's)")
     ap.add_argument("--mappers", type=int, default=2, help="mappers taking the blocks in turn")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--genome-bp", type=int, default=WORKLOAD["genome_bp"], help="smaller genome for quick checks")
-    ap.add_argument("--nreads", type=int, default=WORKLOAD["reads"], help="fewer reads for quick checks")
+    ap.add_argument("--requests", type=int, default=None, help="requests of the serving workload")
+    ap.add_argument("--genome-bp", type=int, default=None, help="smaller genome for quick checks")
+    ap.add_argument("--nreads", type=int, default=None, help="fewer reads for quick checks")
     args = ap.parse_args()
-    if args.genome_bp != WORKLOAD["genome_bp"] or args.nreads != WORKLOAD["reads"]:
-        WORKLOAD.update(genome_bp=args.genome_bp, reads=args.nreads,
-                        workload=f"reduced check: {args.genome_bp} bp genome, {args.nreads} x 150 bp reads, e=7")
+    WORKLOAD.clear()
+    WORKLOAD.update(WORKLOADS[args.workload])
+    if args.block is None:
+        args.block = WORKLOAD["block"]
+    if args.genome_bp is not None or args.nreads is not None:
+        WORKLOAD.update(genome_bp=args.genome_bp or WORKLOAD["genome_bp"], reads=args.nreads or WORKLOAD["reads"])
+        WORKLOAD["workload"] = (f"reduced check of {args.workload}: {WORKLOAD['genome_bp']} bp genome, "
+                                f"{WORKLOAD['reads']} reads")
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_gpu(args)
 
