@@ -81,6 +81,7 @@ struct MapBufs {
     uint16_t *unm;       // bit j of halfword w: read 16 w + j has no location (cap_items / 32 + 1)
     uint32_t *tb_list;   // candidates that need a traceback (cap_cands)
     uint32_t *tb_cp;     // (VP, VN) at every 32-base block of each of them (cap_cands * 16)
+    uint32_t *plan_keys; // heap keys of items with more than PLAN_KEYS of them (cap_chunks)
     uint32_t *slow_list; // tracebacks whose route outgrew the fast path (cap_cands)
     // records
     uint32_t *out_w;  // cap_words
@@ -876,109 +877,166 @@ __device__ __forceinline__ uint32_t sel_slot(unsigned long long perm, uint32_t i
 // buckets need refills (some selected seed has more than 32 positions)
 // ======================================================================
 
-__global__ void __launch_bounds__(128) k_plan(uint32_t nitems, const unsigned long long *__restrict__ pl, MapBufs B,
-                                              uint64_t cap_chunks, uint64_t cap_elems) {
-    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
-        const uint32_t nref = B.it_nch[item];
-        if (nref == 0) continue; // one batch of initial chunks, set by k_seed
-        const uint32_t rb = B.it_choff[item], eb = B.it_eloff[item];
-        const uint32_t sbase = rb + item;
-        if ((uint64_t)rb + nref > cap_chunks) {
-            atomicOr(&B.tot[TOT_FLAGS], OV_CHUNKS);
-            B.it_nbat[item] = 0;
-            continue;
-        }
-        if ((uint64_t)eb + B.it_nel[item] > cap_elems) {
-            atomicOr(&B.tot[TOT_FLAGS], OV_ELEMS);
-            B.it_nbat[item] = 0;
-            continue;
-        }
-        const uint32_t ns = B.it_nsel[item];
-        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
-        const unsigned long long perm = B.it_perm[item];
-        uint32_t pc[SWM_MAX_SEL], sst[SWM_MAX_SEL], scn[SWM_MAX_SEL];
-        uint32_t hloc[SWM_MAX_SEL + 8], hidx[SWM_MAX_SEL + 8];
-        uint32_t hs = 0, rc = 0, e = 0, b = 0, br0 = 0, be0 = 0, npos = 0, runs = 0;
-        for (uint32_t i = 0; i < ns; i++) { // initial fetch of <= 32 per seed, 2194-2236
-            const uint2 sv = B.sel[sb + sel_slot(perm, i)];
-            sst[i] = sv.x;
-            scn[i] = sv.y;
-            const uint32_t get = scn[i] > SWM_PER_FETCH ? SWM_PER_FETCH : scn[i];
-            pc[i] = get;
-            e += get;
-            npos += get;
-            runs += get ? 1u : 0u;
-        }
-        for (uint32_t i = 0; i < ns; i++) { // seeds_heap_insert, 1919-1935 (keys: raw positions)
-            if (pc[i] != scn[i]) {
-                hs++;
-                hloc[hs] = (uint32_t)(pl[sst[i] + pc[i] - 1] >> 16);
-                hidx[hs] = i;
-                uint32_t q = hs;
-                while (q > 1) {
-                    const uint32_t t = q / 2;
-                    if (hloc[t] > hloc[q]) {
-                        uint32_t a = hloc[t];
-                        hloc[t] = hloc[q];
-                        hloc[q] = a;
-                        a = hidx[t];
-                        hidx[t] = hidx[q];
-                        hidx[q] = a;
-                    } else break;
-                    q = t;
+__device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, d);
+        if ((int)lane_id() >= d) v += t;
+    }
+    return v;
+}
+
+#define PLAN_WARPS 4
+#define PLAN_KEYS 512 // heap keys of an item held in shared memory; more go to global scratch
+
+struct PlanSmem {
+    uint32_t sst[SWM_MAX_SEL], scn[SWM_MAX_SEL], pc[SWM_MAX_SEL], koff[SWM_MAX_SEL + 1];
+    uint32_t hloc[SWM_MAX_SEL + 8], hidx[SWM_MAX_SEL + 8];
+    uint32_t key[PLAN_KEYS];
+};
+
+// One warp per item whose buckets need refills (a warp looks at 32 items at
+// a time and takes those with refills one by one). The heap keys (the raw
+// position of the last element of every chunk that leaves a seed with
+// positions to fetch: pl[start + 32 (j + 1) - 1] >> 16 for refill j) are all
+// known up front, so the lanes load them in parallel; lane 0 then runs the
+// seed heap of alignment_rmdup (2194-2419) on shared memory only.
+__global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(uint32_t nitems, const unsigned long long *__restrict__ pl,
+                                                          MapBufs B, uint64_t cap_chunks, uint64_t cap_elems) {
+    __shared__ PlanSmem sm_all[PLAN_WARPS];
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
+    PlanSmem &S = sm_all[wib];
+    for (uint32_t base = (blockIdx.x * PLAN_WARPS + wib) * 32; base < nitems; base += gridDim.x * PLAN_WARPS * 32) {
+        const uint32_t mine = base + lane < nitems ? B.it_nch[base + lane] : 0u;
+        uint32_t todo = __ballot_sync(0xffffffffu, mine != 0); // items without refills: one batch, set by k_seed
+        while (todo) {
+            const uint32_t t = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint32_t item = base + t;
+            const uint32_t nref = __shfl_sync(0xffffffffu, mine, t);
+            const uint32_t rb = B.it_choff[item], eb = B.it_eloff[item];
+            const uint32_t sbase = rb + item;
+            if ((uint64_t)rb + nref > cap_chunks || (uint64_t)eb + B.it_nel[item] > cap_elems) {
+                if (lane == 0) {
+                    atomicOr(&B.tot[TOT_FLAGS], (uint64_t)rb + nref > cap_chunks ? OV_CHUNKS : OV_ELEMS);
+                    B.it_nbat[item] = 0;
                 }
+                continue;
             }
-        }
-        for (;;) { // 2261-2419
-            if (hs > 0 && npos + SWM_PER_FETCH <= SWM_BATCH_POSITIONS && 1 + 2 * runs < SWM_MAX_RUNS_BLOCK) {
-                const uint32_t i = hidx[1];
-                const uint32_t left = scn[i] - pc[i];
-                const uint32_t get = left > SWM_PER_FETCH ? SWM_PER_FETCH : left;
-                B.ch_g[rb + rc] = sst[i] + pc[i];
-                B.ch_meta[rb + rc] = get | (i << 8);
-                rc++;
-                pc[i] += get;
-                e += get;
-                npos += get;
-                runs++;
-                // seeds_heap_pop_and_insert, 1936-1962 (loop bound i * 2 < size)
-                if (pc[i] == scn[i]) {
-                    hloc[1] = hloc[hs];
-                    hidx[1] = hidx[hs];
-                    hs--;
-                } else {
-                    hloc[1] = (uint32_t)(pl[sst[i] + pc[i] - 1] >> 16);
+            const uint32_t ns = B.it_nsel[item];
+            const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+            const unsigned long long perm = B.it_perm[item];
+            // seed records in rank order and the offsets of their keys
+            uint32_t carry = 0;
+            for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
+                const uint32_t i = i0 + lane;
+                uint32_t r = 0;
+                if (i < ns) {
+                    const uint2 sv = B.sel[sb + sel_slot(perm, i)];
+                    S.sst[i] = sv.x;
+                    S.scn[i] = sv.y;
+                    S.pc[i] = sv.y > SWM_PER_FETCH ? SWM_PER_FETCH : sv.y; // initial fetch, 2194-2236
+                    r = sv.y > SWM_PER_FETCH ? (sv.y - 1) / SWM_PER_FETCH : 0u;
                 }
-                uint32_t q = 1;
-                while (q * 2 < hs) {
-                    uint32_t t = q * 2;
-                    if (q * 2 + 1 <= hs && hloc[q * 2] > hloc[q * 2 + 1]) t = q * 2 + 1;
-                    if (hloc[t] < hloc[q]) {
-                        uint32_t a = hloc[t];
-                        hloc[t] = hloc[q];
-                        hloc[q] = a;
-                        a = hidx[t];
-                        hidx[t] = hidx[q];
-                        hidx[q] = a;
-                    } else break;
-                    q = t;
-                }
+                const uint32_t inc = warp_scan_incl(r);
+                if (i < ns) S.koff[i] = carry + inc - r;
+                carry += __shfl_sync(0xffffffffu, inc, 31);
             }
-            if (npos + SWM_PER_FETCH > SWM_BATCH_POSITIONS || hs == 0 || 1 + 2 * runs >= SWM_MAX_RUNS_BLOCK) {
-                if (npos > 0) {
-                    B.bt_c0[sbase + b] = rb + br0; // refill chunks of the batch; batch 0 also
-                    B.bt_c1[sbase + b] = rb + rc;  // holds every initial chunk
-                    B.bt_e0[sbase + b] = eb + be0;
-                    b++;
+            if (lane == 0) S.koff[ns] = carry; // == nref
+            __syncwarp();
+            uint32_t *keys = nref <= PLAN_KEYS ? S.key : B.plan_keys + rb;
+            for (uint32_t c = lane; c < nref; c += 32) {
+                uint32_t lo = 0, hi = ns; // seed with koff <= c < koff of the next
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (S.koff[mid] <= c) lo = mid;
+                    else hi = mid;
                 }
-                br0 = rc;
-                be0 = e;
-                npos = 0;
-                runs = 0;
-                if (hs == 0) break;
+                const uint32_t j = c - S.koff[lo];
+                keys[c] = (uint32_t)(pl[S.sst[lo] + SWM_PER_FETCH * (j + 1) - 1] >> 16);
             }
+            __syncwarp();
+            if (lane == 0) {
+                uint32_t hs = 0, rc = 0, e = 0, b = 0, br0 = 0, be0 = 0, npos = 0, runs = 0;
+                for (uint32_t i = 0; i < ns; i++) {
+                    e += S.pc[i];
+                    npos += S.pc[i];
+                    runs += S.pc[i] ? 1u : 0u;
+                }
+                auto key_of = [&](uint32_t i) { return keys[S.koff[i] + S.pc[i] / SWM_PER_FETCH - 1]; };
+                for (uint32_t i = 0; i < ns; i++) { // seeds_heap_insert, 1919-1935 (keys: raw positions)
+                    if (S.pc[i] != S.scn[i]) {
+                        hs++;
+                        S.hloc[hs] = key_of(i);
+                        S.hidx[hs] = i;
+                        uint32_t q = hs;
+                        while (q > 1) {
+                            const uint32_t t = q / 2;
+                            if (S.hloc[t] > S.hloc[q]) {
+                                uint32_t a = S.hloc[t];
+                                S.hloc[t] = S.hloc[q];
+                                S.hloc[q] = a;
+                                a = S.hidx[t];
+                                S.hidx[t] = S.hidx[q];
+                                S.hidx[q] = a;
+                            } else break;
+                            q = t;
+                        }
+                    }
+                }
+                for (;;) { // 2261-2419
+                    if (hs > 0 && npos + SWM_PER_FETCH <= SWM_BATCH_POSITIONS && 1 + 2 * runs < SWM_MAX_RUNS_BLOCK) {
+                        const uint32_t i = S.hidx[1];
+                        const uint32_t left = S.scn[i] - S.pc[i];
+                        const uint32_t get = left > SWM_PER_FETCH ? SWM_PER_FETCH : left;
+                        B.ch_g[rb + rc] = S.sst[i] + S.pc[i];
+                        B.ch_meta[rb + rc] = get | (i << 8);
+                        rc++;
+                        S.pc[i] += get;
+                        e += get;
+                        npos += get;
+                        runs++;
+                        // seeds_heap_pop_and_insert, 1936-1962 (loop bound i * 2 < size)
+                        if (S.pc[i] == S.scn[i]) {
+                            S.hloc[1] = S.hloc[hs];
+                            S.hidx[1] = S.hidx[hs];
+                            hs--;
+                        } else {
+                            S.hloc[1] = key_of(i);
+                        }
+                        uint32_t q = 1;
+                        while (q * 2 < hs) {
+                            uint32_t t = q * 2;
+                            if (q * 2 + 1 <= hs && S.hloc[q * 2] > S.hloc[q * 2 + 1]) t = q * 2 + 1;
+                            if (S.hloc[t] < S.hloc[q]) {
+                                uint32_t a = S.hloc[t];
+                                S.hloc[t] = S.hloc[q];
+                                S.hloc[q] = a;
+                                a = S.hidx[t];
+                                S.hidx[t] = S.hidx[q];
+                                S.hidx[q] = a;
+                            } else break;
+                            q = t;
+                        }
+                    }
+                    if (npos + SWM_PER_FETCH > SWM_BATCH_POSITIONS || hs == 0 || 1 + 2 * runs >= SWM_MAX_RUNS_BLOCK) {
+                        if (npos > 0) {
+                            B.bt_c0[sbase + b] = rb + br0; // refill chunks of the batch; batch 0 also
+                            B.bt_c1[sbase + b] = rb + rc;  // holds every initial chunk
+                            B.bt_e0[sbase + b] = eb + be0;
+                            b++;
+                        }
+                        br0 = rc;
+                        be0 = e;
+                        npos = 0;
+                        runs = 0;
+                        if (hs == 0) break;
+                    }
+                }
+                B.it_nbat[item] = b;
+            }
+            __syncwarp();
         }
-        B.it_nbat[item] = b;
     }
 }
 
@@ -1010,15 +1068,6 @@ struct CandSmem {
     uint32_t st[SWM_MAX_SEL];    // bucket start of each selected seed
     uint32_t cn[SWM_MAX_SEL];    // bucket count of each selected seed
 };
-
-__device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        uint32_t t = __shfl_up_sync(0xffffffffu, v, d);
-        if ((int)lane_id() >= d) v += t;
-    }
-    return v;
-}
 
 #define CAND_WARPS 8
 
@@ -1955,7 +2004,7 @@ static void free_bufs(MapBufs &B) {
     void *ps[] = {B.it_w, B.sel, B.sel_fl, B.it_perm, B.unm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
-                  B.cc_item, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
+                  B.cc_item, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
                   B.tb_cp, B.slow_list,
                   B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
     for (void *p : ps) cudaFree(p);
@@ -1998,7 +2047,7 @@ static int alloc_items(swm_mapper *m) {
 static int alloc_work(swm_mapper *m) {
     MapBufs &B = m->b;
     int rc = SWM_OK;
-    cudaFree(B.ch_g); cudaFree(B.ch_meta); cudaFree(B.bt_c0); cudaFree(B.bt_c1); cudaFree(B.bt_e0);
+    cudaFree(B.ch_g); cudaFree(B.ch_meta); cudaFree(B.plan_keys); cudaFree(B.bt_c0); cudaFree(B.bt_c1); cudaFree(B.bt_e0);
     cudaFree(B.bt_cnt); cudaFree(B.sort_scratch); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
     cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
     cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
@@ -2006,6 +2055,7 @@ static int alloc_work(swm_mapper *m) {
     cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
     rc |= dmalloc(&B.ch_g, m->cap_chunks);
     rc |= dmalloc(&B.ch_meta, m->cap_chunks);
+    rc |= dmalloc(&B.plan_keys, m->cap_chunks);
     rc |= dmalloc(&B.bt_c0, m->cap_chunks + m->cap_items);
     rc |= dmalloc(&B.bt_c1, m->cap_chunks + m->cap_items);
     rc |= dmalloc(&B.bt_e0, m->cap_chunks + m->cap_items);
@@ -2135,7 +2185,8 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     rc = swm_exclusive_scan(B.it_nel, B.it_eloff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_ELEMS, st);
     if (rc) return rc;
     m->launches += 6;
-    k_plan<<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, ix->d_pl, B, m->cap_chunks, m->cap_elems);
+    k_plan<<<grid_cap(nitems, PLAN_WARPS * 32, 16), PLAN_WARPS * 32, 0, st>>>(
+        nitems, ix->d_pl, B, m->cap_chunks, m->cap_elems);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[2], st));
