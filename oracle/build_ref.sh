@@ -12,6 +12,8 @@
 #   serial_index           serial_index.c with D1 + D2
 #   libswref.so            mapper_cpe.c:78-133,214-660,1244-2590 with D1,D4,D6,
 #                          DMA as memcpy and faaw as an atomic fetch-add
+#   libswref_sam.so        mapper_mpe.c:31-69,315-687 (the SAM writer) with
+#                          gzwrite / gzprintf appending to a memory buffer
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF_DIR="${REF_DIR:-/root/reference}"
@@ -42,6 +44,9 @@ if [ -f "$REF_DIR/serial_index.c" ] && [ -f "$REF_DIR/mapper_cpe.c" ]; then
       -e 's/if(sum_err==err) break;/if(sum_err==err) break; if(match_site < 0) break;/' \
       -e 's/^\( *\)sindex_t pre_small = invalid_value;/\1if (heap_size == 0) { pos_ind[0] = 0; return 1; }\n\1sindex_t pre_small = invalid_value;/' \
       > "$SRC/mapper_ref.c"
+  # SAM writer: tags and formatting constants, sam_header .. sam_format_2
+  { sed -n '31,69p' "$REF_DIR/mapper_mpe.c"
+    sed -n '315,687p' "$REF_DIR/mapper_mpe.c"; } > "$SRC/sam_ref.c"
 fi
 
 if [ ! -f "$SRC/mapper_ref.c" ]; then
@@ -56,4 +61,9 @@ $CC $CFLAGS -fPIC -ftrivial-auto-var-init=zero -I"$SHIM" -I"$SRC" -include "$SHI
     -c "$SRC/mapper_ref.c" -o "$OUT/mapper_ref.o"
 $CC $CFLAGS -fPIC -I"$SHIM" -I"$SRC" -c "$SHIM/mapper_driver.c" -o "$OUT/mapper_driver.o"
 $CC -shared -o "$OUT/libswref.so" "$OUT/mapper_ref.o" "$OUT/mapper_driver.o" -lpthread
+if [ -f "$SRC/sam_ref.c" ]; then
+  $CC $CFLAGS -fPIC -I"$SHIM" -I"$SRC" -include "$SHIM/sam_prelude.h" -c "$SRC/sam_ref.c" -o "$OUT/sam_ref.o"
+  $CC $CFLAGS -fPIC -I"$SHIM" -I"$SRC" -c "$SHIM/sam_driver.c" -o "$OUT/sam_driver.o"
+  $CC -shared -o "$OUT/libswref_sam.so" "$OUT/sam_ref.o" "$OUT/sam_driver.o"
+fi
 echo "build_ref: ok"

@@ -23,7 +23,7 @@ BIN_MAP = os.path.join(PKG, "swm_mapper")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["swm_index.cu", "swm_map.cu"]
-HOST_SOURCES = ["swm_files.c"]
+HOST_SOURCES = ["swm_files.c", "swm_sam.c"]
 
 
 def _run(cmd: list[str], cwd: str | None = None) -> None:
@@ -59,7 +59,8 @@ def build_cuda() -> str:
     nvcc = _nvcc()
     objdir = os.path.join(PKG, "_build")
     os.makedirs(objdir, exist_ok=True)
-    headers = [os.path.join(INCLUDE, "swmapper.h"), os.path.join(CSRC, "swm_common.cuh")]
+    headers = [os.path.join(INCLUDE, "swmapper.h"), os.path.join(INCLUDE, "swm_sam.h"),
+               os.path.join(CSRC, "swm_common.cuh")]
     objs = []
     jobs = []
     for s in CUDA_SOURCES:
@@ -82,14 +83,26 @@ def build_cuda() -> str:
     return LIB_CUDA
 
 
+def _have_zlib() -> bool:
+    """zlib headers and library present (the mapper CLI then writes .sam.gz)."""
+    probe = subprocess.run(["gcc", "-x", "c", "-", "-lz", "-o", os.devnull],
+                           input="#include <zlib.h>\nint main(void){return zlibVersion()==0;}\n",
+                           capture_output=True, text=True)
+    return probe.returncode == 0
+
+
 def build_cli() -> None:
+    """swm_index and swm_mapper, the drop-ins for serial_index and the mapper."""
+    zl = _have_zlib()
     for name, out in (("cli_index.c", BIN_INDEX), ("cli_mapper.c", BIN_MAP)):
         src = os.path.join(CSRC, name)
         if not os.path.exists(src):
             continue
-        if not _newer(out, [src, LIB_CUDA, os.path.join(INCLUDE, "swmapper.h")]):
-            _run(["gcc", "-O2", "-std=gnu11", "-I", INCLUDE, src, "-o", out,
-                  "-L", PKG, "-lswmapper_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread"])
+        if not _newer(out, [src, LIB_CUDA, os.path.join(INCLUDE, "swmapper.h"), os.path.join(INCLUDE, "swm_sam.h")]):
+            extra = ["-DHAVE_ZLIB"] if (zl and name == "cli_mapper.c") else []
+            libs = ["-lz"] if extra else []
+            _run(["gcc", "-O2", "-std=gnu11", *extra, "-I", INCLUDE, src, "-o", out,
+                  "-L", PKG, "-lswmapper_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread", *libs])
 
 
 def build_all() -> None:
