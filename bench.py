@@ -384,7 +384,7 @@ def run_gpu(args):
             drain()
 
     inf = ix.info()
-    index_bytes = (2 * (4 << (2 * inf.k)) + 8 * inf.n_seeds + 4 * (inf.n_words2 + inf.n_words3))
+    index_bytes = (2 * (4 << (2 * inf.k)) + 6 * inf.n_seeds + 4 * (inf.n_words2 + inf.n_words3))
     input_bytes = reads.nbytes + lens.nbytes + index_bytes
     flush = input_bytes < L2_FLUSH_BYTES  # small inputs: flush L2 between timed steps
     d_flush = C.c_void_p()

@@ -34,7 +34,8 @@ struct swm_index {
     uint64_t n, n_seeds, n_words2, n_words3, ref_length;
     uint32_t *d_count;     // 4^k
     uint32_t *d_off;       // 4^k + 1 start offsets (mapper_mpe.c:250-255)
-    unsigned long long *d_pl; // n_seeds (+8): position << 16 | lseed, bucket order
+    uint32_t *d_pos;       // n_seeds (+8): positions, bucket order (.positions)
+    uint16_t *d_ls;        // n_seeds (+8): their 12-bit flank codes (.pos_lseeds)
     uint32_t *d_b2;        // n_words2 + SWM_PAD_WORDS
     uint32_t *d_b3;        // n_words3 + SWM_PAD_WORDS
 };

@@ -12,9 +12,8 @@
 //   kb_sort_*   per-bucket sort of the keys: positions are unique, so sorting
 //               each bucket restores the ascending order the reference's
 //               serial scatter produces
-//   The sorted keys stay resident as the mapper's index (one 8-byte load per
-//   position and flank code); kb_split / kb_pack convert to and from the
-//   reference's separate .positions (u32) and .pos_lseeds (u16) files.
+//   kb_split    the sorted keys into the resident index: positions (u32) and
+//               flank codes (u16), the layout of .positions / .pos_lseeds
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -357,12 +356,6 @@ __global__ void kb_split(const unsigned long long *__restrict__ keys, uint64_t S
     }
 }
 
-__global__ void kb_pack(const uint32_t *__restrict__ pos, const uint16_t *__restrict__ lseed, uint64_t S,
-                        unsigned long long *__restrict__ keys) {
-    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < S; j += (uint64_t)gridDim.x * blockDim.x)
-        keys[j] = ((unsigned long long)pos[j] << 16) | lseed[j];
-}
-
 // ----------------------------------------------------------- host helpers
 
 static int sm_count(int device) {
@@ -382,7 +375,8 @@ static void index_release(swm_index *ix) {
     if (!ix) return;
     cudaFree(ix->d_count);
     cudaFree(ix->d_off);
-    cudaFree(ix->d_pl);
+    cudaFree(ix->d_pos);
+    cudaFree(ix->d_ls);
     cudaFree(ix->d_b2);
     cudaFree(ix->d_b3);
     free(ix);
@@ -418,7 +412,10 @@ static int build_on_device(const uint8_t *d_seq, uint64_t n, uint32_t k, int dev
     ix->ref_length = ix->n_words2 * 4 * 16;
     cudaStream_t st = 0;
     uint32_t *d_s2 = nullptr, *d_cursor = nullptr, *d_tmp = nullptr, *d_lists = nullptr, *d_nlist = nullptr;
+    unsigned long long *d_keys = nullptr; // position << 16 | lseed: sorting these sorts positions in a bucket
     auto cleanup = [&]() {
+        cudaFree(d_keys);
+        d_keys = nullptr;
         cudaFree(d_s2);
         cudaFree(d_cursor);
         cudaFree(d_tmp);
@@ -465,9 +462,7 @@ static int build_on_device(const uint8_t *d_seq, uint64_t n, uint32_t k, int dev
     CUC(cudaStreamSynchronize(st));
     const uint64_t S = S32;
     ix->n_seeds = S;
-    TRYC(dalloc(&ix->d_pl, S + 8));
-    CUC(cudaMemsetAsync(ix->d_pl + S, 0, 8 * 8, st));
-    unsigned long long *d_keys = ix->d_pl;
+    TRYC(dalloc(&d_keys, S + 8));
     if (S) {
         CUC(cudaMemcpyAsync(d_cursor, ix->d_off, nb * 4, cudaMemcpyDeviceToDevice, st));
         kb_scatter<<<grid_for(T, 256, device, 16), 256, 0, st>>>(ix->d_b2, ix->d_b3, d_s2, T, k, d_cursor, d_keys);
@@ -524,6 +519,14 @@ static int build_on_device(const uint8_t *d_seq, uint64_t n, uint32_t k, int dev
         }
         CUC(cudaGetLastError());
     }
+    // the mapper reads the two halves separately: flank codes for every
+    // fetched entry, positions only for the entries the flank filter keeps
+    TRYC(dalloc(&ix->d_pos, S + 8));
+    TRYC(dalloc(&ix->d_ls, S + 8));
+    CUC(cudaMemsetAsync(ix->d_pos + S, 0, 8 * 4, st));
+    CUC(cudaMemsetAsync(ix->d_ls + S, 0, 8 * 2, st));
+    if (S) kb_split<<<grid_for(S, 256, device, 16), 256, 0, st>>>(d_keys, S, ix->d_pos, ix->d_ls);
+    CUC(cudaGetLastError());
     CUC(cudaStreamSynchronize(st));
     cleanup();
     *out = ix;
@@ -584,24 +587,10 @@ extern "C" int swm_index_download(const swm_index *ix, uint32_t *hash_count, uin
         SWM_CUDA(cudaMemcpy(hash_offset_end, ix->d_off + 1, nb * 4, cudaMemcpyDeviceToHost));
         hash_offset_end[nb] = (uint32_t)ix->n_seeds;
     }
-    if ((positions || pos_lseeds) && ix->n_seeds) {
-        uint32_t *d_p = nullptr;
-        uint16_t *d_l = nullptr;
-        if ((positions && dalloc(&d_p, ix->n_seeds)) || (pos_lseeds && dalloc(&d_l, ix->n_seeds))) {
-            cudaFree(d_p);
-            return SWM_ERR_OOM;
-        }
-        kb_split<<<grid_for(ix->n_seeds, 256, ix->device, 16), 256>>>(ix->d_pl, ix->n_seeds, d_p, d_l);
-        cudaError_t e1 = cudaGetLastError();
-        if (e1 == cudaSuccess && positions) e1 = cudaMemcpy(positions, d_p, ix->n_seeds * 4, cudaMemcpyDeviceToHost);
-        if (e1 == cudaSuccess && pos_lseeds) e1 = cudaMemcpy(pos_lseeds, d_l, ix->n_seeds * 2, cudaMemcpyDeviceToHost);
-        cudaFree(d_p);
-        cudaFree(d_l);
-        if (e1 != cudaSuccess) {
-            swm_set_error("index download: %s", cudaGetErrorString(e1));
-            return SWM_ERR_CUDA;
-        }
-    }
+    if (positions && ix->n_seeds)
+        SWM_CUDA(cudaMemcpy(positions, ix->d_pos, ix->n_seeds * 4, cudaMemcpyDeviceToHost));
+    if (pos_lseeds && ix->n_seeds)
+        SWM_CUDA(cudaMemcpy(pos_lseeds, ix->d_ls, ix->n_seeds * 2, cudaMemcpyDeviceToHost));
     if (base_2bits && ix->n_words2)
         SWM_CUDA(cudaMemcpy(base_2bits, ix->d_b2, ix->n_words2 * 4, cudaMemcpyDeviceToHost));
     if (base_3bits && ix->n_words3)
@@ -692,31 +681,27 @@ extern "C" int swm_index_open(const char *prefix, uint32_t k, int device, swm_in
             uint64_t t = swmf_ref_info_total((const char *)info, ninfo);
             if (t) ix->n = t;
         }
-        uint32_t *d_tmp = nullptr, *d_p = nullptr;
-        uint16_t *d_l = nullptr;
-        if (dalloc(&ix->d_count, nb) || dalloc(&ix->d_off, nb + 1) || dalloc(&ix->d_pl, S + 8) ||
-            dalloc(&d_p, S) || dalloc(&d_l, S) || dalloc(&ix->d_b2, ix->n_words2 + SWM_PAD_WORDS) ||
+        uint32_t *d_tmp = nullptr;
+        if (dalloc(&ix->d_count, nb) || dalloc(&ix->d_off, nb + 1) || dalloc(&ix->d_pos, S + 8) ||
+            dalloc(&ix->d_ls, S + 8) || dalloc(&ix->d_b2, ix->n_words2 + SWM_PAD_WORDS) ||
             dalloc(&ix->d_b3, ix->n_words3 + SWM_PAD_WORDS) || dalloc(&d_tmp, swm_scan_tmp_words(nb))) {
             rc = SWM_ERR_OOM;
         } else if (cudaMemcpy(ix->d_count, cnt, nb * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-                   (S && cudaMemcpy(d_p, pos, S * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
-                   (S && cudaMemcpy(d_l, ls, S * 2, cudaMemcpyHostToDevice) != cudaSuccess) ||
+                   (S && cudaMemcpy(ix->d_pos, pos, S * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
+                   (S && cudaMemcpy(ix->d_ls, ls, S * 2, cudaMemcpyHostToDevice) != cudaSuccess) ||
                    (nb2 && cudaMemcpy(ix->d_b2, b2, nb2, cudaMemcpyHostToDevice) != cudaSuccess) ||
                    (nb3 && cudaMemcpy(ix->d_b3, b3, nb3, cudaMemcpyHostToDevice) != cudaSuccess) ||
-                   cudaMemset(ix->d_pl + S, 0, 64) != cudaSuccess ||
+                   cudaMemset(ix->d_pos + S, 0, 32) != cudaSuccess || cudaMemset(ix->d_ls + S, 0, 16) != cudaSuccess ||
                    cudaMemset(ix->d_b2 + ix->n_words2, 0, SWM_PAD_WORDS * 4) != cudaSuccess ||
                    cudaMemset(ix->d_b3 + ix->n_words3, 0, SWM_PAD_WORDS * 4) != cudaSuccess) {
             swm_set_error("H2D of index under %s failed", prefix);
             rc = SWM_ERR_CUDA;
         } else {
-            if (S) kb_pack<<<grid_for(S, 256, device, 16), 256>>>(d_p, d_l, S, ix->d_pl);
             // hash_offset rebuilt from the counts (mapper_mpe.c:250-255)
             rc = swm_exclusive_scan(ix->d_count, ix->d_off, nullptr, nb, nb, d_tmp, nullptr, 0);
             if (rc == SWM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = SWM_ERR_CUDA;
         }
         cudaFree(d_tmp);
-        cudaFree(d_p);
-        cudaFree(d_l);
         if (rc != SWM_OK) {
             index_release(ix);
             ix = nullptr;

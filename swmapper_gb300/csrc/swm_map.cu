@@ -898,10 +898,10 @@ struct PlanSmem {
 // One warp per item whose buckets need refills (a warp looks at 32 items at
 // a time and takes those with refills one by one). The heap keys (the raw
 // position of the last element of every chunk that leaves a seed with
-// positions to fetch: pl[start + 32 (j + 1) - 1] >> 16 for refill j) are all
+// positions to fetch: pos[start + 32 (j + 1) - 1] for refill j) are all
 // known up front, so the lanes load them in parallel; lane 0 then runs the
 // seed heap of alignment_rmdup (2194-2419) on shared memory only.
-__global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(uint32_t nitems, const unsigned long long *__restrict__ pl,
+__global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(uint32_t nitems, const uint32_t *__restrict__ pos,
                                                           MapBufs B, uint64_t cap_chunks, uint64_t cap_elems) {
     __shared__ PlanSmem sm_all[PLAN_WARPS];
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
@@ -953,7 +953,7 @@ __global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(uint32_t nitems, const
                     else hi = mid;
                 }
                 const uint32_t j = c - S.koff[lo];
-                keys[c] = (uint32_t)(pl[S.sst[lo] + SWM_PER_FETCH * (j + 1) - 1] >> 16);
+                keys[c] = pos[S.sst[lo] + SWM_PER_FETCH * (j + 1) - 1];
             }
             __syncwarp();
             if (lane == 0) {
@@ -1044,10 +1044,13 @@ __global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(uint32_t nitems, const
 // k_cand: one warp per batch slot -- gather, adjust, filter, sort-unique
 // ======================================================================
 
-__device__ __forceinline__ void warp_sort_small(uint32_t &v) {
+// Bitonic sort of the first K lanes' values (K = 2..32, lanes >= K hold
+// 0xffffffff): the network's first group of K lanes ends ascending.
+template <int K>
+__device__ __forceinline__ void warp_sort_k(uint32_t &v) {
     const uint32_t lane = lane_id();
 #pragma unroll
-    for (int size = 2; size <= 32; size <<= 1) {
+    for (int size = 2; size <= K; size <<= 1) {
 #pragma unroll
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
             uint32_t w = __shfl_xor_sync(0xffffffffu, v, stride);
@@ -1058,7 +1061,19 @@ __device__ __forceinline__ void warp_sort_small(uint32_t &v) {
     }
 }
 
+// Ascending sort of the values of lanes 0 .. n - 1 (n <= 32, uniform).
+__device__ __forceinline__ void warp_sort_small(uint32_t &v, uint32_t n) {
+    if (n <= 1) return;
+    if (n <= 2) warp_sort_k<2>(v);
+    else if (n <= 4) warp_sort_k<4>(v);
+    else if (n <= 8) warp_sort_k<8>(v);
+    else if (n <= 16) warp_sort_k<16>(v);
+    else warp_sort_k<32>(v);
+}
+
 #define CAND_MAXCH 128 // chunks (runs) per batch: block_size < 256 allows at most 128
+
+#define CAND_SMEM_KEEP 64 // batches of up to this many elements keep their survivors in shared memory
 
 struct CandSmem {
     uint32_t g[CAND_MAXCH];      // first global index of each chunk
@@ -1067,21 +1082,22 @@ struct CandSmem {
     uint32_t sel[SWM_MAX_SEL];   // base | shift << 16 | rl << 20 | rh << 24
     uint32_t st[SWM_MAX_SEL];    // bucket start of each selected seed
     uint32_t cn[SWM_MAX_SEL];    // bucket count of each selected seed
+    uint32_t sc[CAND_SMEM_KEEP]; // kept positions of a batch of <= CAND_SMEM_KEEP elements
 };
 
 #define CAND_WARPS 8
 
 // One warp per item, every batch of the item: element-parallel gather of
 // (position, flank code) pairs, position adjust, flank filter, sort-unique.
-__global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(uint32_t nitems, const unsigned long long *__restrict__ pl,
-                                                             MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
-                                                             uint32_t klong) {
+__global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(uint32_t nitems, const uint32_t *__restrict__ pos,
+                                                             const uint16_t *__restrict__ lsd, MapBufs B,
+                                                             uint64_t cap_chunks, uint64_t cap_elems, uint32_t klong) {
     __shared__ CandSmem sm_all[CAND_WARPS];
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     CandSmem &S = sm_all[wib];
     const uint32_t lt = (1u << lane) - 1;
-    uint32_t *scratch = B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS;
+    uint32_t *gscratch = B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS;
     for (uint32_t item = blockIdx.x * CAND_WARPS + wib; item < nitems; item += gridDim.x * CAND_WARPS) {
         const uint32_t nb = B.it_nbat[item];
         uint32_t total = 0;
@@ -1145,6 +1161,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(uint32_t nitems, co
                 const uint32_t E = carry;
                 if (lane == 0) S.start[nchk] = (uint16_t)E;
                 __syncwarp();
+                uint32_t *scratch = E <= CAND_SMEM_KEEP ? S.sc : gscratch;
                 uint32_t kept = 0;
                 for (uint32_t eb = 0; eb < E; eb += 32) {
                     const uint32_t el = eb + lane;
@@ -1162,11 +1179,13 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(uint32_t nitems, co
                         const uint32_t sm = S.sel[S.meta[q] >> 8];
                         const uint32_t base = sm & 0xffffu, shift = (sm >> 16) & 0xfu, rl = (sm >> 20) & 0xfu,
                                        rh = (sm >> 24) & 0xfu;
-                        const unsigned long long v = pl[g];
-                        const uint32_t raw = (uint32_t)(v >> 16), ls = (uint32_t)(v & 0xffffu);
-                        p = raw > base ? raw - base : 0u; // adjust_ref_pos_rmdup, 1893-1917
+                        const uint32_t ls = lsd[g];
                         const uint32_t rs = (((ls >> shift) ^ rl) | ((ls >> (6 + shift)) ^ rh)) & 7u; // 2107-2112
                         ok = (rs == 0) && (el != 0); // element 0 of the batch is dropped (2113)
+                        if (ok) { // positions only for the entries the flank filter keeps
+                            const uint32_t raw = pos[g];
+                            p = raw > base ? raw - base : 0u; // adjust_ref_pos_rmdup, 1893-1917
+                        }
                     }
                     const uint32_t m = __ballot_sync(0xffffffffu, ok);
                     if (ok) scratch[kept + __popc(m & lt)] = p;
@@ -1177,7 +1196,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(uint32_t nitems, co
                 uint32_t *dst = B.cand_ub + e0;
                 if (kept <= 32) {
                     uint32_t v = lane < kept ? scratch[lane] : 0xffffffffu;
-                    warp_sort_small(v);
+                    warp_sort_small(v, kept);
                     const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
                     const bool keep = lane < kept && (lane == 0 || prev != v);
                     const uint32_t m = __ballot_sync(0xffffffffu, keep);
@@ -2186,11 +2205,11 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     if (rc) return rc;
     m->launches += 6;
     k_plan<<<grid_cap(nitems, PLAN_WARPS * 32, 16), PLAN_WARPS * 32, 0, st>>>(
-        nitems, ix->d_pl, B, m->cap_chunks, m->cap_elems);
+        nitems, ix->d_pos, B, m->cap_chunks, m->cap_elems);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecord(m->ev[2], st));
-    k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(nitems, ix->d_pl, B, m->cap_chunks, m->cap_elems,
+    k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(nitems, ix->d_pos, ix->d_ls, B, m->cap_chunks, m->cap_elems,
                                                      ix->k + SWM_SEED_STEP - 1);
     m->launches++;
     LAUNCH_CHECK();
