@@ -435,6 +435,26 @@ def run_gpu(args):
             acc["ms_" + sname] = acc.get("ms_" + sname, 0.0) + m.stage_ms(sname) * args.steps
     gcups = tot_cells / tot_elapsed / 1e9
 
+    # the plain per-batch launch for comparison: one mapper, blocks of 4,096
+    # reads (the plain configuration's batch), each mapped and waited for in turn
+    plain_block = min(4096, nreads)
+    mp = swm.Mapper(ix, max_reads=plain_block)
+    for b0 in range(0, min(nreads, 4 * plain_block), plain_block):  # warm-up
+        mp.map_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, min(plain_block, nreads - b0), E,
+                      d_e.value + b0 if eper is not None else None)
+    rt.cudaDeviceSynchronize()
+    t0 = time.perf_counter()
+    plain_mapped = 0
+    for b0 in range(0, nreads, plain_block):
+        mp.map_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, min(plain_block, nreads - b0), E,
+                      d_e.value + b0 if eper is not None else None)
+        plain_mapped += mp.stats()["mapped_reads"]
+    rt.cudaDeviceSynchronize()
+    plain_t = time.perf_counter() - t0
+    del mp
+    plain = {"value": round(plain_mapped / plain_t, 1), "unit": UNIT, "block_reads": plain_block, "mappers": 1,
+             "path": "swm_map_device per block of 4,096 reads, synchronous; host clock over one pass"}
+
     # end to end through the host API: two mappers in ping-pong, packed
     # results; the reads and the result buffers are page-locked host memory
     mappers = (mappers + [swm.Mapper(ix, max_reads=block)])[:2]
@@ -540,7 +560,8 @@ def run_gpu(args):
             "per_step": {k: int(v) if not k.startswith("ms_") else round(v, 3) for k, v in per_step.items()},
             "stages": stage_rows, "stage_timing": "kernel times of one mapper alone (untimed pass)",
             "clocks": clk, "e2e": e2e,
-            "gpu_launches": int(acc["launches"]), "roofline": roofline, "int_pipe": int_pipe}
+            "gpu_launches": int(acc["launches"]), "roofline": roofline, "int_pipe": int_pipe,
+            "plain_per_batch": plain}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         arrays = ix.download()
         mix = host_map_index(arrays, w["k"])

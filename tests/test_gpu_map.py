@@ -306,3 +306,34 @@ def test_gpu_device_submit_two_mappers(cuda_lib):
     finally:
         rt.cudaFree(d_reads)
         rt.cudaFree(d_lens)
+
+
+def test_gpu_requests_same_alone_and_in_the_mix(cuda_lib):
+    """Serving coalesces requests that arrive together into one block: every
+    request's records and unmapped ids are the same mapped alone and in the
+    mix (read ids shifted by the request's offset in the block)."""
+    g = genome(2_000_000, 61, "repeats100m")
+    sizes = [1, 7, 300, 64, 1000, 5, 2]
+    reads, lens, _, _ = synth.reads(g, sum(sizes), 50, 250, 0.03, seed=63)
+    eper = np.minimum(np.ceil(0.05 * lens), 15).astype(np.uint8)
+    ix = cuda_lib.Index.build(g)
+    m = cuda_lib.Mapper(ix, max_reads=sum(sizes))
+    mixed = m.map(reads, lens, int(eper.max()), errors_per_read=eper)
+    got_mix = {}
+    for rec in mixed.records():
+        got_mix.setdefault(rec[0] >> 1, []).append(rec)
+    unm_mix = set(int(u) >> 1 for u in mixed.unmapped)
+    off = 0
+    for sz in sizes:
+        sl = slice(off, off + int(sz))
+        alone = m.map(reads[sl], lens[sl], int(eper[sl].max()), errors_per_read=eper[sl])
+        for rec in alone.records():
+            r = (rec[0] >> 1) + off
+            want = ((2 * r + (rec[0] & 1)),) + tuple(rec[1:])
+            assert want in got_mix.get(r, []), (sz, r)
+        for u in alone.unmapped:
+            assert (int(u) >> 1) + off in unm_mix
+        n_alone = sum(1 for _ in alone.records())
+        n_mix = sum(len(got_mix.get(r, [])) for r in range(off, off + int(sz)))
+        assert n_alone == n_mix
+        off += int(sz)
