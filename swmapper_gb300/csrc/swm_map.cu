@@ -51,7 +51,18 @@ enum { TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT
 
 #define ARENA_CAP_DEFAULT (1u << 20)
 
+// The inputs of one block, in device memory so that the captured launch
+// sequence of a mapper does not depend on them.
+struct BlockParams {
+    const char *reads;     // reads_num reads at a fixed stride
+    const uint32_t *lens;  // their lengths
+    const uint8_t *e;      // per-read thresholds, or null
+    uint64_t stride;
+    uint32_t nreads, nitems, errors, pad;
+};
+
 struct MapBufs {
+    BlockParams *par;      // the block's inputs (device copy)
     // per item
     uint32_t *it_w;        // items * 32: [0..15] Myers planes, [16..31] Hamming planes
     uint2 *sel;            // items * 64: (bucket start, count) of the seed of long seed l, shift t at 4 l + t
@@ -132,6 +143,12 @@ struct swm_mapper {
     cudaEvent_t ev[9];
     float stage_ms[8];
     uint64_t launches;
+    // the block's launch sequence, captured once per buffer set and read
+    // length class; the block's inputs reach it through B.par
+    BlockParams *h_par;        // pinned
+    cudaGraphExec_t gexec;
+    int gclass;                // k_seed variant the graph was captured with
+    uint32_t gen, ggen;        // buffer generation now / when the graph was captured
 };
 
 // ======================================================================
@@ -237,12 +254,14 @@ struct SeedSmem {
 };
 #define SK(arr, w, t) S.arr[(w)][((t) + (w)) & 31]
 
-__global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const char *__restrict__ reads,
-                                                          const uint32_t *__restrict__ lens, uint64_t stride,
-                                                          uint32_t nreads, uint32_t e_glob,
-                                                          const uint8_t *__restrict__ e_arr,
-                                                          const uint32_t *__restrict__ off, uint32_t k, MapBufs B) {
+__global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const uint32_t *__restrict__ off, uint32_t k, MapBufs B) {
     __shared__ SeedSmem sm_all[SEED_WARPS];
+    const BlockParams P = *B.par;
+    const char *__restrict__ reads = P.reads;
+    const uint32_t *__restrict__ lens = P.lens;
+    const uint8_t *__restrict__ e_arr = P.e;
+    const uint64_t stride = P.stride;
+    const uint32_t nreads = P.nreads, e_glob = P.errors;
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     SeedSmem &S = sm_all[wib];
     uint2 *__restrict__ sel = B.sel;
@@ -584,11 +603,13 @@ __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const u
 }
 
 template <int NL>
-__global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const char *__restrict__ reads,
-                                                           const uint32_t *__restrict__ lens, uint64_t stride,
-                                                           uint32_t nreads, uint32_t e_glob,
-                                                           const uint8_t *__restrict__ e_arr,
-                                                           const uint32_t *__restrict__ off, MapBufs B) {
+__global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const uint32_t *__restrict__ off, MapBufs B) {
+    const BlockParams P = *B.par;
+    const char *__restrict__ reads = P.reads;
+    const uint32_t *__restrict__ lens = P.lens;
+    const uint8_t *__restrict__ e_arr = P.e;
+    const uint64_t stride = P.stride;
+    const uint32_t nreads = P.nreads, e_glob = P.errors;
     uint2 *__restrict__ sel = B.sel;
     uint32_t *__restrict__ it_w = B.it_w;
     const uint32_t tid = threadIdx.x;
@@ -901,8 +922,9 @@ struct PlanSmem {
 // positions to fetch: pos[start + 32 (j + 1) - 1] for refill j) are all
 // known up front, so the lanes load them in parallel; lane 0 then runs the
 // seed heap of alignment_rmdup (2194-2419) on shared memory only.
-__global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(uint32_t nitems, const uint32_t *__restrict__ pos,
-                                                          MapBufs B, uint64_t cap_chunks, uint64_t cap_elems) {
+__global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(const uint32_t *__restrict__ pos, MapBufs B,
+                                                          uint64_t cap_chunks, uint64_t cap_elems) {
+    const uint32_t nitems = B.par->nitems;
     __shared__ PlanSmem sm_all[PLAN_WARPS];
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     PlanSmem &S = sm_all[wib];
@@ -1089,9 +1111,10 @@ struct CandSmem {
 
 // One warp per item, every batch of the item: element-parallel gather of
 // (position, flank code) pairs, position adjust, flank filter, sort-unique.
-__global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(uint32_t nitems, const uint32_t *__restrict__ pos,
+__global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(const uint32_t *__restrict__ pos,
                                                              const uint16_t *__restrict__ lsd, MapBufs B,
                                                              uint64_t cap_chunks, uint64_t cap_elems, uint32_t klong) {
+    const uint32_t nitems = B.par->nitems;
     __shared__ CandSmem sm_all[CAND_WARPS];
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
@@ -1240,8 +1263,9 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(uint32_t nitems, co
 }
 
 // Dense candidate list: item by item, batch by batch, in verification order.
-__global__ void __launch_bounds__(256) k_compact(uint32_t nitems, MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
+__global__ void __launch_bounds__(256) k_compact(MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
                                                  uint64_t cap_cands) {
+    const uint32_t nitems = B.par->nitems;
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
         // one thread per item: its scalars in one round trip, then its few
@@ -1431,11 +1455,12 @@ __device__ __forceinline__ void load_window(const uint32_t *__restrict__ b2, uin
 
 #define TB_TEXT_MAX 2304 // >= 4 bytes x every route entry a bounded walk can make
 
-__global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ lens, const uint32_t *__restrict__ b2,
+__global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
                                                 uint64_t b2_words, uint64_t ref_length, MapBufs B,
                                                 uint64_t cap_chunks, uint64_t cap_elems, uint64_t cap_cands,
                                                 uint64_t cap_arena) {
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint32_t *__restrict__ lens = B.par->lens;
     const uint64_t nc_all = B.tot[TOT_CANDS];
     const uint64_t nc = nc_all < cap_cands ? nc_all : cap_cands;
     unsigned long long cells = 0, passed = 0;
@@ -1574,12 +1599,12 @@ __device__ __forceinline__ int match_run(const uint32_t *WL, const uint32_t *WH,
     return run;
 }
 
-__global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__restrict__ lens,
-                                                          const uint32_t *__restrict__ b2, uint64_t b2_words,
+__global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__restrict__ b2, uint64_t b2_words,
                                                           uint64_t ref_length, MapBufs B, uint64_t cap_chunks,
                                                           uint64_t cap_elems, uint64_t cap_cands, uint64_t cap_arena) {
     __shared__ TbSmem T;
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint32_t *__restrict__ lens = B.par->lens;
     const uint32_t tid = threadIdx.x;
     const uint64_t ntb = B.tot[TOT_TB];
     for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + tid; q < ntb; q += (uint64_t)gridDim.x * blockDim.x) {
@@ -1757,11 +1782,11 @@ __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__rest
 // Traceback with the whole D0 / HP history in local memory, for the rare walks
 // whose route outgrows the shared-memory path of k_traceback (align_reads,
 // mapper_cpe.c:288-509).
-__global__ void __launch_bounds__(128) k_traceback_slow(const uint32_t *__restrict__ lens,
-                                                        const uint32_t *__restrict__ b2, uint64_t b2_words,
+__global__ void __launch_bounds__(128) k_traceback_slow(const uint32_t *__restrict__ b2, uint64_t b2_words,
                                                         uint64_t ref_length, MapBufs B, uint64_t cap_chunks,
                                                         uint64_t cap_elems, uint64_t cap_cands, uint64_t cap_arena) {
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint32_t *__restrict__ lens = B.par->lens;
     const uint64_t nslow = B.tot[TOT_SLOW];
     for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nslow; q += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t c = B.slow_list[q];
@@ -1874,10 +1899,11 @@ __global__ void __launch_bounds__(128) k_traceback_slow(const uint32_t *__restri
 // ======================================================================
 
 template <bool WRITE>
-__global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
+__global__ void __launch_bounds__(128) k_records(MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
                                                  uint64_t cap_cands, uint64_t cap_recs, uint64_t cap_words,
                                                  uint64_t cap_bytes) {
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint32_t nitems = B.par->nitems;
     // distinct arrays: loads of later candidates may pass earlier stores
     const uint8_t *__restrict__ vflag = B.vr_flag;
     const uint32_t *__restrict__ vloc = B.vr_loc;
@@ -1982,7 +2008,8 @@ __global__ void __launch_bounds__(128) k_records(uint32_t nitems, MapBufs B, uin
     }
 }
 
-__global__ void k_batches_stat(uint32_t nitems, MapBufs B) {
+__global__ void k_batches_stat(MapBufs B) {
+    const uint32_t nitems = B.par->nitems;
     unsigned long long s = 0;
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x)
         s += B.it_nbat[item];
@@ -2020,7 +2047,7 @@ static int dmalloc(T **p, uint64_t count) {
 }
 
 static void free_bufs(MapBufs &B) {
-    void *ps[] = {B.it_w, B.sel, B.sel_fl, B.it_perm, B.unm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
+    void *ps[] = {B.par, B.it_w, B.sel, B.sel_fl, B.it_perm, B.unm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
@@ -2060,12 +2087,15 @@ static int alloc_items(swm_mapper *m) {
     rc |= dmalloc(&B.it_coff, I + 1);
     rc |= dmalloc(&B.tot, TOT_N);
     rc |= dmalloc(&B.stat, ST_N);
+    rc |= dmalloc(&B.par, 1);
+    m->gen++;
     return rc ? SWM_ERR_OOM : SWM_OK;
 }
 
 static int alloc_work(swm_mapper *m) {
     MapBufs &B = m->b;
     int rc = SWM_OK;
+    m->gen++; // the captured graph holds the old buffers
     cudaFree(B.ch_g); cudaFree(B.ch_meta); cudaFree(B.plan_keys); cudaFree(B.bt_c0); cudaFree(B.bt_c1); cudaFree(B.bt_e0);
     cudaFree(B.bt_cnt); cudaFree(B.sort_scratch); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
     cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
@@ -2131,7 +2161,8 @@ extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper *
                          cudaHostAlloc((void **)&m->h_e, max_reads, 0) != cudaSuccess ||
                          cudaHostAlloc((void **)&m->h_unm, (m->cap_items / 32 + 1) * 2, 0) != cudaSuccess ||
                          cudaHostAlloc((void **)&m->h_tot, TOT_N * 4, 0) != cudaSuccess ||
-                         cudaHostAlloc((void **)&m->h_stat, ST_N * 8, 0) != cudaSuccess))
+                         cudaHostAlloc((void **)&m->h_stat, ST_N * 8, 0) != cudaSuccess ||
+                         cudaHostAlloc((void **)&m->h_par, sizeof(BlockParams), 0) != cudaSuccess))
         rc = SWM_ERR_OOM;
     if (rc != SWM_OK) {
         swm_mapper_free(m);
@@ -2146,6 +2177,7 @@ extern "C" void swm_mapper_free(swm_mapper *m) {
     if (!m) return;
     cudaSetDevice(m->device);
     if (m->st) cudaStreamSynchronize(m->st);
+    if (m->gexec) cudaGraphExecDestroy(m->gexec);
     free_bufs(m->b);
     cudaFree(m->d_reads);
     cudaFree(m->d_lens);
@@ -2161,6 +2193,7 @@ extern "C" void swm_mapper_free(swm_mapper *m) {
     cudaFreeHost(m->h_unm);
     cudaFreeHost(m->h_tot);
     cudaFreeHost(m->h_stat);
+    cudaFreeHost(m->h_par);
     for (int i = 0; i < 9; i++)
         if (m->ev[i]) cudaEventDestroy(m->ev[i]);
     if (m->st) cudaStreamDestroy(m->st);
@@ -2176,80 +2209,128 @@ extern "C" void swm_mapper_free(swm_mapper *m) {
         }                                                                                           \
     } while (0)
 
-// Queue the whole pipeline for one block on m->st. No host synchronisation.
-static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, uint64_t stride, uint32_t nreads,
-                   uint32_t errors, const uint8_t *d_e) {
+// The whole pipeline of one block on st, every size read on the device (the
+// grids cover the buffers' capacity; kernels loop over what the block has).
+// Captured into the mapper's graph; gclass picks the seed kernel.
+static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     MapBufs &B = m->b;
-    cudaStream_t st = m->st;
-    const uint32_t nitems = 2 * nreads;
+    const uint32_t *d_n = &B.par->nitems;
+    const uint64_t ci = m->cap_items;
     const swm_index *ix = m->ix;
     m->launches = 0;
+    SWM_CUDA(cudaMemcpyAsync(B.par, m->h_par, sizeof(BlockParams), cudaMemcpyHostToDevice, st));
     SWM_CUDA(cudaMemsetAsync(B.tot, 0, TOT_N * 4, st));
     SWM_CUDA(cudaMemsetAsync(B.stat, 0, ST_N * 8, st));
-    SWM_CUDA(cudaEventRecord(m->ev[0], st));
-    if (ix->k == K12 && stride <= 10 * KL12 + KL12 - 1)
-        k_seed12<10><<<grid_cap(nitems, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(
-            d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, B);
-    else if (ix->k == K12)
-        k_seed12<16><<<grid_cap(nitems, SEED12_THREADS, 8), SEED12_THREADS, 0, st>>>(
-            d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, B);
+    // stage events: external records become event nodes of the captured graph
+    SWM_CUDA(cudaEventRecordWithFlags(m->ev[0], st, cudaEventRecordExternal));
+    if (gclass == 1)
+        k_seed12<10><<<grid_cap(ci, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(ix->d_off, B);
+    else if (gclass == 2)
+        k_seed12<16><<<grid_cap(ci, SEED12_THREADS, 8), SEED12_THREADS, 0, st>>>(ix->d_off, B);
     else
-        k_seed<<<grid_cap((uint64_t)nitems, SEED_WARPS * 32, 8), SEED_WARPS * 32, 0, st>>>(
-            d_reads, d_lens, stride, nreads, errors, d_e, ix->d_off, ix->k, B);
+        k_seed<<<grid_cap(ci, SEED_WARPS * 32, 8), SEED_WARPS * 32, 0, st>>>(ix->d_off, ix->k, B);
     m->launches++;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[1], st));
-    int rc = swm_exclusive_scan(B.it_nch, B.it_choff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_CHUNKS, st);
+    SWM_CUDA(cudaEventRecordWithFlags(m->ev[1], st, cudaEventRecordExternal));
+    int rc = swm_exclusive_scan(B.it_nch, B.it_choff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_CHUNKS, st);
     if (rc) return rc;
-    rc = swm_exclusive_scan(B.it_nel, B.it_eloff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_ELEMS, st);
+    rc = swm_exclusive_scan(B.it_nel, B.it_eloff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_ELEMS, st);
     if (rc) return rc;
     m->launches += 6;
-    k_plan<<<grid_cap(nitems, PLAN_WARPS * 32, 16), PLAN_WARPS * 32, 0, st>>>(
-        nitems, ix->d_pos, B, m->cap_chunks, m->cap_elems);
+    k_plan<<<grid_cap(ci, PLAN_WARPS * 32, 16), PLAN_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
+                                                                          m->cap_elems);
     m->launches++;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[2], st));
-    k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(nitems, ix->d_pos, ix->d_ls, B, m->cap_chunks, m->cap_elems,
+    SWM_CUDA(cudaEventRecordWithFlags(m->ev[2], st, cudaEventRecordExternal));
+    k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(ix->d_pos, ix->d_ls, B, m->cap_chunks, m->cap_elems,
                                                      ix->k + SWM_SEED_STEP - 1);
     m->launches++;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[3], st));
-    rc = swm_exclusive_scan(B.it_ncand, B.it_coff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_CANDS, st);
+    SWM_CUDA(cudaEventRecordWithFlags(m->ev[3], st, cudaEventRecordExternal));
+    rc = swm_exclusive_scan(B.it_ncand, B.it_coff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_CANDS, st);
     if (rc) return rc;
     m->launches += 3;
-    k_compact<<<grid_cap(nitems, 256, 8), 256, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems, m->cap_cands);
+    k_compact<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands);
     m->launches++;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[4], st));
-    k_verify<<<grid_cap(m->cap_cands, 128, 64), 128, 0, st>>>(d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
+    SWM_CUDA(cudaEventRecordWithFlags(m->ev[4], st, cudaEventRecordExternal));
+    k_verify<<<grid_cap(m->cap_cands, 128, 64), 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
                                                                ix->ref_length, B, m->cap_chunks, m->cap_elems,
                                                                m->cap_cands, m->cap_arena);
     m->launches++;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[5], st));
+    SWM_CUDA(cudaEventRecordWithFlags(m->ev[5], st, cudaEventRecordExternal));
     k_traceback<<<grid_cap(m->cap_cands, TB_THREADS, 16), TB_THREADS, 0, st>>>(
-        d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
+        ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
         m->cap_arena);
     k_traceback_slow<<<grid_cap(m->cap_cands, 128, 4), 128, 0, st>>>(
-        d_lens, ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
+        ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
         m->cap_arena);
     m->launches += 2;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[6], st));
-    k_records<false><<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems, m->cap_cands,
-                                                                 m->cap_recs, m->cap_words, m->cap_bytes);
-    rc = swm_exclusive_scan(B.it_nrec, B.it_recoff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_RECS, st);
+    SWM_CUDA(cudaEventRecordWithFlags(m->ev[6], st, cudaEventRecordExternal));
+    k_records<false><<<grid_cap(ci, 128, 32), 128, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands,
+                                                             m->cap_recs, m->cap_words, m->cap_bytes);
+    rc = swm_exclusive_scan(B.it_nrec, B.it_recoff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_RECS, st);
     if (rc) return rc;
-    rc = swm_exclusive_scan(B.it_nw, B.it_woff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_WORDS, st);
+    rc = swm_exclusive_scan(B.it_nw, B.it_woff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_WORDS, st);
     if (rc) return rc;
-    rc = swm_exclusive_scan(B.it_nb, B.it_boff, nullptr, nitems, nitems, B.scan_tmp, B.tot + TOT_BYTES, st);
+    rc = swm_exclusive_scan(B.it_nb, B.it_boff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_BYTES, st);
     if (rc) return rc;
-    k_records<true><<<grid_cap(nitems, 128, 32), 128, 0, st>>>(nitems, B, m->cap_chunks, m->cap_elems, m->cap_cands,
-                                                                m->cap_recs, m->cap_words, m->cap_bytes);
-    k_batches_stat<<<grid_cap(nitems, 256, 8), 256, 0, st>>>(nitems, B);
+    k_records<true><<<grid_cap(ci, 128, 32), 128, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands,
+                                                            m->cap_recs, m->cap_words, m->cap_bytes);
+    k_batches_stat<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B);
     m->launches += 12;
     LAUNCH_CHECK();
-    SWM_CUDA(cudaEventRecord(m->ev[7], st));
+    SWM_CUDA(cudaEventRecordWithFlags(m->ev[7], st, cudaEventRecordExternal));
+    SWM_CUDA(cudaMemcpyAsync(m->h_tot, B.tot, TOT_N * 4, cudaMemcpyDeviceToHost, st));
+    SWM_CUDA(cudaMemcpyAsync(m->h_stat, B.stat, ST_N * 8, cudaMemcpyDeviceToHost, st));
+    return SWM_OK;
+}
+
+static void drop_graph(swm_mapper *m) {
+    if (m->gexec) cudaGraphExecDestroy(m->gexec);
+    m->gexec = nullptr;
+}
+
+// Queue one block on m->st: its inputs into the pinned parameter block, then
+// the mapper's graph (captured again after its buffers changed). No host
+// synchronisation.
+static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, uint64_t stride, uint32_t nreads,
+                   uint32_t errors, const uint8_t *d_e) {
+    const int gclass = m->ix->k != K12 ? 0 : (stride <= 10 * KL12 + KL12 - 1 ? 1 : 2);
+    BlockParams *P = m->h_par;
+    P->reads = d_reads;
+    P->lens = d_lens;
+    P->e = d_e;
+    P->stride = stride;
+    P->nreads = nreads;
+    P->nitems = 2 * nreads;
+    P->errors = errors;
+    P->pad = 0;
+    if (!m->gexec || m->gclass != gclass || m->ggen != m->gen) {
+        drop_graph(m);
+        cudaGraph_t g = nullptr;
+        SWM_CUDA(cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_ops(m, m->st, gclass);
+        const cudaError_t ce = cudaStreamEndCapture(m->st, &g);
+        if (rc != SWM_OK || ce != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            if (rc == SWM_OK) swm_set_error("capturing the block pipeline: %s", cudaGetErrorString(ce));
+            cudaGetLastError();
+            return rc != SWM_OK ? rc : SWM_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&m->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            m->gexec = nullptr;
+            swm_set_error("instantiating the block pipeline: %s", cudaGetErrorString(ie));
+            return SWM_ERR_CUDA;
+        }
+        m->gclass = gclass;
+        m->ggen = m->gen;
+    }
+    SWM_CUDA(cudaGraphLaunch(m->gexec, m->st));
     return SWM_OK;
 }
 
@@ -2261,11 +2342,6 @@ static void grow(uint64_t *cap, uint64_t need) {
 }
 
 // Queue the copy of the block's totals to pinned memory (after enqueue).
-static int queue_totals(swm_mapper *m) {
-    SWM_CUDA(cudaMemcpyAsync(m->h_tot, m->b.tot, TOT_N * 4, cudaMemcpyDeviceToHost, m->st));
-    SWM_CUDA(cudaMemcpyAsync(m->h_stat, m->b.stat, ST_N * 8, cudaMemcpyDeviceToHost, m->st));
-    return SWM_OK;
-}
 
 // Wait for the queued block and inspect its totals. *again is set when a
 // work buffer was too small; the capacities are grown and the buffers
@@ -2316,12 +2392,11 @@ static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *a
         return alloc_work(m);
     }
     float t;
-    for (int i = 0; i < 7; i++) {
-        cudaEventElapsedTime(&t, m->ev[i], m->ev[i + 1]);
-        m->stage_ms[i] = t;
+    for (int i = 0; i < 8; i++) {
+        const cudaError_t te = cudaEventElapsedTime(&t, m->ev[i < 7 ? i : 0], m->ev[i < 7 ? i + 1 : 7]);
+        m->stage_ms[i] = te == cudaSuccess ? t : 0.0f;
+        if (te != cudaSuccess) cudaGetLastError(); // timing only: no stale error for later calls
     }
-    cudaEventElapsedTime(&t, m->ev[0], m->ev[7]);
-    m->stage_ms[7] = t;
     const unsigned long long *stat = m->h_stat;
     swm_map_stats &S = m->stats;
     memset(&S, 0, sizeof S);
@@ -2350,7 +2425,6 @@ static int run_block(swm_mapper *m, const char *d_reads, const uint32_t *d_lens,
                      uint32_t errors, const uint8_t *d_e, uint64_t retries) {
     for (int attempt = 0; attempt < 8; attempt++) {
         int rc = enqueue(m, d_reads, d_lens, stride, nreads, errors, d_e);
-        if (!rc) rc = queue_totals(m);
         if (rc) return rc;
         int again = 0;
         rc = finish_block(m, nreads, retries, &again);
@@ -2415,7 +2489,6 @@ extern "C" int swm_map_device_submit(swm_mapper *m, const char *d_reads, const u
     m->cur_n = reads_num;
     m->cur_errors = errors;
     rc = enqueue(m, d_reads, d_lens, stride, (uint32_t)reads_num, errors, d_errors);
-    if (!rc) rc = queue_totals(m);
     if (rc) return rc;
     m->pending = 2;
     return SWM_OK;
@@ -2639,7 +2712,6 @@ extern "C" int swm_map_submit(swm_mapper *m, const swm_batch *b) {
     m->have_result = 0;
     rc = enqueue(m, m->d_reads, m->d_lens, b->stride, (uint32_t)b->reads_num, b->errors,
                  b->errors_per_read ? m->d_e : nullptr);
-    if (!rc) rc = queue_totals(m);
     if (rc) return rc;
     m->pending = 1;
     return SWM_OK;
