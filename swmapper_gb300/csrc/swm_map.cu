@@ -47,7 +47,19 @@ enum {
     ST_N
 };
 // device totals (u32), written by the scans
-enum { TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT_ARENA, TOT_FLAGS, TOT_TB, TOT_SLOW, TOT_N };
+enum {
+    TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT_ARENA, TOT_FLAGS, TOT_TB, TOT_SLOW,
+    TOT_VQ, TOT_TBQ, // work-queue heads of k_verify and k_traceback
+    TOT_N
+};
+
+// Next 32 work units of a warp from a device work queue (head *q): every lane
+// gets the same base; the warp is done when it reaches n.
+__device__ __forceinline__ uint32_t warp_take(uint32_t *q) {
+    uint32_t b = 0;
+    if ((threadIdx.x & 31) == 0) b = atomicAdd(q, 32u);
+    return __shfl_sync(0xffffffffu, b, 0);
+}
 
 #define ARENA_CAP_DEFAULT (1u << 20)
 
@@ -1464,7 +1476,11 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
     const uint64_t nc_all = B.tot[TOT_CANDS];
     const uint64_t nc = nc_all < cap_cands ? nc_all : cap_cands;
     unsigned long long cells = 0, passed = 0;
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (uint64_t)gridDim.x * blockDim.x) {
+    for (;;) { // persistent warps take candidates 32 at a time from the queue
+        const uint32_t cb = warp_take(&B.tot[TOT_VQ]);
+        if (cb >= nc) break;
+        const uint64_t c = cb + (threadIdx.x & 31);
+        if (c >= nc) continue;
         const uint32_t item = B.cc_item[c], p = B.cc_pos[c];
         const uint32_t L = lens[item >> 1], e = B.it_e[item];
         uint32_t rl;
@@ -1607,7 +1623,11 @@ __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__rest
     const uint32_t *__restrict__ lens = B.par->lens;
     const uint32_t tid = threadIdx.x;
     const uint64_t ntb = B.tot[TOT_TB];
-    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + tid; q < ntb; q += (uint64_t)gridDim.x * blockDim.x) {
+    for (;;) { // persistent warps take tracebacks 32 at a time from the queue (walks vary in length)
+        const uint32_t qb = warp_take(&B.tot[TOT_TBQ]);
+        if (qb >= ntb) break;
+        const uint64_t q = qb + (tid & 31);
+        if (q >= ntb) continue;
         const uint32_t c = B.tb_list[q];
         const uint32_t item = B.cc_item[c];
         const uint32_t L = lens[item >> 1], e = B.it_e[item];
@@ -2254,7 +2274,7 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[4], st, cudaEventRecordExternal));
-    k_verify<<<grid_cap(m->cap_cands, 128, 64), 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
+    k_verify<<<grid_cap(m->cap_cands, 128, 16), 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
                                                                ix->ref_length, B, m->cap_chunks, m->cap_elems,
                                                                m->cap_cands, m->cap_arena);
     m->launches++;
