@@ -330,6 +330,14 @@ def run_gpu(args):
     w = WORKLOAD
     g, reads, lens, eper = make_workload(rank)
     E = e_arg(eper)
+    bucketed = False
+    if args.buckets and int(lens.min()) != int(lens.max()):
+        # reads of similar length share a block (autotuner length buckets of 32 bp)
+        from swmapper_gb300 import tune as swtune
+        order = np.concatenate([ix_ for _, ix_ in swtune.length_buckets(lens)])
+        reads, lens = np.ascontiguousarray(reads[order]), np.ascontiguousarray(lens[order])
+        eper = None if eper is None else np.ascontiguousarray(eper[order])
+        bucketed = True
     t0 = time.perf_counter()
     ix = swm.Index.build(g, k=w["k"], device=local)
     index_build_s = time.perf_counter() - t0
@@ -347,6 +355,15 @@ def run_gpu(args):
         rt.cudaMemcpy(d_e, eper.ctypes.data, eper.nbytes, 1)
     # NMAP mappers (own stream and buffers each) take the blocks in turn, so
     # one block's gather-bound stages overlap another's ALU-bound ones
+    tuned = None
+    if args.tune:  # reads per block and mappers from timed trials on the resident reads
+        from swmapper_gb300 import tune as swtune
+        # a window from the middle of the reads (with length buckets: reads of middling length)
+        n_t = min(nreads, 2 * 262144)
+        o_t = (nreads - n_t) // 2
+        tuned = swtune.tune(ix, d_reads.value + o_t * stride, d_lens.value + o_t * 4, stride, n_t, E,
+                            d_e.value + o_t if eper is not None else None)
+        block, args.mappers = min(tuned["block"], nreads), tuned["mappers"]
     mappers = [swm.Mapper(ix, max_reads=block) for _ in range(args.mappers)]
     m = mappers[0]
     streams = [C.c_void_p(mm.stream()) for mm in mappers]
@@ -551,6 +568,7 @@ def run_gpu(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded genome and reads of the workload's shapes; no public dataset)",
             "config": {**WORKLOAD, "block_reads": block, "mappers": args.mappers,
+                       "autotune": tuned, "length_buckets": bucketed,
                        "parallelism": f"replicas x{ws} (reads sharded by rank)",
                        "l2": (f"inputs {input_bytes / 1e6:.0f} MB < L2: L2 flushed ({L2_FLUSH_BYTES >> 20} MiB write) "
                               f"before each timed step" if flush else
@@ -741,6 +759,9 @@ def main():
                     help="benchmark configuration (default: batched, the headline line)")
     ap.add_argument("--block", type=int, default=None, help="reads per mapping block (default: the workload's)")
     ap.add_argument("--mappers", type=int, default=2, help="mappers taking the blocks in turn")
+    ap.add_argument("--tune", type=int, default=1, help="autotune reads per block and mappers (1) or not (0)")
+    ap.add_argument("--buckets", type=int, default=1,
+                    help="group reads of different lengths into 32-bp length buckets (1) or not (0)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)

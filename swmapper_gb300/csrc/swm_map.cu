@@ -615,7 +615,11 @@ __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const u
 }
 
 template <int NL>
-__global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const uint32_t *__restrict__ off, MapBufs B) {
+// Items whose read length is outside [lo_len, hi_len] belong to the other
+// instantiation launched beside this one (reads of up to 164 bases take the
+// 10-long-seed kernel, longer ones the 16-long-seed kernel).
+__global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const uint32_t *__restrict__ off, MapBufs B,
+                                                           uint32_t lo_len, uint32_t hi_len) {
     const BlockParams P = *B.par;
     const char *__restrict__ reads = P.reads;
     const uint32_t *__restrict__ lens = P.lens;
@@ -633,6 +637,7 @@ __global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const uint32_t *__res
         const uint32_t pair = 3u << (lane_id() & ~1u);
         const uint32_t r = item >> 1, strand = item & 1;
         const uint32_t L = lens[r];
+        if (L < lo_len || L > hi_len) continue; // both lanes of the read skip it
         const uint32_t e = e_arr ? e_arr[r] : e_glob;
         if (L > SWM_MAX_READ_LEN || L > stride || e > SWM_MAX_ERRORS || L > NL * KL12 + KL12 - 1) {
             atomicOr(&B.tot[TOT_FLAGS], OV_BAD);
@@ -2243,11 +2248,15 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     SWM_CUDA(cudaMemsetAsync(B.stat, 0, ST_N * 8, st));
     // stage events: external records become event nodes of the captured graph
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[0], st, cudaEventRecordExternal));
-    if (gclass == 1)
-        k_seed12<10><<<grid_cap(ci, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(ix->d_off, B);
-    else if (gclass == 2)
-        k_seed12<16><<<grid_cap(ci, SEED12_THREADS, 8), SEED12_THREADS, 0, st>>>(ix->d_off, B);
-    else
+    const uint32_t short_max = 10 * KL12 + KL12 - 1; // 164: longest read with <= 10 long seeds
+    if (gclass == 1) {
+        k_seed12<10><<<grid_cap(ci, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(ix->d_off, B, 0u, 0xffffffffu);
+    } else if (gclass == 2) { // each read to the instantiation of its length
+        k_seed12<10><<<grid_cap(ci, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(ix->d_off, B, 0u, short_max);
+        k_seed12<16><<<grid_cap(ci, SEED12_THREADS, 8), SEED12_THREADS, 0, st>>>(ix->d_off, B, short_max + 1,
+                                                                                   0xffffffffu);
+        m->launches++;
+    } else
         k_seed<<<grid_cap(ci, SEED_WARPS * 32, 8), SEED_WARPS * 32, 0, st>>>(ix->d_off, ix->k, B);
     m->launches++;
     LAUNCH_CHECK();

@@ -1,0 +1,106 @@
+"""Autotuner for the batched form: reads per block, mappers and length buckets.
+
+The mapping kernels take one read-length class per block (the seed kernel is
+instantiated for at most 10 or 16 long seeds, verification runs in lockstep
+over a warp's candidates), so reads of very different lengths in one block
+waste lanes. The autotuner
+
+* groups reads into length buckets of 32 bp (`length_buckets`), so a block
+  holds reads of similar length, and
+* times a sample of resident reads under every (reads per block, mappers)
+  candidate and keeps the fastest (`tune`), with an optional cache key
+  (for example GPU, k, length bucket, e).
+
+Results do not depend on the choice: every read maps the same in any block.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+BUCKET_BP = 32
+BLOCKS = (65536, 131072, 262144, 524288)
+MAPPERS = (1, 2, 3)
+
+_cache: dict = {}
+
+
+def length_buckets(lens: np.ndarray, bucket_bp: int = BUCKET_BP) -> list[tuple[int, np.ndarray]]:
+    """(bucket, read indices in input order) for every non-empty 32-bp length bucket."""
+    b = (lens.astype(np.int64) - 1) // bucket_bp
+    order = np.argsort(b, kind="stable")
+    keys = b[order]
+    out = []
+    if order.size:
+        cuts = np.flatnonzero(np.diff(keys)) + 1
+        for part in np.split(order, cuts):
+            out.append((int(b[part[0]]), part))
+    return out
+
+
+def _cudart():
+    for name in ("libcudart.so.13", "libcudart.so", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            rt = C.CDLL(name)
+            rt.cudaDeviceSynchronize.argtypes = []
+            return rt
+        except OSError:
+            continue
+    raise RuntimeError("libcudart not found")
+
+
+def run_blocks(mappers, d_reads: int, d_lens: int, stride: int, nreads: int, e: int, d_e: int | None, block: int,
+               on_done=None):
+    """Map nreads device-resident reads in blocks taken by the mappers in turn
+    (swm_map_device_submit / swm_map_device_wait); on_done(mapper) after each."""
+    pend = []
+    for i, b0 in enumerate(range(0, nreads, block)):
+        nb = min(block, nreads - b0)
+        if len(pend) == len(mappers):
+            pm = pend.pop(0)
+            pm.wait_device()
+            if on_done:
+                on_done(pm)
+        m = mappers[i % len(mappers)]
+        m.submit_device(d_reads + b0 * stride, d_lens + b0 * 4, stride, nb, e,
+                        None if d_e is None else d_e + b0)
+        pend.append(m)
+    while pend:
+        pm = pend.pop(0)
+        pm.wait_device()
+        if on_done:
+            on_done(pm)
+
+
+def tune(index, d_reads: int, d_lens: int, stride: int, nreads: int, e: int, d_e: int | None = None,
+         key=None, blocks=BLOCKS, mappers=MAPPERS, min_sample: int = 262144) -> dict:
+    """Fastest (reads per block, mappers) for these device-resident reads, timed
+    on a sample of at least min_sample reads (two passes, the second timed)."""
+    import swmapper_gb300 as swm
+    if key is not None and key in _cache:
+        return _cache[key]
+    rt = _cudart()
+    best = None
+    trials = []
+    for nm in mappers:
+        for blk in blocks:
+            n = min(nreads, max(min_sample, nm * blk))
+            if blk > n and blk != blocks[0]:
+                continue
+            ms = [swm.Mapper(index, max_reads=min(blk, n)) for _ in range(nm)]
+            run_blocks(ms, d_reads, d_lens, stride, n, e, d_e, min(blk, n))  # warm-up (graphs, buffers)
+            rt.cudaDeviceSynchronize()
+            t0 = time.perf_counter()
+            run_blocks(ms, d_reads, d_lens, stride, n, e, d_e, min(blk, n))
+            rt.cudaDeviceSynchronize()
+            rate = n / (time.perf_counter() - t0)
+            del ms
+            trials.append({"block": blk, "mappers": nm, "reads_per_s": round(rate, 1)})
+            if best is None or rate > best["reads_per_s"]:
+                best = trials[-1]
+    res = {"block": best["block"], "mappers": best["mappers"], "trials": trials}
+    if key is not None:
+        _cache[key] = res
+    return res
