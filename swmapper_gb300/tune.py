@@ -1,9 +1,8 @@
 """Autotuner for the batched form: reads per block, mappers and length buckets.
 
-The mapping kernels take one read-length class per block (the seed kernel is
-instantiated for at most 10 or 16 long seeds, verification runs in lockstep
-over a warp's candidates), so reads of very different lengths in one block
-waste lanes. The autotuner
+Verification runs the lanes of a warp in lockstep over their candidates'
+read lengths, so reads of very different lengths side by side waste lanes.
+The autotuner
 
 * groups reads into length buckets of 32 bp (`length_buckets`), so a block
   holds reads of similar length, and
