@@ -600,9 +600,11 @@ def count_mapped(buf, nreads):
 
 def run_serving(args):
     """Batch latency under Poisson arrivals: one host thread coalesces the
-    requests that have arrived (up to one block of reads) and hands them to two
-    mappers in turn (swm_map_submit / swm_map_wait_packed); a request's latency
-    runs from its arrival to the return of the wait that delivers its records."""
+    requests that have arrived (up to one block of reads) into the next free
+    block slot (a mapper: swm_map_submit / swm_map_wait_packed), so requests
+    arriving while others are on the GPU join the next block and overlap with
+    them; the slots are sized by free device memory. A request's latency runs
+    from its arrival to the return of the wait that delivers its records."""
     import swmapper_gb300 as swm
     ws, rank, local = dist_env()
     rt = cudart()
@@ -619,8 +621,18 @@ def run_serving(args):
     sizes = np.maximum(sizes, 1)
     starts = np.concatenate([[0], np.cumsum(sizes)[:-1]]) % max(1, reads.shape[0] - 4096)
     block = args.block
-    mappers = [swm.Mapper(ix, max_reads=block) for _ in range(2)]
-    bufs = [swm.PackedBuffers(block) for _ in range(2)]
+    # admission by free device memory: as many block slots (mappers, each with
+    # its own buffers) as half of the free memory holds, two to four
+    rt.cudaMemGetInfo.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+    free0, total = C.c_size_t(), C.c_size_t()
+    rt.cudaMemGetInfo(C.byref(free0), C.byref(total))
+    mappers = [swm.Mapper(ix, max_reads=block)]
+    free1 = C.c_size_t()
+    rt.cudaMemGetInfo(C.byref(free1), C.byref(total))
+    per_slot = max(1, free0.value - free1.value)
+    nslots = int(max(2, min(4, (free1.value // 2) // per_slot + 1)))
+    mappers += [swm.Mapper(ix, max_reads=block) for _ in range(nslots - 1)]
+    bufs = [swm.PackedBuffers(block) for _ in range(nslots)]
 
     streams = [C.c_void_p(mm.stream()) for mm in mappers]
     rt.cudaStreamQuery.argtypes = [C.c_void_p]
@@ -630,7 +642,7 @@ def run_serving(args):
         latency of each and the span from the first arrival to the last reply."""
         nq = len(arrivals)
         lat = np.zeros(nq)
-        pend = []   # (mapper index, [request ids]), oldest first
+        pend = []   # (mapper index, [request ids]), oldest first; mappers are taken in turn
         nxt = 0
         slot = 0
         t_start = time.perf_counter()
@@ -646,7 +658,7 @@ def run_serving(args):
 
         while nxt < nq or pend:
             now = time.perf_counter() - t_start
-            if nxt < nq and arrivals[nxt] <= now and len(pend) < 2:
+            if nxt < nq and arrivals[nxt] <= now and len(pend) < nslots:
                 # coalesce what has arrived, up to one block of reads
                 ids, n = [], 0
                 while nxt < nq and arrivals[nxt] <= now and n + sizes[nxt] <= block:
@@ -656,8 +668,8 @@ def run_serving(args):
                 sel = np.concatenate([np.arange(starts[q], starts[q] + sizes[q]) for q in ids])
                 mappers[slot].submit(reads[sel], lens[sel], e_arg(eper), None if eper is None else eper[sel])
                 pend.append((slot, ids))
-                slot ^= 1
-            elif pend and (len(pend) == 2 or nxt >= nq or rt.cudaStreamQuery(streams[pend[0][0]]) == 0):
+                slot = (slot + 1) % nslots
+            elif pend and (len(pend) == nslots or nxt >= nq or rt.cudaStreamQuery(streams[pend[0][0]]) == 0):
                 complete()
             elif not pend:
                 time.sleep(max(0.0, min(arrivals[nxt] - now, 0.0005)))
@@ -680,7 +692,9 @@ def run_serving(args):
             "higher_is_better": False, "peak_reads_per_s": round(peak, 1), "loads": rows,
             "requests": nreq, "reads_per_request_mean": round(float(sizes.mean()), 1),
             "index_build_s": round(index_build_s, 3), "data": "synthetic",
-            "config": {**WORKLOAD, "block_reads": block, "mappers": 2}}
+            "config": {**WORKLOAD, "block_reads": block, "mappers": nslots,
+                       "admission": f"{nslots} block slots: half of the free device memory "
+                                    f"({free1.value >> 20} MiB) over {per_slot >> 20} MiB per slot"}}
     print(json.dumps(line), flush=True)
 
 
