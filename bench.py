@@ -359,7 +359,7 @@ def run_gpu(args):
     if args.tune:  # reads per block and mappers from timed trials on the resident reads
         from swmapper_gb300 import tune as swtune
         # a window from the middle of the reads (with length buckets: reads of middling length)
-        n_t = min(nreads, 2 * 262144)
+        n_t = min(nreads, 2_000_000)
         o_t = (nreads - n_t) // 2
         tuned = swtune.tune(ix, d_reads.value + o_t * stride, d_lens.value + o_t * 4, stride, n_t, E,
                             d_e.value + o_t if eper is not None else None)
@@ -474,8 +474,9 @@ def run_gpu(args):
 
     # end to end through the host API: two mappers in ping-pong, packed
     # results; the reads and the result buffers are page-locked host memory
-    mappers = (mappers + [swm.Mapper(ix, max_reads=block)])[:2]
-    bufs = [swm.PackedBuffers(block), swm.PackedBuffers(block)]
+    ne = max(2, args.e2e_mappers)
+    mappers = (mappers + [swm.Mapper(ix, max_reads=block) for _ in range(ne)])[:ne]
+    bufs = [swm.PackedBuffers(block) for _ in range(ne)]
     rt.cudaHostRegister.argtypes = [C.c_void_p, C.c_size_t, C.c_uint]
     pinned = [reads, lens] + [a for bf in bufs for a in (bf.words, bf.cigar, bf.rlen)]
     for a in pinned:
@@ -484,24 +485,24 @@ def run_gpu(args):
 
     def e2e_run(nsteps, acc2):
         """nsteps passes over the reads as one continuous stream of blocks:
-        block i + 2 is submitted as soon as block i's results are back."""
+        block i + ne is submitted as soon as block i's results are back."""
         pend = []
 
         def drain():
             j, pm = pend.pop(0)
-            pm.wait_packed(bufs[j % 2])
-            acc2["mapped"] += count_mapped(bufs[j % 2], blocks[j % len(blocks)][1])
+            pm.wait_packed(bufs[j % ne])
+            acc2["mapped"] += count_mapped(bufs[j % ne], blocks[j % len(blocks)][1])
             st = pm.stats()
             acc2["h2d"] += st["h2d_bytes"]
             acc2["d2h"] += st["d2h_bytes"]
 
         for i in range(nsteps * len(blocks)):
             b0, nb = blocks[i % len(blocks)]
-            if len(pend) == 2:
+            if len(pend) == ne:
                 drain()
-            mappers[i % 2].submit(reads[b0:b0 + nb], lens[b0:b0 + nb], E,
+            mappers[i % ne].submit(reads[b0:b0 + nb], lens[b0:b0 + nb], E,
                                   None if eper is None else eper[b0:b0 + nb])
-            pend.append((i, mappers[i % 2]))
+            pend.append((i, mappers[i % ne]))
         while pend:
             drain()
 
@@ -518,7 +519,7 @@ def run_gpu(args):
         rt.cudaHostUnregister(a.ctypes.data)
     e2e = {"value": e2e_mapped / e2e_t, "unit": UNIT,
            "h2d_bytes_per_step": int(acc2["h2d"] / e2e_steps), "d2h_bytes_per_step": int(acc2["d2h"] / e2e_steps),
-           "steps": e2e_steps, "path": "swm_map_submit + swm_map_wait_packed, 2 mappers ping-pong over a continuous stream of "
+           "steps": e2e_steps, "path": f"swm_map_submit + swm_map_wait_packed, {ne} mappers in turn over a continuous stream of "
                    "blocks, page-locked host buffers"}
 
     # roofline of the dominant kernel
@@ -777,6 +778,7 @@ def main():
     ap.add_argument("--buckets", type=int, default=1,
                     help="group reads of different lengths into 32-bp length buckets (1) or not (0)")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-mappers", type=int, default=4, help="mappers in the end-to-end pipeline (>= 2)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

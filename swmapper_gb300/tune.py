@@ -74,9 +74,10 @@ def run_blocks(mappers, d_reads: int, d_lens: int, stride: int, nreads: int, e: 
 
 
 def tune(index, d_reads: int, d_lens: int, stride: int, nreads: int, e: int, d_e: int | None = None,
-         key=None, blocks=BLOCKS, mappers=MAPPERS, min_sample: int = 262144) -> dict:
+         key=None, blocks=BLOCKS, mappers=MAPPERS, min_sample: int = 1 << 20) -> dict:
     """Fastest (reads per block, mappers) for these device-resident reads, timed
-    on a sample of at least min_sample reads (two passes, the second timed)."""
+    on at least min_sample reads, so every mapper gets blocks (two passes, the
+    second timed)."""
     import swmapper_gb300 as swm
     if key is not None and key in _cache:
         return _cache[key]
@@ -85,7 +86,7 @@ def tune(index, d_reads: int, d_lens: int, stride: int, nreads: int, e: int, d_e
     trials = []
     for nm in mappers:
         for blk in blocks:
-            n = min(nreads, max(min_sample, nm * blk))
+            n = min(nreads, max(min_sample, 2 * nm * blk))
             if blk > n and blk != blocks[0]:
                 continue
             ms = [swm.Mapper(index, max_reads=min(blk, n)) for _ in range(nm)]
