@@ -1112,7 +1112,7 @@ __device__ __forceinline__ void warp_sort_small(uint32_t &v, uint32_t n) {
 
 #define CAND_MAXCH 128 // chunks (runs) per batch: block_size < 256 allows at most 128
 
-#define CAND_SMEM_KEEP 64 // batches of up to this many elements keep their survivors in shared memory
+#define CAND_SMEM_KEEP 64 // survivors of a batch held in shared memory (more go to global scratch)
 
 struct CandSmem {
     uint32_t g[CAND_MAXCH];      // first global index of each chunk
@@ -1121,7 +1121,7 @@ struct CandSmem {
     uint32_t sel[SWM_MAX_SEL];   // base | shift << 16 | rl << 20 | rh << 24
     uint32_t st[SWM_MAX_SEL];    // bucket start of each selected seed
     uint32_t cn[SWM_MAX_SEL];    // bucket count of each selected seed
-    uint32_t sc[CAND_SMEM_KEEP]; // kept positions of a batch of <= CAND_SMEM_KEEP elements
+    uint32_t sc[CAND_SMEM_KEEP]; // kept positions of a batch, while they fit
 };
 
 #define CAND_WARPS 8
@@ -1201,7 +1201,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(const uint32_t *__r
                 const uint32_t E = carry;
                 if (lane == 0) S.start[nchk] = (uint16_t)E;
                 __syncwarp();
-                uint32_t *scratch = E <= CAND_SMEM_KEEP ? S.sc : gscratch;
+                uint32_t *scratch = S.sc; // survivors; moved to global scratch if they outgrow it
                 uint32_t kept = 0;
                 for (uint32_t eb = 0; eb < E; eb += 32) {
                     const uint32_t el = eb + lane;
@@ -1228,6 +1228,11 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(const uint32_t *__r
                         }
                     }
                     const uint32_t m = __ballot_sync(0xffffffffu, ok);
+                    if (scratch == S.sc && kept + __popc(m) > CAND_SMEM_KEEP) {
+                        for (uint32_t i = lane; i < kept; i += 32) gscratch[i] = S.sc[i];
+                        scratch = gscratch;
+                        __syncwarp();
+                    }
                     if (ok) scratch[kept + __popc(m & lt)] = p;
                     kept += __popc(m);
                 }
