@@ -455,14 +455,14 @@ def run_gpu(args):
     # the plain per-batch launch for comparison: one mapper, blocks of 4,096
     # reads (the plain configuration's batch), each mapped and waited for in turn
     plain_block = min(4096, nreads)
-    mp = swm.Mapper(ix, max_reads=plain_block)
-    for b0 in range(0, min(nreads, 4 * plain_block), plain_block):  # warm-up
+    mp = swm.Mapper(ix, max_reads=plain_block) if args.plain else None
+    for b0 in range(0, min(nreads, 4 * plain_block) if mp else 0, plain_block):  # warm-up
         mp.map_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, min(plain_block, nreads - b0), E,
                       d_e.value + b0 if eper is not None else None)
     rt.cudaDeviceSynchronize()
     t0 = time.perf_counter()
     plain_mapped = 0
-    for b0 in range(0, nreads, plain_block):
+    for b0 in range(0, nreads if mp else 0, plain_block):
         mp.map_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, min(plain_block, nreads - b0), E,
                       d_e.value + b0 if eper is not None else None)
         plain_mapped += mp.stats()["mapped_reads"]
@@ -470,7 +470,8 @@ def run_gpu(args):
     plain_t = time.perf_counter() - t0
     del mp
     plain = {"value": round(plain_mapped / plain_t, 1), "unit": UNIT, "block_reads": plain_block, "mappers": 1,
-             "path": "swm_map_device per block of 4,096 reads, synchronous; host clock over one pass"}
+             "path": "swm_map_device per block of 4,096 reads, synchronous; host clock over one pass"} if args.plain \
+        else None
 
     # end to end through the host API: two mappers in ping-pong, packed
     # results; the reads and the result buffers are page-locked host memory
@@ -783,6 +784,7 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--requests", type=int, default=None, help="requests of the serving workload")
+    ap.add_argument("--plain", type=int, default=1, help="also time the plain per-batch launch (1) or not (0)")
     ap.add_argument("--genome-bp", type=int, default=None, help="smaller genome for quick checks")
     ap.add_argument("--nreads", type=int, default=None, help="fewer reads for quick checks")
     args = ap.parse_args()
