@@ -297,8 +297,9 @@ STAGES = ["seed", "plan", "candidates", "compact", "verify", "traceback", "recor
 
 def stage_bytes(stage, st, L, e):
     """Algorithmic DRAM bytes of one stage over a whole step: what the stage must
-    read and write once (index entries are 8-byte (position, flank) pairs;
-    `chunks` counts refill chunks)."""
+    read and write once (index entries: 2-byte flank codes read for every
+    fetched entry, 4-byte positions for the survivors; `chunks` counts refill
+    chunks)."""
     nl = L // 15
     items = st["items"]
     ns = min(e + 1, nl) * 4
@@ -306,8 +307,9 @@ def stage_bytes(stage, st, L, e):
         return items * (L + nl * 4 * 8 + 128 + ns * 12 + 16)
     if stage == "plan":   # items with refills only: seed table, refill chunks, batch records
         return st["chunks"] * (8 + 8) + st["batches"] * 12 + items * 8
-    if stage == "candidates":  # (position, flank) pairs, seed table, refill chunks, candidates
-        return st["fetched"] * 8 + items * ns * 12 + st["chunks"] * 8 + st["candidates"] * 4
+    if stage == "candidates":  # flank codes of every fetched entry, positions of the survivors, seed
+        # records (8 B + flank byte), refill chunks, candidates written
+        return st["fetched"] * 2 + st["candidates"] * 4 + items * ns * 9 + st["chunks"] * 8 + st["candidates"] * 4
     if stage == "compact":
         return st["candidates"] * 12 + st["batches"] * 12
     if stage == "verify":
