@@ -554,6 +554,22 @@ __device__ __forceinline__ uint32_t ld_keep(const uint32_t *p, uint64_t pol) {
     asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
     return v;
 }
+__device__ __forceinline__ uint2 ld_keep2(const uint32_t *p, uint64_t pol) { // p 8-byte aligned
+    uint2 v;
+    asm("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(p), "l"(pol));
+    return v;
+}
+
+// Start and count of bucket sd: one 8-byte load holds off[sd] and off[sd + 1]
+// when sd is even; an odd sd takes off[sd + 1] from a second load.
+__device__ __forceinline__ void bucket_range(const uint32_t *__restrict__ off, uint32_t sd, uint64_t pol,
+                                             uint32_t &o0, uint32_t &c) {
+    const bool odd = sd & 1u;
+    const uint2 v = ld_keep2(off + (sd & ~1u), pol);
+    const uint32_t w = odd ? ld_keep(off + sd + 1, pol) : 0u;
+    o0 = odd ? v.y : v.x;
+    c = (odd ? w : v.y) - o0;
+}
 
 // Seed code of the seed at read offset o (12 bases from o) from the
 // interleaved words w0 = word o / 16 and w1 = the next one; with N bases
@@ -580,6 +596,8 @@ __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const u
                                                const uint32_t *__restrict__ off, uint64_t pol,
                                                uint2 *__restrict__ rec, uint32_t *__restrict__ flw,
                                                uint32_t (&cnt)[NL], uint32_t (&nref)[NL]) {
+    static_assert(NL % 2 == 0, "flank words are stored in pairs");
+    uint32_t pf = 0;
 #pragma unroll
     for (int l = 0; l < NL; l++) {
         const bool act = (uint32_t)l < nl;
@@ -587,7 +605,7 @@ __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const u
         const uint32_t nlo = wj0 + 1 < 8 ? plo[wj0 + 1] : 0u, nhi = wj0 + 1 < 8 ? phi[wj0 + 1] : 0u;
         const uint32_t lr = (sh0 ? __funnelshift_r(plo[wj0], nlo, sh0) : plo[wj0]) & 0x7fffu;
         const uint32_t hr = (sh0 ? __funnelshift_r(phi[wj0], nhi, sh0) : phi[wj0]) & 0x7fffu;
-        uint32_t csum = 0, rsum = 0, f = 0;
+        uint32_t csum = 0, rsum = 0, f = 0, po = 0, pc = 0;
 #pragma unroll
         for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
             const uint32_t o = ob + sft, w = o >> 4;
@@ -598,17 +616,21 @@ __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const u
                 sd = seed12_nfix(sd, ~(s5 ? __funnelshift_r(pok[wj], nx, s5) : pok[wj]), sft);
             }
             sd = act ? sd : 0u;
-            const uint32_t o0 = ld_keep(off + sd, pol);
-            const uint32_t c = ld_keep(off + sd + 1, pol) - o0;
+            uint32_t o0, c;
+            bucket_range(off, sd, pol, o0, c);
             const uint32_t m = (1u << sft) - 1, kk = K12 + sft;
             const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & 7u;
             const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & 7u;
-            rec[SWM_SEED_STEP * l + sft] = make_uint2(o0, c);
+            if (sft & 1) // two records per 16-byte store
+                reinterpret_cast<uint4 *>(rec)[(SWM_SEED_STEP * l + sft) >> 1] = make_uint4(po, pc, o0, c);
+            po = o0;
+            pc = c;
             f |= (rl | (rh << 3)) << (8 * sft);
             csum += c;
             rsum += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
         }
-        flw[l] = f;
+        if (l & 1) reinterpret_cast<uint2 *>(flw)[l >> 1] = make_uint2(pf, f); // two long seeds per store
+        pf = f;
         cnt[l] = act ? csum : 0u;
         nref[l] = act ? rsum : 0u;
     }
