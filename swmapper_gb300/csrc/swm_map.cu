@@ -1137,8 +1137,8 @@ __device__ __forceinline__ void warp_sort_small(uint32_t &v, uint32_t n) {
 #define CAND_SMEM_KEEP 64 // survivors of a batch held in shared memory (more go to global scratch)
 
 struct CandSmem {
-    uint32_t g[CAND_MAXCH];      // first global index of each chunk
-    uint32_t meta[CAND_MAXCH];   // len | sel << 8
+    uint32_t gs[CAND_MAXCH];     // first global index of each chunk minus its start in the batch
+    uint32_t cm[CAND_MAXCH];     // descriptor (sel[]) of the chunk's seed
     uint16_t start[CAND_MAXCH + 1];
     uint32_t sel[SWM_MAX_SEL];   // base | shift << 16 | rl << 20 | rh << 24
     uint32_t st[SWM_MAX_SEL];    // bucket start of each selected seed
@@ -1147,10 +1147,13 @@ struct CandSmem {
 };
 
 #define CAND_WARPS 8
+#ifndef CAND_MIN_BLOCKS
+#define CAND_MIN_BLOCKS 8 // resident blocks per SM the register budget is sized for
+#endif
 
 // One warp per item, every batch of the item: element-parallel gather of
 // (position, flank code) pairs, position adjust, flank filter, sort-unique.
-__global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(const uint32_t *__restrict__ pos,
+__global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const uint32_t *__restrict__ pos,
                                                              const uint16_t *__restrict__ lsd, MapBufs B,
                                                              uint64_t cap_chunks, uint64_t cap_elems, uint32_t klong) {
     const uint32_t nitems = B.par->nitems;
@@ -1197,10 +1200,10 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(const uint32_t *__r
                         const uint32_t m = __ballot_sync(0xffffffffu, len != 0);
                         const uint32_t inc = warp_scan_incl(len);
                         if (len) {
-                            const uint32_t q = nchk + __popc(m & lt);
-                            S.g[q] = S.st[i];
-                            S.meta[q] = len | (i << 8);
-                            S.start[q] = (uint16_t)(carry + inc - len);
+                            const uint32_t q = nchk + __popc(m & lt), st0 = carry + inc - len;
+                            S.gs[q] = S.st[i] - st0;
+                            S.cm[q] = S.sel[i];
+                            S.start[q] = (uint16_t)st0;
                         }
                         nchk += __popc(m);
                         carry += __shfl_sync(0xffffffffu, inc, 31);
@@ -1208,15 +1211,18 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(const uint32_t *__r
                 }
                 for (uint32_t q0 = c0; q0 < c1; q0 += 32) {
                     const uint32_t c = q0 + lane;
-                    uint32_t len = 0;
+                    uint32_t len = 0, meta = 0;
                     if (c < c1) {
-                        const uint32_t meta = B.ch_meta[c];
+                        meta = B.ch_meta[c];
                         len = meta & 0xffu;
-                        S.g[nchk + (c - q0)] = B.ch_g[c];
-                        S.meta[nchk + (c - q0)] = meta;
                     }
                     const uint32_t inc = warp_scan_incl(len);
-                    if (c < c1) S.start[nchk + (c - q0)] = (uint16_t)(carry + inc - len);
+                    if (c < c1) {
+                        const uint32_t st0 = carry + inc - len;
+                        S.gs[nchk + (c - q0)] = B.ch_g[c] - st0;
+                        S.cm[nchk + (c - q0)] = S.sel[meta >> 8];
+                        S.start[nchk + (c - q0)] = (uint16_t)st0;
+                    }
                     nchk += min(32u, c1 - q0);
                     carry += __shfl_sync(0xffffffffu, inc, 31);
                 }
@@ -1224,21 +1230,20 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(const uint32_t *__r
                 if (lane == 0) S.start[nchk] = (uint16_t)E;
                 __syncwarp();
                 uint32_t *scratch = S.sc; // survivors; moved to global scratch if they outgrow it
-                uint32_t kept = 0;
+                uint32_t kept = 0, cdone = 0; // cdone: chunks that start before eb
                 for (uint32_t eb = 0; eb < E; eb += 32) {
                     const uint32_t el = eb + lane;
+                    // chunks are non-empty, so at most 32 start in [eb, eb + 32):
+                    // lane j looks at chunk cdone + j and the starts become a bit mask
+                    const uint32_t cs = cdone + lane < nchk ? S.start[cdone + lane] : eb + 32;
+                    const uint32_t bits = __reduce_or_sync(0xffffffffu, cs < eb + 32 ? 1u << (cs - eb) : 0u);
+                    const uint32_t q = cdone + __popc(bits & (0xffffffffu >> (31 - lane))) - 1; // chunk of el
+                    cdone += __popc(bits);
                     bool ok = false;
                     uint32_t p = 0;
                     if (el < E) {
-                        uint32_t lo = 0, hi = nchk; // last chunk with start <= el
-                        while (hi - lo > 1) {
-                            const uint32_t mid = (lo + hi) >> 1;
-                            if (S.start[mid] <= el) lo = mid;
-                            else hi = mid;
-                        }
-                        const uint32_t q = lo;
-                        const uint32_t g = S.g[q] + (el - S.start[q]);
-                        const uint32_t sm = S.sel[S.meta[q] >> 8];
+                        const uint32_t g = S.gs[q] + el;
+                        const uint32_t sm = S.cm[q];
                         const uint32_t base = sm & 0xffffu, shift = (sm >> 16) & 0xfu, rl = (sm >> 20) & 0xfu,
                                        rh = (sm >> 24) & 0xfu;
                         const uint32_t ls = lsd[g];
@@ -1262,13 +1267,25 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, 8) k_cand(const uint32_t *__r
                 uint32_t u = 0;
                 uint32_t *dst = B.cand_ub + e0;
                 if (kept <= 32) {
-                    uint32_t v = lane < kept ? scratch[lane] : 0xffffffffu;
-                    warp_sort_small(v, kept);
-                    const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
-                    const bool keep = lane < kept && (lane == 0 || prev != v);
-                    const uint32_t m = __ballot_sync(0xffffffffu, keep);
-                    if (keep) dst[__popc(m & lt)] = v;
-                    u = __popc(m);
+                    // survivors are mostly copies of a few positions: take the
+                    // distinct values smallest first (up to 8), sort what is left
+                    uint32_t v = lane < kept ? scratch[lane] : 0xffffffffu, res = 0;
+                    for (;;) {
+                        const uint32_t m = __reduce_min_sync(0xffffffffu, v);
+                        if (m == 0xffffffffu || u == 8) break;
+                        res = lane == u ? m : res;
+                        v = v == m ? 0xffffffffu : v;
+                        u++;
+                    }
+                    if (lane < u) dst[lane] = res;
+                    if (__any_sync(0xffffffffu, v != 0xffffffffu)) {
+                        warp_sort_k<32>(v);
+                        const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
+                        const bool keep = v != 0xffffffffu && (lane == 0 || prev != v);
+                        const uint32_t m = __ballot_sync(0xffffffffu, keep);
+                        if (keep) dst[u + __popc(m & lt)] = v;
+                        u += __popc(m);
+                    }
                 } else {
                     uint32_t n2 = 64;
                     while (n2 < kept) n2 <<= 1;
