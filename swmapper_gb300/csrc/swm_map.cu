@@ -168,6 +168,11 @@ struct swm_mapper {
 // ======================================================================
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ uint32_t lanemask_lt() { // lanes below this one
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
 
 __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned long long v) {
 #pragma unroll
@@ -514,6 +519,18 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const uint32_t *__rest
 #define K12 12u
 #define KL12 15u
 #define SEED12_THREADS 64
+// resident blocks per SM the register budget of each k_seed12 is sized for
+// (0: the compiler's choice). The short-read kernel is latency-bound on its
+// bucket-offset lookups: 16 blocks (64 registers, a few spills) keep twice as
+// many lookups in flight as its natural 80 registers and run 20-25% faster;
+// the 16-long-seed kernel loses more to spills than it gains.
+#ifndef SEED12_MIN_BLOCKS_10
+#define SEED12_MIN_BLOCKS_10 16
+#endif
+#ifndef SEED12_MIN_BLOCKS_16
+#define SEED12_MIN_BLOCKS_16 0
+#endif
+#define SEED12_BOUNDS __launch_bounds__(SEED12_THREADS, NL == 10 ? SEED12_MIN_BLOCKS_10 : SEED12_MIN_BLOCKS_16)
 
 // 4 read bytes -> 4 lo bits, 4 hi bits, 4 "is A/C/G/T" bits (base j of the
 // word at bit j). Code ((c >> 1) ^ (c >> 2)) & 3 maps A C G T to 0 1 2 3;
@@ -640,7 +657,7 @@ template <int NL>
 // Items whose read length is outside [lo_len, hi_len] belong to the other
 // instantiation launched beside this one (reads of up to 164 bases take the
 // 10-long-seed kernel, longer ones the 16-long-seed kernel).
-__global__ void __launch_bounds__(SEED12_THREADS) k_seed12(const uint32_t *__restrict__ off, MapBufs B,
+__global__ void SEED12_BOUNDS k_seed12(const uint32_t *__restrict__ off, MapBufs B,
                                                            uint32_t lo_len, uint32_t hi_len) {
     const BlockParams P = *B.par;
     const char *__restrict__ reads = P.reads;
@@ -1161,8 +1178,8 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     CandSmem &S = sm_all[wib];
-    const uint32_t lt = (1u << lane) - 1;
-    uint32_t *gscratch = B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS;
+    // a warp's survivors past CAND_SMEM_KEEP go to its slice of global scratch
+    auto gscratch = [&]() { return B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS; };
     for (uint32_t item = blockIdx.x * CAND_WARPS + wib; item < nitems; item += gridDim.x * CAND_WARPS) {
         const uint32_t nb = B.it_nbat[item];
         uint32_t total = 0;
@@ -1200,7 +1217,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
                         const uint32_t m = __ballot_sync(0xffffffffu, len != 0);
                         const uint32_t inc = warp_scan_incl(len);
                         if (len) {
-                            const uint32_t q = nchk + __popc(m & lt), st0 = carry + inc - len;
+                            const uint32_t q = nchk + __popc(m & lanemask_lt()), st0 = carry + inc - len;
                             S.gs[q] = S.st[i] - st0;
                             S.cm[q] = S.sel[i];
                             S.start[q] = (uint16_t)st0;
@@ -1229,7 +1246,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
                 const uint32_t E = carry;
                 if (lane == 0) S.start[nchk] = (uint16_t)E;
                 __syncwarp();
-                uint32_t *scratch = S.sc; // survivors; moved to global scratch if they outgrow it
+                bool spilled = false; // survivors in S.sc, or in global scratch once they outgrow it
                 uint32_t kept = 0, cdone = 0; // cdone: chunks that start before eb
                 for (uint32_t eb = 0; eb < E; eb += 32) {
                     const uint32_t el = eb + lane;
@@ -1255,12 +1272,17 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
                         }
                     }
                     const uint32_t m = __ballot_sync(0xffffffffu, ok);
-                    if (scratch == S.sc && kept + __popc(m) > CAND_SMEM_KEEP) {
-                        for (uint32_t i = lane; i < kept; i += 32) gscratch[i] = S.sc[i];
-                        scratch = gscratch;
+                    if (!spilled && kept + __popc(m) > CAND_SMEM_KEEP) {
+                        uint32_t *gs = gscratch();
+                        for (uint32_t i = lane; i < kept; i += 32) gs[i] = S.sc[i];
+                        spilled = true;
                         __syncwarp();
                     }
-                    if (ok) scratch[kept + __popc(m & lt)] = p;
+                    if (ok) {
+                        const uint32_t at = kept + __popc(m & lanemask_lt());
+                        if (spilled) gscratch()[at] = p;
+                        else S.sc[at] = p;
+                    }
                     kept += __popc(m);
                 }
                 __syncwarp();
@@ -1269,7 +1291,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
                 if (kept <= 32) {
                     // survivors are mostly copies of a few positions: take the
                     // distinct values smallest first (up to 8), sort what is left
-                    uint32_t v = lane < kept ? scratch[lane] : 0xffffffffu, res = 0;
+                    uint32_t v = lane < kept ? S.sc[lane] : 0xffffffffu, res = 0;
                     for (;;) {
                         const uint32_t m = __reduce_min_sync(0xffffffffu, v);
                         if (m == 0xffffffffu || u == 8) break;
@@ -1283,13 +1305,13 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
                         const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
                         const bool keep = v != 0xffffffffu && (lane == 0 || prev != v);
                         const uint32_t m = __ballot_sync(0xffffffffu, keep);
-                        if (keep) dst[u + __popc(m & lt)] = v;
+                        if (keep) dst[u + __popc(m & lanemask_lt())] = v;
                         u += __popc(m);
                     }
                 } else {
                     uint32_t n2 = 64;
                     while (n2 < kept) n2 <<= 1;
-                    uint32_t *buf = scratch;
+                    uint32_t *buf = spilled ? gscratch() : S.sc;
                     for (uint32_t i = kept + lane; i < n2; i += 32) buf[i] = 0xffffffffu;
                     __syncwarp();
                     for (uint32_t size = 2; size <= n2; size <<= 1) {
@@ -1310,7 +1332,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
                         const uint32_t i = i0 + lane;
                         const bool keep = i < kept && (i == 0 || buf[i - 1] != buf[i]);
                         const uint32_t m = __ballot_sync(0xffffffffu, keep);
-                        if (keep) dst[u + __popc(m & lt)] = buf[i];
+                        if (keep) dst[u + __popc(m & lanemask_lt())] = buf[i];
                         u += __popc(m);
                     }
                 }
