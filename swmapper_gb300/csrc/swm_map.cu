@@ -1764,7 +1764,11 @@ __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__rest
                 search_site--; pre = 3; match_site--; sum_err++; start--;
             }
         }
-        while (i >= 0) { // mapper_cpe.c:412-466
+        // mapper_cpe.c:412-466. One iteration = a run of matching steps (if
+        // any) and the step after it: a run stops at a base that differs, so
+        // the reference's next iteration would find no run and take that
+        // step; doing both here keeps the lanes of a warp in step.
+        while (i >= 0) {
             if (sum_err == err) break;
             if (match_site < 0) break; // defined stop below the window start
             if (search_site >= 0 && search_site <= 2 * (int)e) {
@@ -1778,7 +1782,7 @@ __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__rest
                     }
                     i -= run;
                     match_site -= run;
-                    continue;
+                    if (i < 0 || match_site < 0) break;
                 }
             }
             uint32_t d0b, hpb;
