@@ -780,7 +780,8 @@ def main():
     ap.add_argument("--tune", type=int, default=1, help="autotune reads per block and mappers (1) or not (0)")
     ap.add_argument("--buckets", type=int, default=1,
                     help="group reads of different lengths into 32-bp length buckets (1) or not (0)")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10,
+                    help="passes over the reads in the end-to-end stream (pipeline fill and drain amortised over them)")
     ap.add_argument("--e2e-mappers", type=int, default=4, help="mappers in the end-to-end pipeline (>= 2)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
