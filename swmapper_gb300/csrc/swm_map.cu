@@ -50,6 +50,7 @@ enum {
 enum {
     TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT_ARENA, TOT_FLAGS, TOT_TB, TOT_SLOW,
     TOT_VQ, TOT_TBQ, // work-queue heads of k_verify and k_traceback
+    TOT_VT, TOT_VTQ, // candidates alive after the head of verification, and their queue head
     TOT_N
 };
 
@@ -102,6 +103,8 @@ struct MapBufs {
     uint32_t *vr_aoff;
     uint8_t *arena;   // long CIGAR texts
     uint16_t *unm;       // bit j of halfword w: read 16 w + j has no location (cap_items / 32 + 1)
+    uint2 *vt_x;         // candidates alive after the head of verification: (candidate, ones) (cap_cands)
+    uint4 *vt_st;        // and their Myers state (VP, VN, VP and VN at the start of block 1) (cap_cands)
     uint32_t *tb_list;   // candidates that need a traceback (cap_cands)
     uint32_t *tb_cp;     // (VP, VN) at every 32-base block of each of them (cap_cands * 16)
     uint32_t *plan_keys; // heap keys of items with more than PLAN_KEYS of them (cap_chunks)
@@ -1406,16 +1409,13 @@ __device__ __forceinline__ uint32_t window_start(uint32_t base_pos, uint32_t L, 
 // Banded Myers / Hyyro recurrence of banded_myers_simd (mapper_cpe.c:519-660)
 // with the pattern-match word built from window bit planes: at read base i
 // bit j of eq is [window[i + j] == read[i]] for j <= 2e, the same word the
-// reference keeps in peq[read[i]]. Returns (error, location) exactly as the
-// reference's final scan (634-650). cp gets (VP, VN) at the start of every
-// 32-base block.
-__device__ __forceinline__ int myers_scan(const uint32_t *WL, const uint32_t *WH, const uint32_t *RW, uint32_t L,
-                                          uint32_t e, uint32_t rl, int *loc_out, uint32_t *cp) {
-    const uint32_t band = 2 * e + 1;
-    const uint32_t MASK = (1u << band) - 1u;
-    uint32_t vp = 0, vn = 0, ones = 0;
-    const uint32_t nblk = (L + 31) >> 5;
-    for (uint32_t b = 0; b < nblk; b++) {
+// reference keeps in peq[read[i]]. myers_blocks runs the 32-base blocks
+// b0 .. b1 - 1 (the last one may be partial) from the state (VP, VN, ones =
+// steps whose D0 bit 0 was set); cp gets (VP, VN) at the start of each.
+__device__ __forceinline__ void myers_blocks(const uint32_t *WL, const uint32_t *WH, const uint32_t *RW, uint32_t L,
+                                             uint32_t MASK, uint32_t b0, uint32_t b1, uint32_t &vp, uint32_t &vn,
+                                             uint32_t &ones, uint32_t *cp) {
+    for (uint32_t b = b0; b < b1; b++) {
         const uint32_t wl0 = WL[b], wl1 = WL[b + 1], wh0 = WH[b], wh1 = WH[b + 1];
         const uint32_t rlw = RW[2 * b], rhw = RW[2 * b + 1];
         const uint32_t steps = min(32u, L - 32 * b);
@@ -1455,6 +1455,12 @@ __device__ __forceinline__ int myers_scan(const uint32_t *WL, const uint32_t *WH
         }
         ones += __popc(acc);
     }
+}
+
+// The reference's final scan (634-650) after all L steps: (error, location)
+// of the first strict minimum with error <= e, or (SWM_MAXERROR, -1).
+__device__ __forceinline__ int myers_final(uint32_t vp, uint32_t vn, uint32_t ones, uint32_t L, uint32_t e,
+                                           uint32_t rl, int *loc_out) {
     int err = (int)L - (int)ones;
     const int last_high = (int)rl - (int)L;
     const int site = (int)L - 1;
@@ -1538,39 +1544,89 @@ __device__ __forceinline__ void load_window(const uint32_t *__restrict__ b2, uin
 
 #define TB_TEXT_MAX 2304 // >= 4 bytes x every route entry a bounded walk can make
 
+// Verification in two passes. The head runs the first VERIFY_HEAD_BLOCKS
+// 32-base blocks of every candidate. The error at the band's site only grows
+// with more steps, and the final scan can lower it by at most
+// last_high <= 2e, so a candidate whose site error is already above 3e
+// cannot end at or below e: the full scan would return (SWM_MAXERROR, -1),
+// and the head writes that result at once. The others are queued with their
+// state, and the tail finishes them. On the benchmark genomes a third to
+// half of all candidates stop in the head.
+#define VERIFY_HEAD_BLOCKS 2
+
+template <bool HEAD>
 __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
                                                 uint64_t b2_words, uint64_t ref_length, MapBufs B,
                                                 uint64_t cap_chunks, uint64_t cap_elems, uint64_t cap_cands,
                                                 uint64_t cap_arena) {
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
     const uint32_t *__restrict__ lens = B.par->lens;
-    const uint64_t nc_all = B.tot[TOT_CANDS];
-    const uint64_t nc = nc_all < cap_cands ? nc_all : cap_cands;
+    uint64_t n;
+    if (HEAD) {
+        const uint64_t nc_all = B.tot[TOT_CANDS];
+        n = nc_all < cap_cands ? nc_all : cap_cands;
+    } else {
+        n = B.tot[TOT_VT];
+    }
     unsigned long long cells = 0, passed = 0;
-    for (;;) { // persistent warps take candidates 32 at a time from the queue
-        const uint32_t cb = warp_take(&B.tot[TOT_VQ]);
-        if (cb >= nc) break;
-        const uint64_t c = cb + (threadIdx.x & 31);
-        if (c >= nc) continue;
+    for (;;) { // persistent warps take work 32 at a time from the queue
+        const uint32_t jb = warp_take(&B.tot[HEAD ? TOT_VQ : TOT_VTQ]);
+        if (jb >= n) break;
+        const uint64_t j = jb + (threadIdx.x & 31);
+        if (j >= n) continue;
+        uint64_t c;
+        uint32_t vp = 0, vn = 0, ones = 0;
+        uint32_t cp[16];
+        cp[0] = cp[1] = 0;
+        if (HEAD) {
+            c = j;
+        } else {
+            const uint2 x = B.vt_x[j];
+            const uint4 st = B.vt_st[j];
+            c = x.x;
+            ones = x.y;
+            vp = st.x;
+            vn = st.y;
+            cp[2] = st.z;
+            cp[3] = st.w;
+        }
         const uint32_t item = B.cc_item[c], p = B.cc_pos[c];
         const uint32_t L = lens[item >> 1], e = B.it_e[item];
         uint32_t rl;
         const uint32_t ws = window_start(p, L, e, ref_length, &rl);
-        if (ws == 0xffffffffu) {
+        if (HEAD && ws == 0xffffffffu) {
             B.vr_flag[c] = VR_INVALID;
             B.vr_err[c] = SWM_MAXERROR;
             B.vr_mloc[c] = -1;
             continue;
         }
+        const uint32_t nblk = (L + 31) >> 5;
+        const bool head_only = HEAD && nblk > VERIFY_HEAD_BLOCKS;
         uint32_t WL[SWM_WIN_WORDS], WH[SWM_WIN_WORDS];
-        load_window(b2, b2_words, ws, L, e, WL, WH);
+        // the head reads window words 0 .. VERIFY_HEAD_BLOCKS only
+        load_window(b2, b2_words, ws, head_only ? 32 * VERIFY_HEAD_BLOCKS - 2 * e : L, e, WL, WH);
         const uint32_t *RW = B.it_w + (uint64_t)item * 32;
         uint32_t rw[16];
 #pragma unroll
-        for (int i = 0; i < 16; i++) rw[i] = RW[i];
+        for (int i = 0; i < 16; i++) rw[i] = (HEAD && i >= 2 * VERIFY_HEAD_BLOCKS) ? 0u : RW[i];
+        const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
+        myers_blocks(WL, WH, rw, L, MASK, HEAD ? 0u : VERIFY_HEAD_BLOCKS,
+                     HEAD ? min(nblk, (uint32_t)VERIFY_HEAD_BLOCKS) : nblk, vp, vn, ones, cp);
+        if (head_only) {
+            if (32 * VERIFY_HEAD_BLOCKS - ones > 3 * e) { // cannot end at or below e
+                cells += (unsigned long long)L * (2 * e + 1);
+                B.vr_err[c] = SWM_MAXERROR;
+                B.vr_mloc[c] = -1;
+                B.vr_flag[c] = VR_FAIL;
+            } else {
+                const uint32_t at = atomicAdd(&B.tot[TOT_VT], 1u);
+                B.vt_x[at] = make_uint2((uint32_t)c, ones);
+                B.vt_st[at] = make_uint4(vp, vn, cp[2], cp[3]);
+            }
+            continue;
+        }
         int loc;
-        uint32_t cp[16];
-        const int err = myers_scan(WL, WH, rw, L, e, rl, &loc, cp);
+        const int err = myers_final(vp, vn, ones, L, e, rl, &loc);
         cells += (unsigned long long)L * (2 * e + 1);
         B.vr_err[c] = err;
         B.vr_mloc[c] = loc;
@@ -1608,7 +1664,6 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
         const uint32_t at = atomicAdd(&B.tot[TOT_TB], 1u);
         B.tb_list[at] = (uint32_t)c;
         uint4 *cpo = reinterpret_cast<uint4 *>(B.tb_cp + (uint64_t)at * 16);
-        const uint32_t nblk = (L + 31) >> 5;
 #pragma unroll
         for (uint32_t k = 0; k < 4; k++)
             if (4 * k < 2 * nblk) cpo[k] = make_uint4(cp[4 * k], cp[4 * k + 1], cp[4 * k + 2], cp[4 * k + 3]);
@@ -2146,7 +2201,7 @@ static void free_bufs(MapBufs &B) {
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
-                  B.tb_cp, B.slow_list,
+                  B.tb_cp, B.slow_list, B.vt_x, B.vt_st,
                   B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
     for (void *p : ps) cudaFree(p);
     memset(&B, 0, sizeof(B));
@@ -2195,7 +2250,7 @@ static int alloc_work(swm_mapper *m) {
     cudaFree(B.bt_cnt); cudaFree(B.sort_scratch); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
     cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
     cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
-    cudaFree(B.tb_list); cudaFree(B.tb_cp); cudaFree(B.slow_list);
+    cudaFree(B.tb_list); cudaFree(B.tb_cp); cudaFree(B.slow_list); cudaFree(B.vt_x); cudaFree(B.vt_st);
     cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
     rc |= dmalloc(&B.ch_g, m->cap_chunks);
     rc |= dmalloc(&B.ch_meta, m->cap_chunks);
@@ -2219,6 +2274,8 @@ static int alloc_work(swm_mapper *m) {
     rc |= dmalloc(&B.tb_list, m->cap_cands);
     rc |= dmalloc(&B.tb_cp, m->cap_cands * 16);
     rc |= dmalloc(&B.slow_list, m->cap_cands);
+    rc |= dmalloc(&B.vt_x, m->cap_cands);
+    rc |= dmalloc(&B.vt_st, m->cap_cands);
     rc |= dmalloc(&B.out_w, m->cap_words);
     rc |= dmalloc(&B.out_c, m->cap_bytes);
     rc |= dmalloc(&B.rec_woff, m->cap_recs);
@@ -2353,10 +2410,13 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[4], st, cudaEventRecordExternal));
-    k_verify<<<grid_cap(m->cap_cands, 128, 16), 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
-                                                               ix->ref_length, B, m->cap_chunks, m->cap_elems,
-                                                               m->cap_cands, m->cap_arena);
-    m->launches++;
+    k_verify<true><<<grid_cap(m->cap_cands, 128, 16), 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
+                                                                     ix->ref_length, B, m->cap_chunks, m->cap_elems,
+                                                                     m->cap_cands, m->cap_arena);
+    k_verify<false><<<grid_cap(m->cap_cands, 128, 16), 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
+                                                                      ix->ref_length, B, m->cap_chunks, m->cap_elems,
+                                                                      m->cap_cands, m->cap_arena);
+    m->launches += 2;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[5], st, cudaEventRecordExternal));
     k_traceback<<<grid_cap(m->cap_cands, TB_THREADS, 16), TB_THREADS, 0, st>>>(
