@@ -51,6 +51,7 @@ enum {
     TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT_ARENA, TOT_FLAGS, TOT_TB, TOT_SLOW,
     TOT_VQ, TOT_TBQ, // work-queue heads of k_verify and k_traceback
     TOT_VT, TOT_VTQ, // candidates alive after the head of verification, and their queue head
+    TOT_PLN, TOT_PLQ, // items with refills, and the queue head of k_plan
     TOT_N
 };
 
@@ -87,6 +88,7 @@ struct MapBufs {
     uint32_t *it_nrec, *it_nw, *it_nb;
     uint32_t *it_recoff, *it_woff, *it_boff; // items + 1
     uint32_t *it_ncand, *it_coff;            // candidates per item, dense offsets (items + 1)
+    uint32_t *plan_list;                     // items with refills (TOT_PLN of them), k_plan's work queue
     // per chunk / batch slot (cap_chunks; batch b of an item sits at slot it_choff + b)
     uint32_t *ch_g, *ch_meta;
     uint32_t *bt_c0, *bt_c1, *bt_e0, *bt_cnt; // cap_chunks + cap_items slots
@@ -966,6 +968,23 @@ __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
     return v;
 }
 
+// The items whose selected buckets need refills, compacted into k_plan's
+// work list (warp-aggregated appends; order does not matter, items are
+// independent).
+__global__ void __launch_bounds__(256) k_plan_list(MapBufs B) {
+    const uint32_t nitems = B.par->nitems;
+    const uint32_t lane = lane_id();
+    for (uint32_t base = blockIdx.x * 256 + (threadIdx.x & ~31u); base < nitems; base += gridDim.x * 256) {
+        const uint32_t item = base + lane;
+        const bool has = item < nitems && B.it_nch[item] != 0;
+        const uint32_t m = __ballot_sync(0xffffffffu, has);
+        uint32_t at = 0;
+        if (lane == 0 && m) at = atomicAdd(&B.tot[TOT_PLN], (uint32_t)__popc(m));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (has) B.plan_list[at + __popc(m & lanemask_lt())] = item;
+    }
+}
+
 #define PLAN_WARPS 4
 #define PLAN_KEYS 512 // heap keys of an item held in shared memory; more go to global scratch
 
@@ -983,141 +1002,142 @@ struct PlanSmem {
 // seed heap of alignment_rmdup (2194-2419) on shared memory only.
 __global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(const uint32_t *__restrict__ pos, MapBufs B,
                                                           uint64_t cap_chunks, uint64_t cap_elems) {
-    const uint32_t nitems = B.par->nitems;
     __shared__ PlanSmem sm_all[PLAN_WARPS];
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     PlanSmem &S = sm_all[wib];
-    for (uint32_t base = (blockIdx.x * PLAN_WARPS + wib) * 32; base < nitems; base += gridDim.x * PLAN_WARPS * 32) {
-        const uint32_t mine = base + lane < nitems ? B.it_nch[base + lane] : 0u;
-        uint32_t todo = __ballot_sync(0xffffffffu, mine != 0); // items without refills: one batch, set by k_seed
-        while (todo) {
-            const uint32_t t = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const uint32_t item = base + t;
-            const uint32_t nref = __shfl_sync(0xffffffffu, mine, t);
-            const uint32_t rb = B.it_choff[item], eb = B.it_eloff[item];
-            const uint32_t sbase = rb + item;
-            if ((uint64_t)rb + nref > cap_chunks || (uint64_t)eb + B.it_nel[item] > cap_elems) {
-                if (lane == 0) {
-                    atomicOr(&B.tot[TOT_FLAGS], (uint64_t)rb + nref > cap_chunks ? OV_CHUNKS : OV_ELEMS);
-                    B.it_nbat[item] = 0;
-                }
-                continue;
-            }
-            const uint32_t ns = B.it_nsel[item];
-            const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
-            const unsigned long long perm = B.it_perm[item];
-            // seed records in rank order and the offsets of their keys
-            uint32_t carry = 0;
-            for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
-                const uint32_t i = i0 + lane;
-                uint32_t r = 0;
-                if (i < ns) {
-                    const uint2 sv = B.sel[sb + sel_slot(perm, i)];
-                    S.sst[i] = sv.x;
-                    S.scn[i] = sv.y;
-                    S.pc[i] = sv.y > SWM_PER_FETCH ? SWM_PER_FETCH : sv.y; // initial fetch, 2194-2236
-                    r = sv.y > SWM_PER_FETCH ? (sv.y - 1) / SWM_PER_FETCH : 0u;
-                }
-                const uint32_t inc = warp_scan_incl(r);
-                if (i < ns) S.koff[i] = carry + inc - r;
-                carry += __shfl_sync(0xffffffffu, inc, 31);
-            }
-            if (lane == 0) S.koff[ns] = carry; // == nref
-            __syncwarp();
-            uint32_t *keys = nref <= PLAN_KEYS ? S.key : B.plan_keys + rb;
-            for (uint32_t c = lane; c < nref; c += 32) {
-                uint32_t lo = 0, hi = ns; // seed with koff <= c < koff of the next
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (S.koff[mid] <= c) lo = mid;
-                    else hi = mid;
-                }
-                const uint32_t j = c - S.koff[lo];
-                keys[c] = pos[S.sst[lo] + SWM_PER_FETCH * (j + 1) - 1];
-            }
-            __syncwarp();
+    // warps take the items with refills one at a time from the list k_plan_list
+    // built: a heavy item (a read in a large repeat family has thousands of
+    // refills) keeps one warp, and the others move on
+    const uint32_t nlist = B.tot[TOT_PLN];
+    for (;;) {
+        uint32_t idx = 0;
+        if (lane == 0) idx = atomicAdd(&B.tot[TOT_PLQ], 1u);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= nlist) break;
+        const uint32_t item = B.plan_list[idx];
+        const uint32_t nref = B.it_nch[item];
+        const uint32_t rb = B.it_choff[item], eb = B.it_eloff[item];
+        const uint32_t sbase = rb + item;
+        if ((uint64_t)rb + nref > cap_chunks || (uint64_t)eb + B.it_nel[item] > cap_elems) {
             if (lane == 0) {
-                uint32_t hs = 0, rc = 0, e = 0, b = 0, br0 = 0, be0 = 0, npos = 0, runs = 0;
-                for (uint32_t i = 0; i < ns; i++) {
-                    e += S.pc[i];
-                    npos += S.pc[i];
-                    runs += S.pc[i] ? 1u : 0u;
-                }
-                auto key_of = [&](uint32_t i) { return keys[S.koff[i] + S.pc[i] / SWM_PER_FETCH - 1]; };
-                for (uint32_t i = 0; i < ns; i++) { // seeds_heap_insert, 1919-1935 (keys: raw positions)
-                    if (S.pc[i] != S.scn[i]) {
-                        hs++;
-                        S.hloc[hs] = key_of(i);
-                        S.hidx[hs] = i;
-                        uint32_t q = hs;
-                        while (q > 1) {
-                            const uint32_t t = q / 2;
-                            if (S.hloc[t] > S.hloc[q]) {
-                                uint32_t a = S.hloc[t];
-                                S.hloc[t] = S.hloc[q];
-                                S.hloc[q] = a;
-                                a = S.hidx[t];
-                                S.hidx[t] = S.hidx[q];
-                                S.hidx[q] = a;
-                            } else break;
-                            q = t;
-                        }
-                    }
-                }
-                for (;;) { // 2261-2419
-                    if (hs > 0 && npos + SWM_PER_FETCH <= SWM_BATCH_POSITIONS && 1 + 2 * runs < SWM_MAX_RUNS_BLOCK) {
-                        const uint32_t i = S.hidx[1];
-                        const uint32_t left = S.scn[i] - S.pc[i];
-                        const uint32_t get = left > SWM_PER_FETCH ? SWM_PER_FETCH : left;
-                        B.ch_g[rb + rc] = S.sst[i] + S.pc[i];
-                        B.ch_meta[rb + rc] = get | (i << 8);
-                        rc++;
-                        S.pc[i] += get;
-                        e += get;
-                        npos += get;
-                        runs++;
-                        // seeds_heap_pop_and_insert, 1936-1962 (loop bound i * 2 < size)
-                        if (S.pc[i] == S.scn[i]) {
-                            S.hloc[1] = S.hloc[hs];
-                            S.hidx[1] = S.hidx[hs];
-                            hs--;
-                        } else {
-                            S.hloc[1] = key_of(i);
-                        }
-                        uint32_t q = 1;
-                        while (q * 2 < hs) {
-                            uint32_t t = q * 2;
-                            if (q * 2 + 1 <= hs && S.hloc[q * 2] > S.hloc[q * 2 + 1]) t = q * 2 + 1;
-                            if (S.hloc[t] < S.hloc[q]) {
-                                uint32_t a = S.hloc[t];
-                                S.hloc[t] = S.hloc[q];
-                                S.hloc[q] = a;
-                                a = S.hidx[t];
-                                S.hidx[t] = S.hidx[q];
-                                S.hidx[q] = a;
-                            } else break;
-                            q = t;
-                        }
-                    }
-                    if (npos + SWM_PER_FETCH > SWM_BATCH_POSITIONS || hs == 0 || 1 + 2 * runs >= SWM_MAX_RUNS_BLOCK) {
-                        if (npos > 0) {
-                            B.bt_c0[sbase + b] = rb + br0; // refill chunks of the batch; batch 0 also
-                            B.bt_c1[sbase + b] = rb + rc;  // holds every initial chunk
-                            B.bt_e0[sbase + b] = eb + be0;
-                            b++;
-                        }
-                        br0 = rc;
-                        be0 = e;
-                        npos = 0;
-                        runs = 0;
-                        if (hs == 0) break;
-                    }
-                }
-                B.it_nbat[item] = b;
+                atomicOr(&B.tot[TOT_FLAGS], (uint64_t)rb + nref > cap_chunks ? OV_CHUNKS : OV_ELEMS);
+                B.it_nbat[item] = 0;
             }
-            __syncwarp();
+            continue;
         }
+        const uint32_t ns = B.it_nsel[item];
+        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+        const unsigned long long perm = B.it_perm[item];
+        // seed records in rank order and the offsets of their keys
+        uint32_t carry = 0;
+        for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            uint32_t r = 0;
+            if (i < ns) {
+                const uint2 sv = B.sel[sb + sel_slot(perm, i)];
+                S.sst[i] = sv.x;
+                S.scn[i] = sv.y;
+                S.pc[i] = sv.y > SWM_PER_FETCH ? SWM_PER_FETCH : sv.y; // initial fetch, 2194-2236
+                r = sv.y > SWM_PER_FETCH ? (sv.y - 1) / SWM_PER_FETCH : 0u;
+            }
+            const uint32_t inc = warp_scan_incl(r);
+            if (i < ns) S.koff[i] = carry + inc - r;
+            carry += __shfl_sync(0xffffffffu, inc, 31);
+        }
+        if (lane == 0) S.koff[ns] = carry; // == nref
+        __syncwarp();
+        uint32_t *keys = nref <= PLAN_KEYS ? S.key : B.plan_keys + rb;
+        for (uint32_t c = lane; c < nref; c += 32) {
+            uint32_t lo = 0, hi = ns; // seed with koff <= c < koff of the next
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (S.koff[mid] <= c) lo = mid;
+                else hi = mid;
+            }
+            const uint32_t j = c - S.koff[lo];
+            keys[c] = pos[S.sst[lo] + SWM_PER_FETCH * (j + 1) - 1];
+        }
+        __syncwarp();
+        if (lane == 0) {
+            uint32_t hs = 0, rc = 0, e = 0, b = 0, br0 = 0, be0 = 0, npos = 0, runs = 0;
+            for (uint32_t i = 0; i < ns; i++) {
+                e += S.pc[i];
+                npos += S.pc[i];
+                runs += S.pc[i] ? 1u : 0u;
+            }
+            auto key_of = [&](uint32_t i) { return keys[S.koff[i] + S.pc[i] / SWM_PER_FETCH - 1]; };
+            for (uint32_t i = 0; i < ns; i++) { // seeds_heap_insert, 1919-1935 (keys: raw positions)
+                if (S.pc[i] != S.scn[i]) {
+                    hs++;
+                    S.hloc[hs] = key_of(i);
+                    S.hidx[hs] = i;
+                    uint32_t q = hs;
+                    while (q > 1) {
+                        const uint32_t t = q / 2;
+                        if (S.hloc[t] > S.hloc[q]) {
+                            uint32_t a = S.hloc[t];
+                            S.hloc[t] = S.hloc[q];
+                            S.hloc[q] = a;
+                            a = S.hidx[t];
+                            S.hidx[t] = S.hidx[q];
+                            S.hidx[q] = a;
+                        } else break;
+                        q = t;
+                    }
+                }
+            }
+            for (;;) { // 2261-2419
+                if (hs > 0 && npos + SWM_PER_FETCH <= SWM_BATCH_POSITIONS && 1 + 2 * runs < SWM_MAX_RUNS_BLOCK) {
+                    const uint32_t i = S.hidx[1];
+                    const uint32_t left = S.scn[i] - S.pc[i];
+                    const uint32_t get = left > SWM_PER_FETCH ? SWM_PER_FETCH : left;
+                    B.ch_g[rb + rc] = S.sst[i] + S.pc[i];
+                    B.ch_meta[rb + rc] = get | (i << 8);
+                    rc++;
+                    S.pc[i] += get;
+                    e += get;
+                    npos += get;
+                    runs++;
+                    // seeds_heap_pop_and_insert, 1936-1962 (loop bound i * 2 < size)
+                    if (S.pc[i] == S.scn[i]) {
+                        S.hloc[1] = S.hloc[hs];
+                        S.hidx[1] = S.hidx[hs];
+                        hs--;
+                    } else {
+                        S.hloc[1] = key_of(i);
+                    }
+                    uint32_t q = 1;
+                    while (q * 2 < hs) {
+                        uint32_t t = q * 2;
+                        if (q * 2 + 1 <= hs && S.hloc[q * 2] > S.hloc[q * 2 + 1]) t = q * 2 + 1;
+                        if (S.hloc[t] < S.hloc[q]) {
+                            uint32_t a = S.hloc[t];
+                            S.hloc[t] = S.hloc[q];
+                            S.hloc[q] = a;
+                            a = S.hidx[t];
+                            S.hidx[t] = S.hidx[q];
+                            S.hidx[q] = a;
+                        } else break;
+                        q = t;
+                    }
+                }
+                if (npos + SWM_PER_FETCH > SWM_BATCH_POSITIONS || hs == 0 || 1 + 2 * runs >= SWM_MAX_RUNS_BLOCK) {
+                    if (npos > 0) {
+                        B.bt_c0[sbase + b] = rb + br0; // refill chunks of the batch; batch 0 also
+                        B.bt_c1[sbase + b] = rb + rc;  // holds every initial chunk
+                        B.bt_e0[sbase + b] = eb + be0;
+                        b++;
+                    }
+                    br0 = rc;
+                    be0 = e;
+                    npos = 0;
+                    runs = 0;
+                    if (hs == 0) break;
+                }
+            }
+            B.it_nbat[item] = b;
+        }
+        __syncwarp();
     }
 }
 
@@ -2198,7 +2218,7 @@ static int dmalloc(T **p, uint64_t count) {
 
 static void free_bufs(MapBufs &B) {
     void *ps[] = {B.par, B.it_w, B.sel, B.sel_fl, B.it_perm, B.unm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
-                  B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand,
+                  B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand, B.plan_list,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
                   B.tb_cp, B.slow_list, B.vt_x, B.vt_st,
@@ -2234,6 +2254,7 @@ static int alloc_items(swm_mapper *m) {
     rc |= dmalloc(&B.it_woff, I + 1);
     rc |= dmalloc(&B.it_boff, I + 1);
     rc |= dmalloc(&B.it_ncand, I);
+    rc |= dmalloc(&B.plan_list, I);
     rc |= dmalloc(&B.it_coff, I + 1);
     rc |= dmalloc(&B.tot, TOT_N);
     rc |= dmalloc(&B.stat, ST_N);
@@ -2393,9 +2414,10 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     rc = swm_exclusive_scan(B.it_nel, B.it_eloff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_ELEMS, st);
     if (rc) return rc;
     m->launches += 6;
+    k_plan_list<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B);
     k_plan<<<grid_cap(ci, PLAN_WARPS * 32, 16), PLAN_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
                                                                           m->cap_elems);
-    m->launches++;
+    m->launches += 2;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[2], st, cudaEventRecordExternal));
     k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(ix->d_pos, ix->d_ls, B, m->cap_chunks, m->cap_elems,
