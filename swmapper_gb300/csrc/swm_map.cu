@@ -51,7 +51,8 @@ enum {
     TOT_CHUNKS = 0, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES, TOT_ARENA, TOT_FLAGS, TOT_TB, TOT_SLOW,
     TOT_VQ, TOT_TBQ, // work-queue heads of k_verify and k_traceback
     TOT_VT, TOT_VTQ, // candidates alive after the head of verification, and their queue head
-    TOT_PLN, TOT_PLQ, // items with refills, and the queue head of k_plan
+    TOT_PLN, TOT_PLQ,  // items with refills and at most 32 selected seeds, queue head of k_plan_lanes
+    TOT_PLW, TOT_PLWQ, // items with refills and more selected seeds, queue head of k_plan
     TOT_N
 };
 
@@ -88,7 +89,7 @@ struct MapBufs {
     uint32_t *it_nrec, *it_nw, *it_nb;
     uint32_t *it_recoff, *it_woff, *it_boff; // items + 1
     uint32_t *it_ncand, *it_coff;            // candidates per item, dense offsets (items + 1)
-    uint32_t *plan_list;                     // items with refills (TOT_PLN of them), k_plan's work queue
+    uint32_t *plan_list; // items with refills: k_plan_lanes' from the front, k_plan's from the back (items)
     // per chunk / batch slot (cap_chunks; batch b of an item sits at slot it_choff + b)
     uint32_t *ch_g, *ch_meta;
     uint32_t *bt_c0, *bt_c1, *bt_e0, *bt_cnt; // cap_chunks + cap_items slots
@@ -968,20 +969,26 @@ __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
     return v;
 }
 
-// The items whose selected buckets need refills, compacted into k_plan's
-// work list (warp-aggregated appends; order does not matter, items are
-// independent).
+// The items whose selected buckets need refills, compacted into the planners'
+// work lists (warp-aggregated appends; order does not matter, items are
+// independent): items with at most PLAN_LANE_SEEDS selected seeds from the
+// front for k_plan_lanes, the others from the back for k_plan.
+#define PLAN_LANE_SEEDS 32
 __global__ void __launch_bounds__(256) k_plan_list(MapBufs B) {
     const uint32_t nitems = B.par->nitems;
     const uint32_t lane = lane_id();
     for (uint32_t base = blockIdx.x * 256 + (threadIdx.x & ~31u); base < nitems; base += gridDim.x * 256) {
         const uint32_t item = base + lane;
         const bool has = item < nitems && B.it_nch[item] != 0;
-        const uint32_t m = __ballot_sync(0xffffffffu, has);
-        uint32_t at = 0;
-        if (lane == 0 && m) at = atomicAdd(&B.tot[TOT_PLN], (uint32_t)__popc(m));
-        at = __shfl_sync(0xffffffffu, at, 0);
-        if (has) B.plan_list[at + __popc(m & lanemask_lt())] = item;
+        const bool few = has && B.it_nsel[item] <= PLAN_LANE_SEEDS;
+        const uint32_t mf = __ballot_sync(0xffffffffu, few), mm = __ballot_sync(0xffffffffu, has && !few);
+        uint32_t af = 0, am = 0;
+        if (lane == 0 && mf) af = atomicAdd(&B.tot[TOT_PLN], (uint32_t)__popc(mf));
+        if (lane == 0 && mm) am = atomicAdd(&B.tot[TOT_PLW], (uint32_t)__popc(mm));
+        af = __shfl_sync(0xffffffffu, af, 0);
+        am = __shfl_sync(0xffffffffu, am, 0);
+        if (few) B.plan_list[af + __popc(mf & lanemask_lt())] = item;
+        if (has && !few) B.plan_list[nitems - 1 - (am + __popc(mm & lanemask_lt()))] = item;
     }
 }
 
@@ -1008,13 +1015,13 @@ __global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(const uint32_t *__rest
     // warps take the items with refills one at a time from the list k_plan_list
     // built: a heavy item (a read in a large repeat family has thousands of
     // refills) keeps one warp, and the others move on
-    const uint32_t nlist = B.tot[TOT_PLN];
+    const uint32_t nlist = B.tot[TOT_PLW], nitems = B.par->nitems;
     for (;;) {
         uint32_t idx = 0;
-        if (lane == 0) idx = atomicAdd(&B.tot[TOT_PLQ], 1u);
+        if (lane == 0) idx = atomicAdd(&B.tot[TOT_PLWQ], 1u);
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= nlist) break;
-        const uint32_t item = B.plan_list[idx];
+        const uint32_t item = B.plan_list[nitems - 1 - idx];
         const uint32_t nref = B.it_nch[item];
         const uint32_t rb = B.it_choff[item], eb = B.it_eloff[item];
         const uint32_t sbase = rb + item;
@@ -1138,6 +1145,180 @@ __global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(const uint32_t *__rest
             B.it_nbat[item] = b;
         }
         __syncwarp();
+    }
+}
+
+// Lane-per-item refill planning for the items with at most PLAN_LANE_SEEDS
+// selected seeds: each lane runs one item's seed heap, the same schedule as
+// k_plan (alignment_rmdup 2194-2419 with the heap of 1919-1962 and its sift
+// bound), and a lane whose item is planned takes the next item from the list.
+// The heap key of seed i is the raw position of the last entry fetched from
+// it, pos[start + fetched - 1], loaded when the seed goes back into the heap.
+// Per-lane state sits in shared memory as [slot][lane], so the lanes' accesses
+// never share a bank.
+#define PLAN_LANE_WARPS 2
+
+struct PlanLaneSmem {
+    uint32_t sst[PLAN_LANE_SEEDS][32], scn[PLAN_LANE_SEEDS][32], pc[PLAN_LANE_SEEDS][32];
+    uint32_t hloc[PLAN_LANE_SEEDS + 1][32];
+    uint8_t hidx[PLAN_LANE_SEEDS + 1][32];
+};
+
+__global__ void __launch_bounds__(PLAN_LANE_WARPS * 32) k_plan_lanes(const uint32_t *__restrict__ pos, MapBufs B,
+                                                                     uint64_t cap_chunks, uint64_t cap_elems) {
+    __shared__ PlanLaneSmem sm_all[PLAN_LANE_WARPS];
+    const uint32_t lane = lane_id();
+    PlanLaneSmem &S = sm_all[threadIdx.x >> 5];
+    const uint32_t nlist = B.tot[TOT_PLN];
+    bool active = false, drained = false;
+    uint32_t item = 0, hs = 0, rc = 0, rb = 0, eb = 0, sbase = 0, e = 0, b = 0, br0 = 0, be0 = 0, npos = 0, runs = 0;
+    for (;;) {
+        // lanes without an item take the next ones from the list (one atomic per warp)
+        const bool need = !active && !drained;
+        const uint32_t m = __ballot_sync(0xffffffffu, need);
+        if (m) {
+            const uint32_t leader = __ffs(m) - 1;
+            uint32_t first = 0;
+            if (lane == leader) first = atomicAdd(&B.tot[TOT_PLQ], (uint32_t)__popc(m));
+            first = __shfl_sync(0xffffffffu, first, leader);
+            if (need) {
+                const uint32_t idx = first + __popc(m & lanemask_lt());
+                if (idx >= nlist) {
+                    drained = true;
+                } else {
+                    item = B.plan_list[idx];
+                    const uint32_t nref = B.it_nch[item];
+                    rb = B.it_choff[item];
+                    eb = B.it_eloff[item];
+                    sbase = rb + item;
+                    if ((uint64_t)rb + nref > cap_chunks || (uint64_t)eb + B.it_nel[item] > cap_elems) {
+                        atomicOr(&B.tot[TOT_FLAGS], (uint64_t)rb + nref > cap_chunks ? OV_CHUNKS : OV_ELEMS);
+                        B.it_nbat[item] = 0;
+                    } else {
+                        const uint32_t ns = B.it_nsel[item];
+                        const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+                        const unsigned long long perm = B.it_perm[item];
+                        e = npos = runs = hs = rc = b = br0 = be0 = 0;
+                        // seed records in rank order and the initial fetch (2194-2236), 8 loads in flight
+                        for (uint32_t i0 = 0; i0 < ns; i0 += 8) {
+                            uint2 sv[8];
+#pragma unroll
+                            for (uint32_t j = 0; j < 8; j++)
+                                sv[j] = i0 + j < ns ? B.sel[sb + sel_slot(perm, i0 + j)] : make_uint2(0u, 0u);
+#pragma unroll
+                            for (uint32_t j = 0; j < 8; j++) {
+                                if (i0 + j >= ns) break;
+                                const uint32_t pc0 = sv[j].y > SWM_PER_FETCH ? SWM_PER_FETCH : sv[j].y;
+                                S.sst[i0 + j][lane] = sv[j].x;
+                                S.scn[i0 + j][lane] = sv[j].y;
+                                S.pc[i0 + j][lane] = pc0;
+                                e += pc0;
+                                npos += pc0;
+                                runs += pc0 ? 1u : 0u;
+                            }
+                        }
+                        // seeds_heap_insert (1919-1935) of the seeds with entries left, in
+                        // seed order; their keys loaded 8 at a time
+                        for (uint32_t i0 = 0; i0 < ns; i0 += 8) {
+                            uint32_t key[8];
+                            bool ins[8];
+#pragma unroll
+                            for (uint32_t j = 0; j < 8; j++) {
+                                const uint32_t i = i0 + j;
+                                ins[j] = i < ns && S.pc[i][lane] != S.scn[i][lane];
+                                key[j] = pos[ins[j] ? S.sst[i][lane] + S.pc[i][lane] - 1 : 0u];
+                            }
+#pragma unroll
+                            for (uint32_t j = 0; j < 8; j++) {
+                                if (!ins[j]) continue;
+                                uint32_t q = ++hs;
+                                while (q > 1) {
+                                    const uint32_t t = q / 2, pk = S.hloc[t][lane];
+                                    if (pk > key[j]) {
+                                        S.hloc[q][lane] = pk;
+                                        S.hidx[q][lane] = S.hidx[t][lane];
+                                        q = t;
+                                    } else {
+                                        break;
+                                    }
+                                }
+                                S.hloc[q][lane] = key[j];
+                                S.hidx[q][lane] = (uint8_t)(i0 + j);
+                            }
+                        }
+                        active = true;
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (__all_sync(0xffffffffu, drained)) break;
+            continue;
+        }
+        if (!active) continue;
+        // one refill (2261-2419), then the batch bounds
+        if (hs > 0 && npos + SWM_PER_FETCH <= SWM_BATCH_POSITIONS && 1 + 2 * runs < SWM_MAX_RUNS_BLOCK) {
+            const uint32_t i = S.hidx[1][lane];
+            const uint32_t st = S.sst[i][lane], cn = S.scn[i][lane];
+            uint32_t pc = S.pc[i][lane];
+            const uint32_t left = cn - pc;
+            const uint32_t get = left > SWM_PER_FETCH ? SWM_PER_FETCH : left;
+            B.ch_g[rb + rc] = st + pc;
+            B.ch_meta[rb + rc] = get | (i << 8);
+            rc++;
+            pc += get;
+            S.pc[i][lane] = pc;
+            e += get;
+            npos += get;
+            runs++;
+            // seeds_heap_pop_and_insert (1936-1962): the root leaves or takes
+            // the seed's next key, then sinks while q * 2 < size
+            uint32_t xk, xi;
+            if (pc == cn) {
+                xk = S.hloc[hs][lane];
+                xi = S.hidx[hs][lane];
+                hs--;
+            } else {
+                xk = pos[st + pc - 1];
+                xi = i;
+            }
+            uint32_t q = 1;
+            while (q * 2 < hs) {
+                uint32_t t = q * 2, kt = S.hloc[t][lane];
+                if (t + 1 <= hs) {
+                    const uint32_t k2 = S.hloc[t + 1][lane];
+                    if (kt > k2) {
+                        t++;
+                        kt = k2;
+                    }
+                }
+                if (kt < xk) {
+                    S.hloc[q][lane] = kt;
+                    S.hidx[q][lane] = S.hidx[t][lane];
+                    q = t;
+                } else {
+                    break;
+                }
+            }
+            S.hloc[q][lane] = xk;
+            S.hidx[q][lane] = (uint8_t)xi;
+        }
+        if (npos + SWM_PER_FETCH > SWM_BATCH_POSITIONS || hs == 0 || 1 + 2 * runs >= SWM_MAX_RUNS_BLOCK) {
+            if (npos > 0) {
+                B.bt_c0[sbase + b] = rb + br0; // refill chunks of the batch; batch 0 also
+                B.bt_c1[sbase + b] = rb + rc;  // holds every initial chunk
+                B.bt_e0[sbase + b] = eb + be0;
+                b++;
+            }
+            br0 = rc;
+            be0 = e;
+            npos = 0;
+            runs = 0;
+            if (hs == 0) {
+                B.it_nbat[item] = b;
+                active = false;
+            }
+        }
     }
 }
 
@@ -2415,9 +2596,11 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     if (rc) return rc;
     m->launches += 6;
     k_plan_list<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B);
+    k_plan_lanes<<<grid_cap(ci, PLAN_LANE_WARPS * 32, 6), PLAN_LANE_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
+                                                                                         m->cap_elems);
     k_plan<<<grid_cap(ci, PLAN_WARPS * 32, 16), PLAN_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
                                                                           m->cap_elems);
-    m->launches += 2;
+    m->launches += 3;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[2], st, cudaEventRecordExternal));
     k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(ix->d_pos, ix->d_ls, B, m->cap_chunks, m->cap_elems,
