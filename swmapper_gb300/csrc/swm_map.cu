@@ -1157,6 +1157,9 @@ __global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(const uint32_t *__rest
 // Per-lane state sits in shared memory as [slot][lane], so the lanes' accesses
 // never share a bank.
 #define PLAN_LANE_WARPS 2
+#ifndef PLAN_LANE_REFILL
+#define PLAN_LANE_REFILL 16
+#endif
 
 struct PlanLaneSmem {
     uint32_t sst[PLAN_LANE_SEEDS][32], scn[PLAN_LANE_SEEDS][32], pc[PLAN_LANE_SEEDS][32];
@@ -1173,10 +1176,12 @@ __global__ void __launch_bounds__(PLAN_LANE_WARPS * 32) k_plan_lanes(const uint3
     bool active = false, drained = false;
     uint32_t item = 0, hs = 0, rc = 0, rb = 0, eb = 0, sbase = 0, e = 0, b = 0, br0 = 0, be0 = 0, npos = 0, runs = 0;
     for (;;) {
-        // lanes without an item take the next ones from the list (one atomic per warp)
+        // lanes without an item take the next ones from the list (one atomic per
+        // warp), once PLAN_LANE_REFILL of them wait or none is busy: the warp
+        // stands still while a lane sets up an item, so set-ups go in groups
         const bool need = !active && !drained;
         const uint32_t m = __ballot_sync(0xffffffffu, need);
-        if (m) {
+        if (m && (__popc(m) >= PLAN_LANE_REFILL || !__any_sync(0xffffffffu, active))) {
             const uint32_t leader = __ffs(m) - 1;
             uint32_t first = 0;
             if (lane == leader) first = atomicAdd(&B.tot[TOT_PLQ], (uint32_t)__popc(m));
