@@ -146,9 +146,13 @@ def shard_seed(rank):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons every 100 ms, time-stamped. The
+    sampler starts before the warm-up (nvidia-smi takes a moment to come up)
+    and stop(t0, t1) keeps the samples taken inside the timed window [t0, t1]
+    (wall clock); a window shorter than the interval keeps the first sample
+    after t0 and the last before it instead ("window": "nearest")."""
 
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
@@ -159,32 +163,51 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
 
-    def stop(self):
+    @staticmethod
+    def _stamp(text):
+        import datetime
+        for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
+            try:
+                return datetime.datetime.strptime(text, fmt).timestamp()
+            except ValueError:
+                continue
+        return None
+
+    def stop(self, t0=None, t1=None):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
         out, _ = self.proc.communicate(timeout=10)
-        sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in out.strip().splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 7:
+            if len(f) < 8:
                 continue
             try:
-                sm.append(float(f[0]))
-                mx.append(float(f[1]))
+                rows.append((self._stamp(f[0]), float(f[1]), float(f[2]),
+                             {nm for nm, v in zip(names, f[4:8]) if v.lower().startswith("active")}))
             except ValueError:
                 continue
-            for nm, v in zip(names, f[3:7]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
+        window = "all"
+        if t0 is not None and rows and all(r[0] is not None for r in rows):
+            inside = [r for r in rows if t0 <= r[0] <= t1]
+            if inside:
+                rows, window = inside, "timed region"
+            else:
+                before = [r for r in rows if r[0] < t0][-1:]
+                after = [r for r in rows if r[0] > t1][:1]
+                rows, window = before + after, "nearest"
+        sm = [r[1] for r in rows]
+        mx = [r[2] for r in rows]
+        reasons = set().union(*[r[3] for r in rows]) if rows else set()
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+                "samples": len(sm), "window": window, "reasons": sorted(reasons)}
 
 
 def measured_peaks():
@@ -429,11 +452,12 @@ def run_gpu(args):
         rt.cudaEventElapsedTime(C.byref(ms), ev0, ev1)
         return ms.value / 1000.0
 
-    run_steps(args.warmup, None)
-    acc = {}
     clocks = ClockSampler(local)
     clocks.start()
+    run_steps(args.warmup, None)
+    acc = {}
     dist.barrier()
+    t_wall0 = time.time()
     if flush: # one step at a time, L2 flushed (outside the events) before each
         elapsed = 0.0
         for _ in range(args.steps):
@@ -442,7 +466,7 @@ def run_gpu(args):
     else:
         elapsed = timed(args.steps, acc)
     dist.barrier()
-    clk = clocks.stop()
+    clk = clocks.stop(t_wall0, time.time())
     tot_elapsed, tot_mapped, tot_cells = aggregate(dist, elapsed, [acc["mapped_reads"], acc["cells"]])
     value = tot_mapped / tot_elapsed
     # kernel times in isolation (one mapper, one block at a time) for the
@@ -574,8 +598,9 @@ def run_gpu(args):
             "config": {**WORKLOAD, "block_reads": block, "mappers": args.mappers,
                        "autotune": tuned, "length_buckets": bucketed,
                        "parallelism": f"replicas x{ws} (reads sharded by rank)",
-                       "l2": (f"inputs {input_bytes / 1e6:.0f} MB < L2: L2 flushed ({L2_FLUSH_BYTES >> 20} MiB write) "
-                              f"before each timed step" if flush else
+                       "l2": (f"inputs {input_bytes / 1e6:.0f} MB (under {L2_FLUSH_BYTES >> 20} MiB, so treated as "
+                              f"possibly cache-resident): L2 flushed ({L2_FLUSH_BYTES >> 20} MiB write) before each "
+                              f"timed step" if flush else
                               f"inputs larger than L2 (reads {reads.nbytes / 1e6:.0f} MB, index "
                               f"{index_bytes / 1e9:.2f} GB); no flush")},
             "gcups": round(gcups, 2), "index_build_s": round(index_build_s, 3),
