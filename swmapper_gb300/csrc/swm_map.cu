@@ -1348,16 +1348,6 @@ __device__ __forceinline__ void warp_sort_k(uint32_t &v) {
     }
 }
 
-// Ascending sort of the values of lanes 0 .. n - 1 (n <= 32, uniform).
-__device__ __forceinline__ void warp_sort_small(uint32_t &v, uint32_t n) {
-    if (n <= 1) return;
-    if (n <= 2) warp_sort_k<2>(v);
-    else if (n <= 4) warp_sort_k<4>(v);
-    else if (n <= 8) warp_sort_k<8>(v);
-    else if (n <= 16) warp_sort_k<16>(v);
-    else warp_sort_k<32>(v);
-}
-
 #define CAND_MAXCH 128 // chunks (runs) per batch: block_size < 256 allows at most 128
 
 #define CAND_SMEM_KEEP 64 // survivors of a batch held in shared memory (more go to global scratch)
