@@ -1348,6 +1348,55 @@ __device__ __forceinline__ void warp_sort_k(uint32_t &v) {
     }
 }
 
+// Ascending sort of the first n <= 32 K values of buf, held in registers as
+// element k * 32 + lane (bitonic network: strides >= 32 within a lane,
+// smaller ones across lanes by shuffles), then the distinct values written to
+// dst in order. Returns how many were written. 0xffffffff pads and never
+// occurs as a position.
+template <int K>
+__device__ __forceinline__ uint32_t warp_sort_unique(const uint32_t *buf, uint32_t n, uint32_t *dst) {
+    const uint32_t lane = lane_id();
+    uint32_t v[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = k * 32 + lane < n ? buf[k * 32 + lane] : 0xffffffffu;
+#pragma unroll
+    for (uint32_t size = 2; size <= 32 * K; size <<= 1) {
+#pragma unroll
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride >= 32) { // partner k ^ (stride / 32) of the same lane; size >= 64
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const int ks = (int)(stride / 32);
+                    if (k & ks) continue;
+                    const bool up = ((k * 32) & size) == 0;
+                    const uint32_t a = v[k], d = v[k | ks];
+                    v[k] = up ? min(a, d) : max(a, d);
+                    v[k | ks] = up ? max(a, d) : min(a, d);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const uint32_t w = __shfl_xor_sync(0xffffffffu, v[k], stride);
+                    const bool up = ((k * 32 + lane) & size) == 0, lower = (lane & stride) == 0;
+                    v[k] = (lower == up) ? min(v[k], w) : max(v[k], w);
+                }
+            }
+        }
+    }
+    uint32_t u = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const uint32_t above = __shfl_up_sync(0xffffffffu, v[k], 1);
+        const uint32_t last = __shfl_sync(0xffffffffu, k ? v[k ? k - 1 : 0] : 0u, 31);
+        const uint32_t prev = lane ? above : last;
+        const bool keep = v[k] != 0xffffffffu && ((k == 0 && lane == 0) || v[k] != prev);
+        const uint32_t m = __ballot_sync(0xffffffffu, keep);
+        if (keep) dst[u + __popc(m & lanemask_lt())] = v[k];
+        u += __popc(m);
+    }
+    return u;
+}
+
 #define CAND_MAXCH 128 // chunks (runs) per batch: block_size < 256 allows at most 128
 
 #define CAND_SMEM_KEEP 64 // survivors of a batch held in shared memory (more go to global scratch)
@@ -1507,8 +1556,14 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
                         if (keep) dst[u + __popc(m & lanemask_lt())] = v;
                         u += __popc(m);
                     }
-                } else {
-                    uint32_t n2 = 64;
+                } else if (kept <= 64) {
+                    u = warp_sort_unique<2>(S.sc, kept, dst);
+                } else if (kept <= 128) {
+                    u = warp_sort_unique<4>(gscratch(), kept, dst);
+                } else if (kept <= 256) {
+                    u = warp_sort_unique<8>(gscratch(), kept, dst);
+                } else { // bitonic sort in the warp's global scratch
+                    uint32_t n2 = 512;
                     while (n2 < kept) n2 <<= 1;
                     uint32_t *buf = spilled ? gscratch() : S.sc;
                     for (uint32_t i = kept + lane; i < n2; i += 32) buf[i] = 0xffffffffu;
