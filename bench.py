@@ -398,7 +398,7 @@ def run_gpu(args):
     rt.cudaStreamWaitEvent.argtypes = [C.c_void_p, C.c_void_p, C.c_uint]
     blocks = [(b0, min(block, nreads - b0)) for b0 in range(0, nreads, block)]
     COUNTERS = ("mapped_reads", "candidates", "cells", "passed", "fetched", "chunks", "batches", "items",
-                "locations", "records", "retries")
+                "locations", "records", "retries", "myers_steps")
 
     def run_steps(nsteps, acc):
         """nsteps passes over the reads as one continuous stream of blocks."""
@@ -580,16 +580,20 @@ def run_gpu(args):
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                 "fallback 6.8 TB/s"}
-    # integer-pipe view of the Myers kernel (the hot loop is LOP3/IADD/SHF work)
+    # integer-pipe view of the Myers kernel: its hot loop is LOP3 / SHF / IADD
+    # work on the ALU pipe, which takes one warp instruction every second cycle
+    # per SM sub-partition (ncu: sm__pipe_alu_cycles_active exceeds the issue
+    # rate on this kernel), so 16 lanes x 4 sub-partitions per SM
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    int_peak = 152 * 128 * sm_mhz * 1e6 / 1e12
-    myers_ops = per_step["candidates"] * L * 21
+    int_peak = 152 * 64 * sm_mhz * 1e6 / 1e12
+    myers_ops = per_step["myers_steps"] * 21
     t_verify = per_step["ms_verify"] / 1e3
     int_pipe = {"kernel": "k_verify", "ops_per_step": int(myers_ops), "achieved_tops": round(myers_ops / t_verify / 1e12, 2)
                 if t_verify > 0 else None, "peak_tops": round(int_peak, 2),
                 "frac": round(myers_ops / t_verify / 1e12 / int_peak, 4) if t_verify > 0 else None,
-                "ops_model": "21 int ops per read base per candidate (17 recurrence + 4 Peq update)",
-                "peak_model": "152 SMs x 128 int lanes x median SM clock under load"}
+                "ops_model": "21 int ops per executed Myers step (17 recurrence + 4 pattern word), steps counted "
+                             "on the device over both passes (the head stops hopeless candidates after 64 bases)",
+                "peak_model": "152 SMs x 64 ALU-pipe lanes (16 per sub-partition) x median SM clock under load"}
 
     line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(tot_elapsed / args.steps * 1e3, 3),

@@ -145,6 +145,8 @@ typedef struct {
     uint64_t retries;           /* block re-runs after growing a work buffer     */
     uint64_t h2d_bytes;         /* host -> device bytes of the block (0 when resident) */
     uint64_t d2h_bytes;         /* device -> host bytes of the block's results   */
+    uint64_t myers_steps;       /* read bases run through the Myers recurrence,
+                                   summed over candidates and both passes       */
 } swm_map_stats;
 
 /* Create a mapping context on the index's device with its own CUDA stream and

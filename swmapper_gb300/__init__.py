@@ -47,7 +47,7 @@ class PackedResult(C.Structure):
 
 
 STAT_FIELDS = ["reads", "items", "chunks", "batches", "fetched", "candidates", "cells", "passed", "records",
-               "locations", "mapped_reads", "retries", "h2d_bytes", "d2h_bytes"]
+               "locations", "mapped_reads", "retries", "h2d_bytes", "d2h_bytes", "myers_steps"]
 
 
 class MapStats(C.Structure):

@@ -44,6 +44,7 @@ enum {
     ST_PASSED,
     ST_LOCS,
     ST_MAPPED,
+    ST_STEPS, // Myers steps (read bases) run by k_verify
     ST_N
 };
 // device totals (u32), written by the scans
@@ -1819,7 +1820,7 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
     } else {
         n = B.tot[TOT_VT];
     }
-    unsigned long long cells = 0, passed = 0;
+    unsigned long long cells = 0, passed = 0, steps = 0;
     for (;;) { // persistent warps take work 32 at a time from the queue
         const uint32_t jb = warp_take(&B.tot[HEAD ? TOT_VQ : TOT_VTQ]);
         if (jb >= n) break;
@@ -1861,8 +1862,9 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
 #pragma unroll
         for (int i = 0; i < 16; i++) rw[i] = (HEAD && i >= 2 * VERIFY_HEAD_BLOCKS) ? 0u : RW[i];
         const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
-        myers_blocks(WL, WH, rw, L, MASK, HEAD ? 0u : VERIFY_HEAD_BLOCKS,
-                     HEAD ? min(nblk, (uint32_t)VERIFY_HEAD_BLOCKS) : nblk, vp, vn, ones, cp);
+        const uint32_t b0 = HEAD ? 0u : VERIFY_HEAD_BLOCKS, b1 = HEAD ? min(nblk, (uint32_t)VERIFY_HEAD_BLOCKS) : nblk;
+        steps += min(L, 32 * b1) - 32 * b0;
+        myers_blocks(WL, WH, rw, L, MASK, b0, b1, vp, vn, ones, cp);
         if (head_only) {
             if (32 * VERIFY_HEAD_BLOCKS - ones > 3 * e) { // cannot end at or below e
                 cells += (unsigned long long)L * (2 * e + 1);
@@ -1921,6 +1923,7 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
     }
     warp_add_u64(&B.stat[ST_CELLS], cells);
     warp_add_u64(&B.stat[ST_PASSED], passed);
+    warp_add_u64(&B.stat[ST_STEPS], steps);
 }
 
 
@@ -2825,6 +2828,7 @@ static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *a
     S.records = m->tot[TOT_RECS];
     S.locations = stat[ST_LOCS];
     S.mapped_reads = stat[ST_MAPPED];
+    S.myers_steps = stat[ST_STEPS];
     S.retries = retries;
     S.h2d_bytes = m->h2d_pending;
     m->h2d_pending = 0;

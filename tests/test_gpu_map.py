@@ -51,6 +51,10 @@ def test_gpu_plain_1mbp(cuda_lib):
     st = m.stats()
     assert st["candidates"] == ref.stats["candidates"]
     assert st["mapped_reads"] == ref.stats["mapped_reads"]
+    # every passing candidate runs all 100 read bases through the recurrence;
+    # no candidate runs more
+    assert 100 * st["passed"] <= st["myers_steps"] <= 100 * st["candidates"]
+    assert st["myers_steps"] >= 64 * st["candidates"] // 2
 
 
 def test_gpu_repeats_multibatch(cuda_lib):
