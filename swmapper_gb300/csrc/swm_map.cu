@@ -1797,14 +1797,34 @@ __device__ __forceinline__ void load_window(const uint32_t *__restrict__ b2, uin
 #define TB_TEXT_MAX 2304 // >= 4 bytes x every route entry a bounded walk can make
 
 // Verification in two passes. The head runs the first VERIFY_HEAD_BLOCKS
-// 32-base blocks of every candidate. The error at the band's site only grows
-// with more steps, and the final scan can lower it by at most
-// last_high <= 2e, so a candidate whose site error is already above 3e
-// cannot end at or below e: the full scan would return (SWM_MAXERROR, -1),
-// and the head writes that result at once. The others are queued with their
-// state, and the tail finishes them. On the benchmark genomes a third to
-// half of all candidates stop in the head.
+// 32-base blocks of every candidate, the tail finishes the ones that can
+// still end at or below e, queued with their state.
+//
+// The band of step i holds the edit-distance cells of read prefix i against
+// window positions i .. i + 31: cell 0 is the site error, and bit k of VP /
+// VN says that cell k + 1 is one above / below cell k. The final scan
+// (mapper_cpe.c:634-650) reports the first of cells 0 .. last_high of the
+// last step that is <= e. No cell of a later step is below the minimum of
+// cells 0 .. last_high of this step: every cell is a diagonal (+0 or +1), an
+// up (+1) or a left (+1) move from cells of the previous step or its own, and
+// a path into the scan range from cell k > last_high needs k - last_high up
+// moves while (cell k) + k never decreases as k grows. So when that minimum is
+// already above e after the head, the full run would return
+// (SWM_MAXERROR, -1), and the head writes that result at once. On the
+// human-scale genome most candidates stop there.
 #define VERIFY_HEAD_BLOCKS 2
+
+// Minimum over cells 0 .. lh of a band: site error err, vertical steps VP /
+// VN (the reference's final scan, taking the minimum instead of the first
+// hit). A fixed-length loop: early exits measured slower.
+__device__ __forceinline__ int band_scan_min(int err, uint32_t vp, uint32_t vn, int lh) {
+    int m = err;
+    for (int k = 0; k < lh; k++) {
+        err += (int)((vp >> k) & 1u) - (int)((vn >> k) & 1u);
+        m = min(m, err);
+    }
+    return m;
+}
 
 template <bool HEAD>
 __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
@@ -1866,7 +1886,7 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
         steps += min(L, 32 * b1) - 32 * b0;
         myers_blocks(WL, WH, rw, L, MASK, b0, b1, vp, vn, ones, cp);
         if (head_only) {
-            if (32 * VERIFY_HEAD_BLOCKS - ones > 3 * e) { // cannot end at or below e
+            if (band_scan_min(32 * VERIFY_HEAD_BLOCKS - (int)ones, vp, vn, (int)rl - (int)L) > (int)e) {
                 cells += (unsigned long long)L * (2 * e + 1);
                 B.vr_err[c] = SWM_MAXERROR;
                 B.vr_mloc[c] = -1;
