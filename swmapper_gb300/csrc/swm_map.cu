@@ -1601,30 +1601,64 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
 }
 
 // Dense candidate list: item by item, batch by batch, in verification order.
+#define COMPACT_HEAVY 16 // candidates above which an item is copied by its whole warp
+
 __global__ void __launch_bounds__(256) k_compact(MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
                                                  uint64_t cap_cands) {
     const uint32_t nitems = B.par->nitems;
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
-    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
+    const uint32_t lane = lane_id();
+    // warp-uniform loop over groups of 32 items
+    for (uint32_t item0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); item0 < nitems;
+         item0 += gridDim.x * blockDim.x) {
+        const uint32_t item = item0 + lane;
         // one thread per item: its scalars in one round trip, then its few
-        // candidates batch by batch
-        const uint32_t nb = B.it_nbat[item], nref = B.it_nch[item];
-        const uint32_t o0 = B.it_coff[item], nc = B.it_ncand[item];
-        const uint32_t sbase = B.it_choff[item] + item, eloff = B.it_eloff[item];
-        if (!nb) continue;
-        if ((uint64_t)o0 + nc > cap_cands) {
-            atomicOr(&B.tot[TOT_FLAGS], OV_CANDS);
-            continue;
-        }
-        uint32_t o = o0;
-        for (uint32_t b = 0; b < nb; b++) {
-            const uint32_t n = nref ? B.bt_cnt[sbase + b] : nc; // one batch when there are no refills
-            const uint32_t e0 = nref ? B.bt_e0[sbase + b] : eloff;
-            for (uint32_t j = 0; j < n; j++) {
-                B.cc_pos[o + j] = B.cand_ub[e0 + j];
-                B.cc_item[o + j] = item;
+        // candidates batch by batch; items with many candidates are left to
+        // the whole warp below
+        uint32_t nb = 0, nref = 0, o0 = 0, nc = 0, sbase = 0, eloff = 0;
+        bool heavy = false;
+        if (item < nitems) {
+            nb = B.it_nbat[item];
+            nref = B.it_nch[item];
+            o0 = B.it_coff[item];
+            nc = B.it_ncand[item];
+            sbase = B.it_choff[item] + item;
+            eloff = B.it_eloff[item];
+            if (nb && (uint64_t)o0 + nc > cap_cands) {
+                atomicOr(&B.tot[TOT_FLAGS], OV_CANDS);
+                nb = 0;
             }
-            o += n;
+            heavy = nb && nc > COMPACT_HEAVY;
+            if (nb && !heavy) {
+                uint32_t o = o0;
+                for (uint32_t b = 0; b < nb; b++) {
+                    const uint32_t n = nref ? B.bt_cnt[sbase + b] : nc; // one batch when there are no refills
+                    const uint32_t e0 = nref ? B.bt_e0[sbase + b] : eloff;
+                    for (uint32_t j = 0; j < n; j++) {
+                        B.cc_pos[o + j] = B.cand_ub[e0 + j];
+                        B.cc_item[o + j] = item;
+                    }
+                    o += n;
+                }
+            }
+        }
+        uint32_t hm = __ballot_sync(0xffffffffu, heavy);
+        while (hm) { // the warp copies each heavy item of the group, lanes over its candidates
+            const uint32_t src = __ffs(hm) - 1;
+            hm &= hm - 1;
+            const uint32_t hnb = __shfl_sync(0xffffffffu, nb, src), hnref = __shfl_sync(0xffffffffu, nref, src);
+            const uint32_t hnc = __shfl_sync(0xffffffffu, nc, src), hsb = __shfl_sync(0xffffffffu, sbase, src);
+            const uint32_t hel = __shfl_sync(0xffffffffu, eloff, src);
+            uint32_t o = __shfl_sync(0xffffffffu, o0, src);
+            for (uint32_t b = 0; b < hnb; b++) {
+                const uint32_t n = hnref ? B.bt_cnt[hsb + b] : hnc;
+                const uint32_t e0 = hnref ? B.bt_e0[hsb + b] : hel;
+                for (uint32_t j = lane; j < n; j += 32) {
+                    B.cc_pos[o + j] = B.cand_ub[e0 + j];
+                    B.cc_item[o + j] = item0 + src;
+                }
+                o += n;
+            }
         }
     }
 }
