@@ -580,6 +580,34 @@ def run_gpu(args):
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                 "fallback 6.8 TB/s"}
+    # gather view of the seed and candidate kernels: they read scattered 32-byte
+    # sectors (bucket offsets; flank codes and positions), so their ceiling is
+    # the rate at which the device serves random sector reads from an array of
+    # their footprint (L2 and DRAM in the proportion that footprint gives),
+    # measured here by a probe kernel
+    gather = None
+    if rank == 0 and ws == 1 and args.workload == "batched":  # per-unit sector counts: batched genome
+        kernels = {}
+        for kern, stage, unit_key, foot in (("k_cand", "candidates", "fetched", 6 * inf.n_seeds),
+                                            ("k_seed12", "seed", "items", 4 << (2 * inf.k))):
+            tr = profile_traffic(kern) or {}
+            spu = tr.get(f"l2_sectors_per_{unit_key}")
+            t_s = per_step["ms_" + stage] / 1e3
+            if not spu or t_s <= 0 or (kern == "k_seed12" and w["k"] != 12):
+                continue
+            foot = max(int(foot), 1 << 20)
+            pk = swm.probe_random_reads(foot, local)
+            ach = spu * per_step[unit_key] / t_s
+            kernels[kern] = {"achieved": round(ach / 1e9, 1), "peak": round(pk / 1e9, 1), "frac": round(ach / pk, 3),
+                             "footprint_bytes": foot, "sectors_per_unit": spu, "unit_of_work": unit_key}
+        gather = {"unit": "G sectors/s",
+                  "peak_model": "swm_probe_random_reads in this run: 4-byte reads from random 32-byte sectors of a "
+                                "buffer of the kernel's gathered footprint (positions + flank codes; bucket "
+                                "offsets), 8 in flight per thread, best of 5 launches",
+                  "achieved_model": "32-byte sectors the kernel requests from L2 per unit of work (ncu "
+                                    "lts__t_sectors_srcunit_tex_op_read, profiles/<kernel>_traffic.txt) x units / "
+                                    "kernel time", "kernels": kernels}
+
     # integer-pipe view of the Myers kernel: its hot loop is LOP3 / SHF / IADD
     # work on the ALU pipe, which takes one warp instruction every second cycle
     # per SM sub-partition (ncu: sm__pipe_alu_cycles_active exceeds the issue
@@ -611,7 +639,7 @@ def run_gpu(args):
             "per_step": {k: int(v) if not k.startswith("ms_") else round(v, 3) for k, v in per_step.items()},
             "stages": stage_rows, "stage_timing": "kernel times of one mapper alone (untimed pass)",
             "clocks": clk, "e2e": e2e,
-            "gpu_launches": int(acc["launches"]), "roofline": roofline, "int_pipe": int_pipe,
+            "gpu_launches": int(acc["launches"]), "roofline": roofline, "int_pipe": int_pipe, "gather_roofline": gather,
             "plain_per_batch": plain}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         arrays = ix.download()

@@ -227,6 +227,14 @@ int swm_mapper_debug_read_words(const swm_mapper *m, uint32_t *words, uint64_t c
 
 void swm_mapper_free(swm_mapper *m);
 
+/* Rate at which the device serves independent random 32-byte reads from a
+ * buffer of the given size (>= 1 MiB; larger than L2 for DRAM, smaller for
+ * L2), in sectors per second: the ceiling of the gather kernels (seed
+ * lookups, candidate gathers), which read scattered sectors rather than
+ * streams. No reference counterpart: measurement of this device, used for
+ * the roofline the benchmark reports. Allocates and frees the buffer. */
+int swm_probe_random_reads(int device, uint64_t bytes, double *sectors_per_s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,6 +99,7 @@ def lib():
         L.swm_mapper_debug_read_words.argtypes = [vp, vp, u64]
         L.swm_mapper_free.argtypes = [vp]
         L.swm_mapper_free.restype = None
+        L.swm_probe_random_reads.argtypes = [C.c_int, u64, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -106,6 +107,14 @@ def lib():
 def _check(rc: int, what: str) -> None:
     if rc != 0:
         raise SwmError(f"{what} failed ({rc}): {lib().swm_last_error().decode(errors='replace')}")
+
+
+def probe_random_reads(nbytes: int, device: int = 0) -> float:
+    """Random 32-byte reads per second the device serves from a buffer of
+    nbytes (swm_probe_random_reads)."""
+    v = C.c_double()
+    _check(lib().swm_probe_random_reads(device, nbytes, C.byref(v)), "swm_probe_random_reads")
+    return float(v.value)
 
 
 class Index:
