@@ -65,6 +65,19 @@ __device__ __forceinline__ uint32_t warp_take(uint32_t *q) {
     return __shfl_sync(0xffffffffu, b, 0);
 }
 
+// 1 when the item's selected buckets form one batch whatever the refill
+// order: no refills, or at most SWM_BATCH_POSITIONS - SWM_PER_FETCH + 1
+// positions. alignment_rmdup refills while npos + 32 <= 2048 and
+// 1 + 2 runs < 256 and flushes once either fails or the seed heap is empty;
+// both only grow, and before the last refill npos <= nel - 1 and, with at
+// most 64 seeds, runs <= nel / 32 + 64 - 1 < 127, so it refills until the
+// heap is empty. That batch holds every chunk, its element 0 is the first
+// seed's first position, and its candidates come out sorted and unique, so
+// the heap's order changes nothing. 0 otherwise (k_plan counts the batches).
+__device__ __forceinline__ uint32_t single_batch(uint32_t nref, uint32_t nel) {
+    return nel > 0 && (nref == 0 || nel + SWM_PER_FETCH - 1 <= SWM_BATCH_POSITIONS) ? 1u : 0u;
+}
+
 #define ARENA_CAP_DEFAULT (1u << 20)
 
 // The inputs of one block, in device memory so that the captured launch
@@ -500,7 +513,7 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const uint32_t *__rest
                 B.it_e[item] = (uint8_t)e;
                 B.it_nch[item] = nref;                  // refill chunks (beyond the first chunk of each seed)
                 B.it_nel[item] = nel;
-                B.it_nbat[item] = (nref == 0 && nel > 0) ? 1u : 0u; // k_plan sets it for items with refills
+                B.it_nbat[item] = single_batch(nref, nel); // k_plan sets it for the other items with refills
             }
         }
         __syncwarp();
@@ -944,7 +957,7 @@ __global__ void SEED12_BOUNDS k_seed12(const uint32_t *__restrict__ off, MapBufs
         B.it_e[item] = (uint8_t)e;
         B.it_nch[item] = nref;
         B.it_nel[item] = nel;
-        B.it_nbat[item] = (nref == 0 && nel > 0) ? 1u : 0u;
+        B.it_nbat[item] = single_batch(nref, nel); // k_plan sets it for the other items with refills
     }
 }
 
@@ -975,12 +988,12 @@ __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
 // independent): items with at most PLAN_LANE_SEEDS selected seeds from the
 // front for k_plan_lanes, the others from the back for k_plan.
 #define PLAN_LANE_SEEDS 32
-__global__ void __launch_bounds__(256) k_plan_list(MapBufs B) {
+__global__ void __launch_bounds__(256) k_plan_list(MapBufs B, uint64_t cap_chunks) {
     const uint32_t nitems = B.par->nitems;
     const uint32_t lane = lane_id();
     for (uint32_t base = blockIdx.x * 256 + (threadIdx.x & ~31u); base < nitems; base += gridDim.x * 256) {
         const uint32_t item = base + lane;
-        const bool has = item < nitems && B.it_nch[item] != 0;
+        const bool has = item < nitems && B.it_nch[item] != 0 && B.it_nbat[item] == 0;
         const bool few = has && B.it_nsel[item] <= PLAN_LANE_SEEDS;
         const uint32_t mf = __ballot_sync(0xffffffffu, few), mm = __ballot_sync(0xffffffffu, has && !few);
         uint32_t af = 0, am = 0;
@@ -990,6 +1003,43 @@ __global__ void __launch_bounds__(256) k_plan_list(MapBufs B) {
         am = __shfl_sync(0xffffffffu, am, 0);
         if (few) B.plan_list[af + __popc(mf & lanemask_lt())] = item;
         if (has && !few) B.plan_list[nitems - 1 - (am + __popc(mm & lanemask_lt()))] = item;
+        // items whose refills all fit in one batch (single_batch) need no heap:
+        // the warp writes their refill chunks seed by seed and the batch record
+        uint32_t one = __ballot_sync(0xffffffffu, item < nitems && B.it_nch[item] != 0 && B.it_nbat[item] == 1);
+        while (one) {
+            const uint32_t it = base + __ffs(one) - 1;
+            one &= one - 1;
+            const uint32_t ns = B.it_nsel[it], nref = B.it_nch[it], rb = B.it_choff[it];
+            if ((uint64_t)rb + nref > cap_chunks) {
+                if (lane == 0) {
+                    atomicOr(&B.tot[TOT_FLAGS], OV_CHUNKS);
+                    B.it_nbat[it] = 0;
+                }
+                continue;
+            }
+            const unsigned long long perm = B.it_perm[it];
+            const uint64_t sb = (uint64_t)it * SWM_MAX_SEL;
+            uint32_t q = 0;
+            for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
+                const uint32_t i = i0 + lane;
+                const uint2 sv = i < ns ? B.sel[sb + sel_slot(perm, i)] : make_uint2(0u, 0u);
+                const uint32_t r = sv.y > SWM_PER_FETCH ? (sv.y - 1) / SWM_PER_FETCH : 0u;
+                const uint32_t rinc = warp_scan_incl(r);
+                const uint32_t q0 = rb + q + rinc - r;
+                for (uint32_t j = 0; j < r; j++) {
+                    const uint32_t at = SWM_PER_FETCH * (j + 1), left = sv.y - at;
+                    B.ch_g[q0 + j] = sv.x + at;
+                    B.ch_meta[q0 + j] = (left > SWM_PER_FETCH ? SWM_PER_FETCH : left) | (i << 8);
+                }
+                q += __shfl_sync(0xffffffffu, rinc, 31);
+            }
+            if (lane == 0) {
+                const uint32_t sbase = rb + it;
+                B.bt_c0[sbase] = rb; // batch 0 also holds every initial chunk
+                B.bt_c1[sbase] = rb + nref;
+                B.bt_e0[sbase] = B.it_eloff[it];
+            }
+        }
     }
 }
 
@@ -2702,7 +2752,7 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     rc = swm_exclusive_scan(B.it_nel, B.it_eloff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_ELEMS, st);
     if (rc) return rc;
     m->launches += 6;
-    k_plan_list<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B);
+    k_plan_list<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks);
     k_plan_lanes<<<grid_cap(ci, PLAN_LANE_WARPS * 32, 6), PLAN_LANE_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
                                                                                          m->cap_elems);
     k_plan<<<grid_cap(ci, PLAN_WARPS * 32, 16), PLAN_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
