@@ -121,9 +121,10 @@ struct MapBufs {
     uint8_t *arena;   // long CIGAR texts
     uint16_t *unm;       // bit j of halfword w: read 16 w + j has no location (cap_items / 32 + 1)
     uint2 *vt_x;         // candidates alive after the head of verification: (candidate, ones) (cap_cands)
-    uint4 *vt_st;        // and their Myers state (VP, VN, VP and VN at the start of block 1) (cap_cands)
+    uint4 *vt_st;        // and their Myers state (VP, VN, checkpoint before base 16) (cap_cands)
+    uint4 *vt_cp;        // and the checkpoints before bases 32 and 48 (cap_cands)
     uint32_t *tb_list;   // candidates that need a traceback (cap_cands)
-    uint32_t *tb_cp;     // (VP, VN) at every 32-base block of each of them (cap_cands * 16)
+    uint32_t *tb_cp;     // (VP, VN) before every 16th read base of each of them (cap_cands * 32)
     uint32_t *plan_keys; // heap keys of items with more than PLAN_KEYS of them (cap_chunks)
     uint32_t *slow_list; // tracebacks whose route outgrew the fast path (cap_cands)
     // records
@@ -1755,12 +1756,16 @@ __device__ __forceinline__ void myers_blocks(const uint32_t *WL, const uint32_t 
         const uint32_t wl0 = WL[b], wl1 = WL[b + 1], wh0 = WH[b], wh1 = WH[b + 1];
         const uint32_t rlw = RW[2 * b], rhw = RW[2 * b + 1];
         const uint32_t steps = min(32u, L - 32 * b);
-        cp[2 * b] = vp; // (VP, VN) before block b, for the traceback
-        cp[2 * b + 1] = vn;
+        cp[4 * b] = vp; // (VP, VN) before bases 32 b and 32 b + 16, for the traceback
+        cp[4 * b + 1] = vn;
         uint32_t acc = 0;
         if (steps == 32) {
 #pragma unroll
             for (uint32_t t = 0; t < 32; t++) {
+                if (t == 16) {
+                    cp[4 * b + 2] = vp;
+                    cp[4 * b + 3] = vn;
+                }
                 const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
                 const uint32_t mL = (uint32_t)((int32_t)(rlw << (31 - t)) >> 31);
                 const uint32_t mH = (uint32_t)((int32_t)(rhw << (31 - t)) >> 31);
@@ -1776,6 +1781,10 @@ __device__ __forceinline__ void myers_blocks(const uint32_t *WL, const uint32_t 
             }
         } else {
             for (uint32_t t = 0; t < steps; t++) {
+                if (t == 16) {
+                    cp[4 * b + 2] = vp;
+                    cp[4 * b + 3] = vn;
+                }
                 const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
                 const uint32_t mL = 0u - ((rlw >> t) & 1u), mH = 0u - ((rhw >> t) & 1u);
                 const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
@@ -1911,7 +1920,7 @@ __device__ __forceinline__ int band_scan_min(int err, uint32_t vp, uint32_t vn, 
 }
 
 template <bool HEAD>
-__global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
+__global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *__restrict__ b2,
                                                 uint64_t b2_words, uint64_t ref_length, MapBufs B,
                                                 uint64_t cap_chunks, uint64_t cap_elems, uint64_t cap_cands,
                                                 uint64_t cap_arena) {
@@ -1932,19 +1941,23 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
         if (j >= n) continue;
         uint64_t c;
         uint32_t vp = 0, vn = 0, ones = 0;
-        uint32_t cp[16];
+        uint32_t cp[32];
         cp[0] = cp[1] = 0;
         if (HEAD) {
             c = j;
         } else {
             const uint2 x = B.vt_x[j];
-            const uint4 st = B.vt_st[j];
+            const uint4 st = B.vt_st[j], st2 = B.vt_cp[j];
             c = x.x;
             ones = x.y;
             vp = st.x;
             vn = st.y;
             cp[2] = st.z;
             cp[3] = st.w;
+            cp[4] = st2.x;
+            cp[5] = st2.y;
+            cp[6] = st2.z;
+            cp[7] = st2.w;
         }
         const uint32_t item = B.cc_item[c], p = B.cc_pos[c];
         const uint32_t L = lens[item >> 1], e = B.it_e[item];
@@ -1979,6 +1992,7 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
                 const uint32_t at = atomicAdd(&B.tot[TOT_VT], 1u);
                 B.vt_x[at] = make_uint2((uint32_t)c, ones);
                 B.vt_st[at] = make_uint4(vp, vn, cp[2], cp[3]);
+                B.vt_cp[at] = make_uint4(cp[4], cp[5], cp[6], cp[7]);
             }
             continue;
         }
@@ -2020,10 +2034,10 @@ __global__ void __launch_bounds__(128) k_verify(const uint32_t *__restrict__ b2,
         B.vr_flag[c] = VR_NEEDTB;
         const uint32_t at = atomicAdd(&B.tot[TOT_TB], 1u);
         B.tb_list[at] = (uint32_t)c;
-        uint4 *cpo = reinterpret_cast<uint4 *>(B.tb_cp + (uint64_t)at * 16);
+        uint4 *cpo = reinterpret_cast<uint4 *>(B.tb_cp + (uint64_t)at * 32);
 #pragma unroll
-        for (uint32_t k = 0; k < 4; k++)
-            if (4 * k < 2 * nblk) cpo[k] = make_uint4(cp[4 * k], cp[4 * k + 1], cp[4 * k + 2], cp[4 * k + 3]);
+        for (uint32_t k = 0; k < 8; k++)
+            if (k < nblk) cpo[k] = make_uint4(cp[4 * k], cp[4 * k + 1], cp[4 * k + 2], cp[4 * k + 3]);
     }
     warp_add_u64(&B.stat[ST_CELLS], cells);
     warp_add_u64(&B.stat[ST_PASSED], passed);
@@ -2051,15 +2065,16 @@ struct TbSmem {
     uint16_t route[TB_ROUTE][TB_THREADS]; // size | kind << 12 (M S I D)
 };
 
-// D0 and HP of read base i: Myers steps from the checkpoint of its block.
+// D0 and HP of read base i: Myers steps from the checkpoint before the
+// 16-base half block that holds it (at most 16 steps).
 __device__ __forceinline__ void myers_at(const uint32_t *WL, const uint32_t *WH, const uint32_t *rw,
                                          const uint32_t *cp, int i, uint32_t MASK, uint32_t &d0o, uint32_t &hpo) {
-    const uint32_t b = (uint32_t)i >> 5, tend = (uint32_t)i & 31;
-    uint32_t vp = cp[2 * b], vn = cp[2 * b + 1];
+    const uint32_t b = (uint32_t)i >> 5, h = ((uint32_t)i >> 4) & 1u, tend = (uint32_t)i & 31;
+    uint32_t vp = cp[4 * b + 2 * h], vn = cp[4 * b + 2 * h + 1]; // checkpoint before base 16 (2 b + h)
     const uint32_t wl0 = WL[b], wl1 = WL[b + 1], wh0 = WH[b], wh1 = WH[b + 1];
     const uint32_t rlw = rw[2 * b], rhw = rw[2 * b + 1];
     uint32_t d0 = 0, hp = 0;
-    for (uint32_t t = 0; t <= tend; t++) {
+    for (uint32_t t = 16 * h; t <= tend; t++) {
         const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
         const uint32_t mL = 0u - ((rlw >> t) & 1u), mH = 0u - ((rhw >> t) & 1u);
         const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
@@ -2120,8 +2135,9 @@ __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__rest
         uint32_t WL[SWM_WIN_WORDS], WH[SWM_WIN_WORDS];
         load_window(b2, b2_words, ws, L, e, WL, WH);
         const uint32_t *RW = B.it_w + (uint64_t)item * 32;
-        uint32_t rw[16], cp[16];
-        const uint4 *cps = reinterpret_cast<const uint4 *>(B.tb_cp + q * 16);
+        uint32_t rw[16], cp[32];
+        const uint4 *cps = reinterpret_cast<const uint4 *>(B.tb_cp + q * 32);
+        const uint32_t nblk = (L + 31) >> 5;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const uint4 r4 = reinterpret_cast<const uint4 *>(RW)[k];
@@ -2129,7 +2145,10 @@ __global__ void __launch_bounds__(TB_THREADS) k_traceback(const uint32_t *__rest
             rw[4 * k + 1] = r4.y;
             rw[4 * k + 2] = r4.z;
             rw[4 * k + 3] = r4.w;
-            const uint4 c4 = cps[k];
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < 8; k++) { // (VP, VN) before bases 32 k and 32 k + 16
+            const uint4 c4 = k < nblk ? cps[k] : make_uint4(0u, 0u, 0u, 0u);
             cp[4 * k] = c4.x;
             cp[4 * k + 1] = c4.y;
             cp[4 * k + 2] = c4.z;
@@ -2559,7 +2578,7 @@ static void free_bufs(MapBufs &B) {
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand, B.plan_list,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
-                  B.tb_cp, B.slow_list, B.vt_x, B.vt_st,
+                  B.tb_cp, B.slow_list, B.vt_x, B.vt_st, B.vt_cp,
                   B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
     for (void *p : ps) cudaFree(p);
     memset(&B, 0, sizeof(B));
@@ -2609,7 +2628,7 @@ static int alloc_work(swm_mapper *m) {
     cudaFree(B.bt_cnt); cudaFree(B.sort_scratch); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
     cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
     cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
-    cudaFree(B.tb_list); cudaFree(B.tb_cp); cudaFree(B.slow_list); cudaFree(B.vt_x); cudaFree(B.vt_st);
+    cudaFree(B.tb_list); cudaFree(B.tb_cp); cudaFree(B.slow_list); cudaFree(B.vt_x); cudaFree(B.vt_st); cudaFree(B.vt_cp);
     cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
     rc |= dmalloc(&B.ch_g, m->cap_chunks);
     rc |= dmalloc(&B.ch_meta, m->cap_chunks);
@@ -2631,10 +2650,11 @@ static int alloc_work(swm_mapper *m) {
     rc |= dmalloc(&B.vr_aoff, m->cap_cands);
     rc |= dmalloc(&B.arena, m->cap_arena);
     rc |= dmalloc(&B.tb_list, m->cap_cands);
-    rc |= dmalloc(&B.tb_cp, m->cap_cands * 16);
+    rc |= dmalloc(&B.tb_cp, m->cap_cands * 32);
     rc |= dmalloc(&B.slow_list, m->cap_cands);
     rc |= dmalloc(&B.vt_x, m->cap_cands);
     rc |= dmalloc(&B.vt_st, m->cap_cands);
+    rc |= dmalloc(&B.vt_cp, m->cap_cands);
     rc |= dmalloc(&B.out_w, m->cap_words);
     rc |= dmalloc(&B.out_c, m->cap_bytes);
     rc |= dmalloc(&B.rec_woff, m->cap_recs);
