@@ -69,6 +69,22 @@ def test_gpu_repeats_multibatch(cuda_lib):
         assert m.stats()["batches"] == ref.stats["batches"]
 
 
+def test_gpu_single_batch_items_near_the_limit(cuda_lib):
+    """Close repeat copies: many items with refills on both sides of the
+    single-batch limit (2017 selected positions), which the planner handles
+    without the seed heap below it and with the heap above it."""
+    g = genome(3_000_000, 7, "human", copies_per_family=1000, div_min=0.005, div_max=0.03, repeat_frac=0.6,
+               rep_len_max=3000)
+    reads, lens, _, _ = synth.reads(g, 600, 150, 150, 0.03, seed=21)
+    _, mix = oracle_index(g)
+    for e in (7, 12):
+        ref = po.map_reads(mix, reads, lens, e, nthreads=8)
+        out, m, _ = _gpu(cuda_lib, g, reads, lens, e)
+        _check(out, ref.records(), ref.unmapped)
+        assert m.stats()["batches"] == ref.stats["batches"]
+        assert m.stats()["candidates"] == ref.stats["candidates"]
+
+
 def test_gpu_uneven_per_read_e(cuda_lib):
     """Read lengths U[50, 250] with e = ceil(0.05 L) per read."""
     g = genome(2_000_000, 9, "repeats100m")
