@@ -6,15 +6,21 @@ of it repeat copies of 300 bp-6 kb families at 1% divergence), k=12 index built
 on the GPU, 1,000,000 reads of 150 bp at 3% error (70% substitutions, 15% 1-bp
 insertions, 15% 1-bp deletions) from both strands, error threshold e=7.
 
-A step maps every read of the workload (both strands, all blocks of 262,144
-reads) with the index and the reads resident in HBM; two mappers take the
-blocks in turn (swm_map_device_submit / swm_map_device_wait), so one block's
-gather-bound stages overlap the other's ALU-bound ones. `value` is mapped reads
-per second over the K timed steps (CUDA events spanning both mappers'
-streams). `e2e` runs the same reads through the public host API (H2D from
-page-locked memory, mapping, D2H of the packed records) with two mappers in
-ping-pong, timed on the host clock. The stage breakdown and the roofline come
-from one extra untimed pass with one mapper, so each kernel runs alone.
+A step maps every read of the workload (both strands, in blocks) with the
+index and the reads resident in HBM; several mappers take the blocks in turn
+(swm_map_device_submit / swm_map_device_wait), so one block's gather-bound
+stages overlap another's ALU-bound ones. Reads per block and the number of
+mappers come from the autotuner (swmapper_gb300/tune.py), run before the timed
+region. `value` is mapped reads per second over the K timed steps (CUDA events
+spanning the mappers' streams). `e2e` runs the same reads through the public
+host API (H2D from page-locked memory, mapping, D2H of the packed records)
+with four mappers in turn over a continuous stream of blocks, timed on the host
+clock. The stage breakdown and the roofline views come from one extra untimed
+pass with one mapper, so each kernel runs alone: `roofline` (the dominant
+kernel's algorithmic bytes against the measured HBM copy bandwidth),
+`gather_roofline` (the seed and candidate kernels' 32-byte sector requests
+against the random-read rate a probe kernel measures at their footprint) and
+`int_pipe` (the Myers steps the device counted x 21 ops against the ALU pipe).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
