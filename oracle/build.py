@@ -11,6 +11,12 @@ REF_DIR = os.path.join(HERE, "_ref")
 LIB_SWREF = os.path.join(REF_DIR, "libswref.so")
 
 
+def reference_tree() -> str:
+    """The reference's source tree: $REF_DIR, else a directory named
+    `reference` beside this repository's root (the same rule as build_ref.sh)."""
+    return os.environ.get("REF_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
 def _newer(target, deps):
     return os.path.exists(target) and all(os.path.getmtime(d) <= os.path.getmtime(target) for d in deps)
 
@@ -34,7 +40,7 @@ def build_ref() -> str | None:
     produced earlier; returns None when neither is available.
     """
     have_src = os.path.exists(os.path.join(REF_DIR, "src", "mapper_ref.c"))
-    have_tree = os.path.exists(os.path.join(os.environ.get("REF_DIR", "/root/reference"), "mapper_cpe.c"))
+    have_tree = os.path.exists(os.path.join(reference_tree(), "mapper_cpe.c"))
     if not (have_src or have_tree):
         return None
     if have_src and os.path.exists(LIB_SWREF) and not have_tree:

@@ -2,7 +2,8 @@
 # build_ref.sh -- compile the reference's own hot-path source for the pinning
 # tests and the reference leg of bench.py (TEST INFRASTRUCTURE).
 #
-# Where the reference tree is present (REF_DIR, default /root/reference) the
+# Where the reference tree is present (REF_DIR; by default a directory named
+# `reference` beside this repository's root) the
 # needed source is cut from it into oracle/_ref/src (git-ignored) and patched
 # at its undefined-behaviour sites only, with the defined meanings D1-D6
 # listed in oracle/swm_oracle.c. Where it is absent (a machine that only
@@ -16,7 +17,7 @@
 #                          gzwrite / gzprintf appending to a memory buffer
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF_DIR="${REF_DIR:-/root/reference}"
+REF_DIR="${REF_DIR:-$(cd "$HERE/../.." && pwd)/reference}"
 OUT="$HERE/_ref"
 SRC="$OUT/src"
 SHIM="$HERE/ref_shim"

@@ -74,6 +74,7 @@ def lib():
             build_oracle()
         L = C.CDLL(LIB_ORACLE)
         L.swo_index_build.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(_Index)]
+        L.swo_index_build_mt.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(_Index)]
         L.swo_index_free.argtypes = [C.POINTER(_Index)]
         L.swo_map_reads.argtypes = [C.POINTER(_MapIdx), C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
                                     C.c_uint32, C.c_uint32, C.POINTER(_Out), C.POINTER(_Stats)]
@@ -118,10 +119,15 @@ class HostIndex:
                 ".base_2bits": self.base_2bits.tobytes(), ".base_3bits": self.base_3bits.tobytes()}
 
 
-def build_index(seq: np.ndarray, k: int = 12) -> HostIndex:
+def build_index(seq: np.ndarray, k: int = 12, nthreads: int = 1) -> HostIndex:
+    """The oracle's index (serial_index.c:157-445); nthreads > 1 splits its
+    loops over host threads with identical output (swo_index_build_mt)."""
     seq = np.ascontiguousarray(seq, dtype=np.uint8)
     ix = _Index()
-    rc = lib().swo_index_build(seq.ctypes.data, seq.size, k, C.byref(ix))
+    if nthreads > 1:
+        rc = lib().swo_index_build_mt(seq.ctypes.data, seq.size, k, nthreads, C.byref(ix))
+    else:
+        rc = lib().swo_index_build(seq.ctypes.data, seq.size, k, C.byref(ix))
     if rc != 0:
         raise RuntimeError(f"swo_index_build failed ({rc})")
     try:

@@ -5,7 +5,7 @@
  * per-read mapping kernel (mapper_cpe.c:229-2590) step for step, in plain C.
  * The GPU implementation in swmapper_gb300/csrc must agree with this file bit
  * for bit. Parity of this file is pinned against the reference source itself,
- * compiled here by oracle/build_ref.sh (tests/test_oracle_pin.py).
+ * compiled here by oracle/build_ref.sh (tests/test_oracle_golden.py).
  *
  * Defined meanings for the reference's undefined behaviour (each one is also
  * applied to the reference build used for pinning, see build_ref.sh):
@@ -141,6 +141,139 @@ int swo_index_build(const uint8_t *seq, uint64_t n, uint32_t k, swo_index *ix) {
     /* cursor (== hash_offset) now holds END offsets, the way the reference
      * writes its .hash_offset file (serial_index.c:105-110). */
     free(seeds2);
+    return 0;
+}
+
+/* The same index with nthreads host threads, identical output (the serial
+ * build above is the restatement; this one only splits its loops). Phase 1:
+ * thread t encodes the 32-base words of its slice of the genome and counts
+ * the k-mers starting there in its own histogram (a sampled start i is
+ * counted when bases i .. i + k - 1 are all A/C/G/T, which is the serial
+ * loop's run == k test). Phase 2: start offsets, and each thread's first slot
+ * in every bucket = the bucket's start + the counts of the slices before it.
+ * Phase 3: each thread scatters its slice's positions in ascending order, so
+ * every bucket holds its positions in ascending order, as the serial scatter
+ * leaves them (serial_index.c:343-352). */
+typedef struct {
+    const uint8_t *seq;
+    uint64_t n, w0, w1;
+    uint32_t k, phase;
+    uint32_t *hist;
+    uint32_t *seeds2;
+    swo_index *ix;
+} ibuild_t;
+
+static void *ibuild_worker(void *arg) {
+    ibuild_t *a = (ibuild_t *)arg;
+    swo_index *ix = a->ix;
+    const uint32_t k = a->k;
+    const uint64_t n = a->n;
+    const uint32_t smask = (k >= 16) ? ~0u : ((1u << (2 * k)) - 1);
+    const uint64_t i0 = a->w0 * 32, i1 = a->w1 * 32 < n ? a->w1 * 32 : n;
+    if (a->phase == 1) {
+        for (uint64_t p = i0; p < i1; p++) {
+            const int c = base_code(a->seq[p]);
+            const uint64_t w = p / 32, b = p % 32;
+            if (c < 0) {
+                ix->base_3bits[w] |= 1u << b;
+                continue;
+            }
+            ix->base_2bits[2 * w] |= (uint32_t)(c & 1) << b;
+            ix->base_2bits[2 * w + 1] |= (uint32_t)(c >> 1) << b;
+            a->seeds2[p / 16] |= (uint32_t)c << (2 * (p % 16));
+        }
+        for (uint64_t i = i0; n >= k && i < i1 && i < n - k + 1; i += SEED_STEP) {
+            uint32_t sd = 0, ok = 1;
+            for (uint32_t j = 0; j < k && ok; j++) {
+                const int c = base_code(a->seq[i + j]);
+                if (c < 0) ok = 0;
+                else sd |= (uint32_t)c << (2 * j);
+            }
+            if (ok) a->hist[sd & smask]++;
+        }
+        return NULL;
+    }
+    const uint32_t nmask = (k >= 32) ? ~0u : ((1u << k) - 1);
+    const uint32_t res = SEED_STEP - 1, rmask = (1u << res) - 1;
+    const uint32_t *b2 = ix->base_2bits, *s2 = a->seeds2;
+    uint32_t *cursor = a->hist; /* this slice's next slot in every bucket */
+    for (uint64_t i = i0; n >= k && i < i1 && i < n - k + 1; i += SEED_STEP) {
+        uint32_t sd = fsr(s2[i / 16], s2[i / 16 + 1], (uint32_t)(i % 16) * 2) & smask;
+        uint32_t nf = fsr(ix->base_3bits[i / 32], ix->base_3bits[i / 32 + 1], (uint32_t)(i % 32)) & nmask;
+        if (nf) continue;
+        uint64_t sp = (i >= res) ? i - res : 0;
+        uint32_t fl = fsr(b2[(sp / 32) * 2], b2[(sp / 32 + 1) * 2], sp % 32) & rmask;
+        uint32_t fh = fsr(b2[(sp / 32) * 2 + 1], b2[(sp / 32 + 1) * 2 + 1], sp % 32) & rmask;
+        sp = i + k;
+        uint32_t bl = fsr(b2[(sp / 32) * 2], b2[(sp / 32 + 1) * 2], sp % 32) & rmask;
+        uint32_t bh = fsr(b2[(sp / 32) * 2 + 1], b2[(sp / 32 + 1) * 2 + 1], sp % 32) & rmask;
+        fl |= bl << res;
+        fh |= bh << res;
+        const uint32_t slot = cursor[sd]++;
+        ix->positions[slot] = (uint32_t)i;
+        ix->pos_lseeds[slot] = (uint16_t)(fl | (fh << (res * 2)));
+    }
+    return NULL;
+}
+
+int swo_index_build_mt(const uint8_t *seq, uint64_t n, uint32_t k, uint32_t nthreads, swo_index *ix) {
+    if (nthreads <= 1 || n < (1u << 20)) return swo_index_build(seq, n, k, ix);
+    memset(ix, 0, sizeof(*ix));
+    if (k < 1 || k > 14 || n >= 0xffffffffull) return -1;
+    if (nthreads > 64) nthreads = 64;
+    const uint64_t nb = 1ull << (2 * k);
+    const uint64_t W = (n + 31) / 32;
+    ix->k = k;
+    ix->n = n;
+    ix->hash_count = calloc(nb, 4);
+    ix->hash_offset = calloc(nb + 1, 4);
+    ix->base_2bits = calloc(2 * W + SWO_PAD_WORDS, 4);
+    ix->base_3bits = calloc(W + SWO_PAD_WORDS, 4);
+    uint32_t *seeds2 = calloc((n + 15) / 16 + SWO_PAD_WORDS, 4);
+    uint32_t *hist = calloc((size_t)nthreads * nb, 4);
+    ibuild_t args[64];
+    pthread_t th[64];
+    if (!ix->hash_count || !ix->hash_offset || !ix->base_2bits || !ix->base_3bits || !seeds2 || !hist) {
+        free(seeds2);
+        free(hist);
+        swo_index_free(ix);
+        return -3;
+    }
+    const uint64_t per = (W + nthreads - 1) / nthreads;
+    for (uint32_t t = 0; t < nthreads; t++) {
+        const uint64_t w0 = t * per < W ? t * per : W, w1 = (t + 1) * per < W ? (t + 1) * per : W;
+        args[t] = (ibuild_t){seq, n, w0, w1, k, 1, hist + (size_t)t * nb, seeds2, ix};
+    }
+    for (uint32_t t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, ibuild_worker, &args[t]);
+    for (uint32_t t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    /* counts, start offsets, and each slice's first slot per bucket */
+    uint64_t S = 0;
+    for (uint64_t b = 0; b < nb; b++) {
+        uint32_t c = 0;
+        for (uint32_t t = 0; t < nthreads; t++) {
+            const uint32_t h = hist[(size_t)t * nb + b];
+            hist[(size_t)t * nb + b] = (uint32_t)(S + c);
+            c += h;
+        }
+        ix->hash_count[b] = c;
+        S += c;
+        ix->hash_offset[b] = (uint32_t)S; /* END offsets, as the serial build leaves them */
+    }
+    ix->hash_offset[nb] = (uint32_t)S;
+    ix->n_seeds = S;
+    ix->positions = malloc((S + 8) * 4);
+    ix->pos_lseeds = malloc((S + 8) * 2);
+    if (!ix->positions || !ix->pos_lseeds) {
+        free(seeds2);
+        free(hist);
+        swo_index_free(ix);
+        return -3;
+    }
+    for (uint32_t t = 0; t < nthreads; t++) args[t].phase = 3;
+    for (uint32_t t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, ibuild_worker, &args[t]);
+    for (uint32_t t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(seeds2);
+    free(hist);
     return 0;
 }
 

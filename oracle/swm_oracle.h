@@ -50,6 +50,8 @@ typedef struct {
  * (serial_index.c:157-445 with defined shifts and a guarded final flush).
  * Returns 0 on success. */
 int swo_index_build(const uint8_t *seq, uint64_t n, uint32_t k, swo_index *out);
+/* The same index built with nthreads host threads (identical output). */
+int swo_index_build_mt(const uint8_t *seq, uint64_t n, uint32_t k, uint32_t nthreads, swo_index *out);
 void swo_index_free(swo_index *ix);
 
 /* Read-only view used by the mapper (mapper_mpe.c:198-314). */

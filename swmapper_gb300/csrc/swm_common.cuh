@@ -42,8 +42,10 @@ struct swm_index {
 
 // Exclusive scan of n u32 values (n read from *d_n when d_n is not NULL,
 // else n_host; clamped to n_cap); out gets n + 1 entries, out[n] = total,
-// and *d_total = total when d_total is not NULL. tmp needs
-// swm_scan_tmp_words(n_cap) words. Implemented in swm_index.cu.
+// and *d_total = total when d_total is not NULL. A total of 2^32 - 1 or more
+// is written as SWM_SCAN_SATURATED (the offsets are then meaningless). tmp
+// needs swm_scan_tmp_words(n_cap) words. Implemented in swm_index.cu.
+#define SWM_SCAN_SATURATED 0xffffffffu
 uint64_t swm_scan_tmp_words(uint64_t n_cap);
 int swm_exclusive_scan(const uint32_t *d_in, uint32_t *d_out, const uint32_t *d_n, uint64_t n_host, uint64_t n_cap,
                        uint32_t *d_tmp, uint32_t *d_total, cudaStream_t st);

@@ -14,12 +14,18 @@
 //               serial scatter produces
 //   kb_split    the sorted keys into the resident index: positions (u32) and
 //               flank codes (u16), the layout of .positions / .pos_lseeds
+#include <errno.h>
+#include <fcntl.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <mutex>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "swm_common.cuh"
@@ -80,11 +86,28 @@ __device__ __forceinline__ uint64_t scan_n(const uint32_t *d_n, uint64_t n_host,
     return n < n_cap ? n : n_cap;
 }
 
+// Sum of one 64-bit value per thread over the block (every thread gets it).
+__device__ __forceinline__ uint64_t block_sum_u64(uint64_t v) {
+    __shared__ unsigned long long wsum64[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    if (lane == 0) wsum64[wid] = v;
+    __syncthreads();
+    uint64_t t = 0;
+    for (int w = 0; w < nw; w++) t += wsum64[w];
+    __syncthreads();
+    return t;
+}
+
+// Totals are 32-bit: a sum that does not fit saturates to SWM_SCAN_SATURATED
+// (each tile's partial, then the total), so callers see an overflow instead
+// of a wrapped value.
 __global__ void k_scan_reduce(const uint32_t *__restrict__ in, const uint32_t *d_n, uint64_t n_host, uint64_t n_cap,
                               uint32_t *__restrict__ part) {
     const uint64_t n = scan_n(d_n, n_host, n_cap);
     const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
-    uint32_t s = 0;
+    uint64_t s = 0;
     if (base < n) {
 #pragma unroll
         for (int v = 0; v < SCAN_V; v++) {
@@ -92,9 +115,9 @@ __global__ void k_scan_reduce(const uint32_t *__restrict__ in, const uint32_t *d
             if (i < n) s += in[i];
         }
     }
-    uint32_t tot;
-    block_excl_scan(s, &tot);
-    if (threadIdx.x == 0) part[blockIdx.x] = (base < n) ? tot : 0u;
+    const uint64_t tot = block_sum_u64(s);
+    if (threadIdx.x == 0)
+        part[blockIdx.x] = (base < n) ? (tot < SWM_SCAN_SATURATED ? (uint32_t)tot : SWM_SCAN_SATURATED) : 0u;
 }
 
 __global__ void k_scan_top(uint32_t *part, const uint32_t *d_n, uint64_t n_host, uint64_t n_cap, uint32_t *out,
@@ -104,7 +127,12 @@ __global__ void k_scan_top(uint32_t *part, const uint32_t *d_n, uint64_t n_host,
     const uint64_t per = (nb + blockDim.x - 1) / blockDim.x;
     const uint64_t b0 = threadIdx.x * per;
     uint32_t s = 0;
-    for (uint64_t i = b0; i < b0 + per && i < nb; i++) s += part[i];
+    uint64_t s64 = 0;
+    for (uint64_t i = b0; i < b0 + per && i < nb; i++) {
+        s += part[i];
+        s64 += part[i];
+    }
+    const uint64_t tot64 = block_sum_u64(s64);
     uint32_t tot;
     uint32_t ex = block_excl_scan(s, &tot);
     for (uint64_t i = b0; i < b0 + per && i < nb; i++) {
@@ -113,6 +141,7 @@ __global__ void k_scan_top(uint32_t *part, const uint32_t *d_n, uint64_t n_host,
         ex += v;
     }
     if (threadIdx.x == 0) {
+        if (tot64 >= SWM_SCAN_SATURATED) tot = SWM_SCAN_SATURATED;
         out[n] = tot;
         if (d_total) *d_total = tot;
     }
@@ -640,81 +669,208 @@ extern "C" int swm_index_build_fasta(const char *fasta_path, const char *prefix,
     return rc;
 }
 
-extern "C" int swm_index_open(const char *prefix, uint32_t k, int device, swm_index **out) {
-    if (!prefix || !out || k < 1 || k > 14) return SWM_ERR_ARG;
-    SWM_CUDA(cudaSetDevice(device));
-    const uint64_t nb = 1ull << (2 * k);
-    void *cnt = nullptr, *pos = nullptr, *ls = nullptr, *b2 = nullptr, *b3 = nullptr, *info = nullptr;
-    size_t ncnt = 0, npos = 0, nls = 0, nb2 = 0, nb3 = 0, ninfo = 0;
-    int rc = SWM_OK;
-    if (swmf_read(prefix, ".hash_count", &cnt, &ncnt) || swmf_read(prefix, ".positions", &pos, &npos) ||
-        swmf_read(prefix, ".pos_lseeds", &ls, &nls) || swmf_read(prefix, ".base_2bits", &b2, &nb2) ||
-        swmf_read(prefix, ".base_3bits", &b3, &nb3)) {
-        swm_set_error("cannot read index files under %s", prefix);
-        rc = SWM_ERR_IO;
+// ------------------------------------------------------------ index load
+//
+// load_ref_info (mapper_mpe.c:198-314) freads each file whole into malloc'ed
+// memory before the mapper uses it. Here each file streams into device
+// memory: one host thread per file reads 32 MiB chunks with pread into two
+// page-locked buffers in turn while the previous chunk's copy runs on the
+// thread's own stream, so disk (or page cache) reads overlap the H2D copies
+// and the five files load concurrently.
+
+#define LOAD_CHUNK (32ull << 20)
+
+static std::string index_path(const char *prefix, const char *ext) { return std::string(prefix) + ext; }
+
+// Size of a regular file, or -1 when it cannot be stat'ed.
+static int64_t file_bytes(const std::string &path) {
+    struct stat sb;
+    if (stat(path.c_str(), &sb) != 0 || !S_ISREG(sb.st_mode)) return -1;
+    return (int64_t)sb.st_size;
+}
+
+struct FileLoad {
+    std::string path;
+    uint64_t bytes;
+    void *d_dst;
+    bool sum_words; // add up the file's u32 words (the bucket counts)
+    uint64_t sum;
+    int rc;
+    char err[256];
+};
+
+static void load_file(FileLoad *L, int device) {
+    L->rc = SWM_OK;
+    L->sum = 0;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        snprintf(L->err, sizeof L->err, "cudaSetDevice(%d) failed", device);
+        L->rc = SWM_ERR_CUDA;
+        return;
     }
-    uint64_t S = npos / 4;
+    const int fd = open(L->path.c_str(), O_RDONLY);
+    if (fd < 0) {
+        snprintf(L->err, sizeof L->err, "cannot open %s", L->path.c_str());
+        L->rc = SWM_ERR_IO;
+        return;
+    }
+#ifdef POSIX_FADV_SEQUENTIAL
+    posix_fadvise(fd, 0, 0, POSIX_FADV_SEQUENTIAL);
+#endif
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    uint8_t *buf[2] = {nullptr, nullptr};
+    const uint64_t chunk = L->bytes < LOAD_CHUNK ? (L->bytes ? L->bytes : 1) : LOAD_CHUNK;
+    bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+    for (int i = 0; i < 2 && ok; i++)
+        ok = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) == cudaSuccess &&
+             cudaHostAlloc((void **)&buf[i], chunk, 0) == cudaSuccess;
+    if (!ok) {
+        snprintf(L->err, sizeof L->err, "staging buffers for %s", L->path.c_str());
+        L->rc = SWM_ERR_OOM;
+    }
+    bool used[2] = {false, false};
+    for (uint64_t off = 0, i = 0; L->rc == SWM_OK && off < L->bytes; i ^= 1) {
+        const uint64_t len = L->bytes - off < chunk ? L->bytes - off : chunk;
+        if (used[i] && cudaEventSynchronize(ev[i]) != cudaSuccess) { // buffer i's last copy is done
+            snprintf(L->err, sizeof L->err, "H2D of %s failed", L->path.c_str());
+            L->rc = SWM_ERR_CUDA;
+            break;
+        }
+        uint64_t got = 0;
+        while (got < len) {
+            const ssize_t r = pread(fd, buf[i] + got, len - got, (off_t)(off + got));
+            if (r < 0 && errno == EINTR) continue;
+            if (r <= 0) break;
+            got += (uint64_t)r;
+        }
+        if (got != len) {
+            snprintf(L->err, sizeof L->err, "%s is shorter than its %llu bytes", L->path.c_str(),
+                     (unsigned long long)L->bytes);
+            L->rc = SWM_ERR_IO;
+            break;
+        }
+        if (L->sum_words) {
+            const uint32_t *w = (const uint32_t *)buf[i];
+            for (uint64_t j = 0; j < len / 4; j++) L->sum += w[j];
+        }
+        if (cudaMemcpyAsync((uint8_t *)L->d_dst + off, buf[i], len, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaEventRecord(ev[i], st) != cudaSuccess) {
+            snprintf(L->err, sizeof L->err, "H2D of %s failed", L->path.c_str());
+            L->rc = SWM_ERR_CUDA;
+            break;
+        }
+        used[i] = true;
+        off += len;
+    }
+    if (st && cudaStreamSynchronize(st) != cudaSuccess && L->rc == SWM_OK) {
+        snprintf(L->err, sizeof L->err, "H2D of %s failed", L->path.c_str());
+        L->rc = SWM_ERR_CUDA;
+    }
+    for (int i = 0; i < 2; i++) {
+        if (buf[i]) cudaFreeHost(buf[i]);
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    }
+    if (st) cudaStreamDestroy(st);
+    close(fd);
+}
+
+extern "C" int swm_index_open(const char *prefix, uint32_t k, int device, swm_index **out) {
+    if (!prefix || !out || k < 1 || k > 14) {
+        swm_set_error("swm_index_open: null argument or k outside [1, 14]");
+        return SWM_ERR_ARG;
+    }
+    // every file present and the sizes consistent before any device work
+    static const char *exts[5] = {".hash_count", ".positions", ".pos_lseeds", ".base_2bits", ".base_3bits"};
+    int64_t sz[5];
+    for (int f = 0; f < 5; f++) {
+        sz[f] = file_bytes(index_path(prefix, exts[f]));
+        if (sz[f] < 0) {
+            swm_set_error("index file %s is missing", index_path(prefix, exts[f]).c_str());
+            return SWM_ERR_IO;
+        }
+    }
+    const uint64_t nb = 1ull << (2 * k);
+    const uint64_t S = (uint64_t)sz[1] / 4;
+    if ((uint64_t)sz[0] != nb * 4 || sz[1] % 4 || (uint64_t)sz[2] != S * 2 || sz[3] % 8 || sz[3] != 2 * sz[4] ||
+        S >= 0xffffffffull) {
+        swm_set_error("index files under %s have inconsistent sizes for k=%u (hash_count %lld, positions %lld, "
+                      "pos_lseeds %lld, base_2bits %lld, base_3bits %lld bytes)",
+                      prefix, k, (long long)sz[0], (long long)sz[1], (long long)sz[2], (long long)sz[3],
+                      (long long)sz[4]);
+        return SWM_ERR_IO;
+    }
+    SWM_CUDA(cudaSetDevice(device));
+    swm_index *ix = (swm_index *)calloc(1, sizeof(swm_index));
+    if (!ix) return SWM_ERR_OOM;
+    ix->device = device;
+    ix->k = k;
+    ix->n_seeds = S;
+    ix->n_words2 = (uint64_t)sz[3] / 4;
+    ix->n_words3 = (uint64_t)sz[4] / 4;
+    ix->ref_length = (uint64_t)sz[3] * 16; // mapper_mpe.c:288
+    ix->n = 32 * ix->n_words3;
+    void *info = nullptr;
+    size_t ninfo = 0;
+    if (swmf_read(prefix, ".ref_info", &info, &ninfo) == 0) {
+        const uint64_t t = swmf_ref_info_total((const char *)info, ninfo);
+        if (t) ix->n = t;
+        free(info);
+    }
+    uint32_t *d_tmp = nullptr;
+    int rc = SWM_OK;
+    if (dalloc(&ix->d_count, nb) || dalloc(&ix->d_off, nb + 1) || dalloc(&ix->d_pos, S + 8) ||
+        dalloc(&ix->d_ls, S + 8) || dalloc(&ix->d_b2, ix->n_words2 + SWM_PAD_WORDS) ||
+        dalloc(&ix->d_b3, ix->n_words3 + SWM_PAD_WORDS) || dalloc(&d_tmp, swm_scan_tmp_words(nb))) {
+        rc = SWM_ERR_OOM;
+    }
     if (rc == SWM_OK) {
-        uint64_t total = 0;
-        const uint32_t *c = (const uint32_t *)cnt;
-        if (ncnt == nb * 4)
-            for (uint64_t i = 0; i < nb; i++) total += c[i];
-        if (ncnt != nb * 4 || npos % 4 || nls != S * 2 || nb2 % 8 || total != S) {
-            swm_set_error("index files under %s are inconsistent (k=%u)", prefix, k);
+        FileLoad loads[5];
+        void *dst[5] = {ix->d_count, ix->d_pos, ix->d_ls, ix->d_b2, ix->d_b3};
+        for (int f = 0; f < 5; f++) {
+            loads[f].path = index_path(prefix, exts[f]);
+            loads[f].bytes = (uint64_t)sz[f];
+            loads[f].d_dst = dst[f];
+            loads[f].sum_words = f == 0;
+            loads[f].err[0] = 0;
+        }
+        std::vector<std::thread> th;
+        for (int f = 1; f < 5; f++) th.emplace_back(load_file, &loads[f], device);
+        load_file(&loads[0], device);
+        for (auto &t : th) t.join();
+        for (int f = 0; f < 5 && rc == SWM_OK; f++)
+            if (loads[f].rc != SWM_OK) {
+                swm_set_error("%s", loads[f].err);
+                rc = loads[f].rc;
+            }
+        if (rc == SWM_OK && loads[0].sum != S) {
+            swm_set_error("index files under %s are inconsistent: hash_count adds up to %llu, positions hold %llu",
+                          prefix, (unsigned long long)loads[0].sum, (unsigned long long)S);
             rc = SWM_ERR_IO;
         }
     }
-    swm_index *ix = nullptr;
     if (rc == SWM_OK) {
-        ix = (swm_index *)calloc(1, sizeof(swm_index));
-        if (!ix) rc = SWM_ERR_OOM;
-    }
-    if (rc == SWM_OK) {
-        ix->device = device;
-        ix->k = k;
-        ix->n_seeds = S;
-        ix->n_words2 = nb2 / 4;
-        ix->n_words3 = nb3 / 4;
-        ix->ref_length = (uint64_t)nb2 * 16; // mapper_mpe.c:288
-        ix->n = 32 * ix->n_words3;
-        if (swmf_read(prefix, ".ref_info", &info, &ninfo) == 0) {
-            uint64_t t = swmf_ref_info_total((const char *)info, ninfo);
-            if (t) ix->n = t;
-        }
-        uint32_t *d_tmp = nullptr;
-        if (dalloc(&ix->d_count, nb) || dalloc(&ix->d_off, nb + 1) || dalloc(&ix->d_pos, S + 8) ||
-            dalloc(&ix->d_ls, S + 8) || dalloc(&ix->d_b2, ix->n_words2 + SWM_PAD_WORDS) ||
-            dalloc(&ix->d_b3, ix->n_words3 + SWM_PAD_WORDS) || dalloc(&d_tmp, swm_scan_tmp_words(nb))) {
-            rc = SWM_ERR_OOM;
-        } else if (cudaMemcpy(ix->d_count, cnt, nb * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-                   (S && cudaMemcpy(ix->d_pos, pos, S * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
-                   (S && cudaMemcpy(ix->d_ls, ls, S * 2, cudaMemcpyHostToDevice) != cudaSuccess) ||
-                   (nb2 && cudaMemcpy(ix->d_b2, b2, nb2, cudaMemcpyHostToDevice) != cudaSuccess) ||
-                   (nb3 && cudaMemcpy(ix->d_b3, b3, nb3, cudaMemcpyHostToDevice) != cudaSuccess) ||
-                   cudaMemset(ix->d_pos + S, 0, 32) != cudaSuccess || cudaMemset(ix->d_ls + S, 0, 16) != cudaSuccess ||
-                   cudaMemset(ix->d_b2 + ix->n_words2, 0, SWM_PAD_WORDS * 4) != cudaSuccess ||
-                   cudaMemset(ix->d_b3 + ix->n_words3, 0, SWM_PAD_WORDS * 4) != cudaSuccess) {
-            swm_set_error("H2D of index under %s failed", prefix);
+        if (cudaMemset(ix->d_pos + S, 0, 32) != cudaSuccess || cudaMemset(ix->d_ls + S, 0, 16) != cudaSuccess ||
+            cudaMemset(ix->d_b2 + ix->n_words2, 0, SWM_PAD_WORDS * 4) != cudaSuccess ||
+            cudaMemset(ix->d_b3 + ix->n_words3, 0, SWM_PAD_WORDS * 4) != cudaSuccess) {
+            swm_set_error("clearing the index padding under %s failed", prefix);
             rc = SWM_ERR_CUDA;
-        } else {
-            // hash_offset rebuilt from the counts (mapper_mpe.c:250-255)
-            rc = swm_exclusive_scan(ix->d_count, ix->d_off, nullptr, nb, nb, d_tmp, nullptr, 0);
-            if (rc == SWM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = SWM_ERR_CUDA;
-        }
-        cudaFree(d_tmp);
-        if (rc != SWM_OK) {
-            index_release(ix);
-            ix = nullptr;
         }
     }
-    free(cnt);
-    free(pos);
-    free(ls);
-    free(b2);
-    free(b3);
-    free(info);
-    if (rc == SWM_OK) *out = ix;
-    return rc;
+    if (rc == SWM_OK) {
+        // hash_offset rebuilt from the counts (mapper_mpe.c:250-255)
+        rc = swm_exclusive_scan(ix->d_count, ix->d_off, nullptr, nb, nb, d_tmp, nullptr, 0);
+        if (rc == SWM_OK && cudaDeviceSynchronize() != cudaSuccess) {
+            swm_set_error("rebuilding hash_offset under %s failed", prefix);
+            rc = SWM_ERR_CUDA;
+        }
+    }
+    cudaFree(d_tmp);
+    if (rc != SWM_OK) {
+        index_release(ix);
+        return rc;
+    }
+    *out = ix;
+    return SWM_OK;
 }
 
 extern "C" void swm_index_free(swm_index *ix) {

@@ -470,7 +470,8 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const uint32_t *__rest
             const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
             const uint32_t ns = nsl * SWM_SEED_STEP;
             const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
-            uint32_t nref = 0, nel = 0;
+            uint32_t nref = 0;
+            uint64_t nel = 0; // saturated below: sums past 32 bits are reported, not wrapped
             for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
                 const uint32_t i = i0 + lane;
                 if (i < ns) {
@@ -497,6 +498,7 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const uint32_t *__rest
                 nref += __shfl_xor_sync(0xffffffffu, nref, d);
                 nel += __shfl_xor_sync(0xffffffffu, nel, d);
             }
+            if (nel > SWM_SCAN_SATURATED) nel = SWM_SCAN_SATURATED;
             // read words: [0..15] Myers planes from the 2-bit words, [16..31] Hamming planes
             uint32_t ow;
             if (lane < 16) {
@@ -513,8 +515,8 @@ __global__ void __launch_bounds__(SEED_WARPS * 32) k_seed(const uint32_t *__rest
                 B.it_perm[item] = perm;
                 B.it_e[item] = (uint8_t)e;
                 B.it_nch[item] = nref;                  // refill chunks (beyond the first chunk of each seed)
-                B.it_nel[item] = nel;
-                B.it_nbat[item] = single_batch(nref, nel); // k_plan sets it for the other items with refills
+                B.it_nel[item] = (uint32_t)nel;
+                B.it_nbat[item] = single_batch(nref, (uint32_t)nel); // k_plan sets it for the other items with refills
             }
         }
         __syncwarp();
@@ -945,7 +947,8 @@ __global__ void SEED12_BOUNDS k_seed12(const uint32_t *__restrict__ off, MapBufs
         // 2194-2196): ranks 0 .. nsl - 1 of the sorted order
         const uint32_t nsl = (e + 1 < nl) ? e + 1 : nl;
         const uint32_t ns = nsl * SWM_SEED_STEP;
-        uint32_t nref = 0, nel = 0;
+        uint32_t nref = 0;
+        uint64_t nel = 0; // saturated below: sums past 32 bits are reported, not wrapped
         unsigned long long perm = 0;
 #pragma unroll
         for (int a = 0; a < NL; a++) {
@@ -953,12 +956,13 @@ __global__ void SEED12_BOUNDS k_seed12(const uint32_t *__restrict__ off, MapBufs
             nel += (uint32_t)a < nsl ? CNT[a] : 0u;
             perm |= (unsigned long long)IDX[a] << (4 * a);
         }
+        if (nel > SWM_SCAN_SATURATED) nel = SWM_SCAN_SATURATED;
         B.it_perm[item] = perm;
         B.it_nsel[item] = (uint8_t)ns;
         B.it_e[item] = (uint8_t)e;
         B.it_nch[item] = nref;
-        B.it_nel[item] = nel;
-        B.it_nbat[item] = single_batch(nref, nel); // k_plan sets it for the other items with refills
+        B.it_nel[item] = (uint32_t)nel;
+        B.it_nbat[item] = single_batch(nref, (uint32_t)nel); // k_plan sets it for the other items with refills
     }
 }
 
@@ -2547,6 +2551,12 @@ __global__ void k_batches_stat(MapBufs B) {
 // host side
 // ======================================================================
 
+// Work-buffer capacities stay below SWM_SCAN_SATURATED, so a block whose
+// 32-bit totals saturated always exceeds them and its later stages skip.
+#define CAP_MAX ((uint64_t)SWM_SCAN_SATURATED - 1)
+
+static uint64_t cap_clamp(uint64_t c) { return c < CAP_MAX ? c : CAP_MAX; }
+
 static int g_sms = 0;
 
 static unsigned grid_cap(uint64_t work, unsigned threads, int per_sm) {
@@ -2673,12 +2683,12 @@ extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper *
     m->device = ix->device;
     m->max_reads = max_reads;
     m->cap_items = 2 * max_reads;
-    m->cap_chunks = m->cap_items * 16 + 1024;
-    m->cap_elems = m->cap_items * 128 + 4096;
-    m->cap_cands = m->cap_items * 8 + 4096;
-    m->cap_recs = m->cap_items + 1024;
-    m->cap_words = m->cap_items * 8 + 4096;
-    m->cap_bytes = m->cap_items * 32 + 4096;
+    m->cap_chunks = cap_clamp(m->cap_items * 16 + 1024);
+    m->cap_elems = cap_clamp(m->cap_items * 128 + 4096);
+    m->cap_cands = cap_clamp(m->cap_items * 8 + 4096);
+    m->cap_recs = cap_clamp(m->cap_items + 1024);
+    m->cap_words = cap_clamp(m->cap_items * 8 + 4096);
+    m->cap_bytes = cap_clamp(m->cap_items * 32 + 4096);
     m->cap_arena = ARENA_CAP_DEFAULT;
     m->stride_cap = 0;
     int rc = SWM_OK;
@@ -2879,7 +2889,7 @@ static void grow(uint64_t *cap, uint64_t need) {
     if (need <= *cap) return;
     uint64_t n = *cap;
     while (n < need) n *= 2;
-    *cap = n + n / 4;
+    *cap = cap_clamp(n + n / 4);
 }
 
 // Queue the copy of the block's totals to pinned memory (after enqueue).
@@ -2901,6 +2911,15 @@ static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *a
                       SWM_MAX_READ_LEN, SWM_MAX_ERRORS);
         return SWM_ERR_ARG;
     }
+    static const int kSums[] = {TOT_CHUNKS, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES};
+    static const char *kSumNames[] = {"refill chunks", "fetched positions", "candidates", "records", "record words",
+                                      "CIGAR bytes"};
+    for (int i = 0; i < 6; i++)
+        if (m->tot[kSums[i]] == SWM_SCAN_SATURATED) {
+            swm_set_error("the block's %s reach 2^32 - 1, past the 32-bit offsets of the work buffers: map it in "
+                          "smaller blocks (%u reads here)", kSumNames[i], nreads);
+            return SWM_ERR_OVERFLOW;
+        }
     bool need = false;
     // totals from the item scans are exact even when a later buffer overflowed
     if (m->tot[TOT_CHUNKS] > m->cap_chunks) {

@@ -123,3 +123,18 @@ def test_block_merge_equals_sort_unique():
         for b in np.unique(tr["batch"]):
             p = tr["pos"][tr["batch"] == b]
             assert np.all(np.diff(p.astype(np.int64)) > 0)
+
+
+@pytest.mark.parametrize("n,kind,k", [(3_000_013, "human", 12), (2_000_032, "repeats100m", 12),
+                                      (1_500_001, "uniform", 10)])
+def test_threaded_oracle_index_equals_serial(n, kind, k):
+    """The threaded oracle build (used for genomes of billions of bases) gives
+    the serial restatement's arrays exactly, with N runs, lowercase bases and
+    slices that split N runs and k-mers."""
+    over = dict(nrun_min=2000, nrun_max=50_000) if kind == "human" else {}
+    g = _genome(n, 91, kind, over, nruns=[(1_000_000 - 5, 1_000_000 + 7)], lower=True)
+    a = po.build_index(g, k)
+    for threads in (3, 8):
+        b = po.build_index(g, k, nthreads=threads)
+        for key in ("hash_count", "hash_offset_end", "positions", "pos_lseeds", "base_2bits", "base_3bits"):
+            assert np.array_equal(getattr(a, key), getattr(b, key)), (threads, key)
