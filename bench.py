@@ -75,7 +75,7 @@ WORKLOADS["serving"] = dict(
              "[1, 4096] reads, 50-250 bp at 3% error, e=ceil(0.05 L); offered load 25/50/90% of the measured peak",
     genome_bp=3_100_000_000, genome_kind="human", genome_seed=31, reads=1_000_000, len_min=50, len_max=250,
     error_rate=0.03, e=None, e_frac=0.05, k=12, read_seed=17, block=65536, requests=3000)
-WORKLOAD = dict(WORKLOADS["batched"])
+WORKLOAD = dict(WORKLOADS["human"])
 METRIC = "mapped reads/s"
 L2_FLUSH_BYTES = 512 << 20   # > the 129 MB L2
 UNIT = "reads/s"
@@ -369,9 +369,16 @@ def run_gpu(args):
         reads, lens = np.ascontiguousarray(reads[order]), np.ascontiguousarray(lens[order])
         eper = None if eper is None else np.ascontiguousarray(eper[order])
         bucketed = True
+    # index build on bases already in device memory (the copy of the genome
+    # is not part of the build), host clock around the synchronous call
+    d_g = C.c_void_p()
+    assert rt.cudaMalloc(C.byref(d_g), g.nbytes) == 0
+    rt.cudaMemcpy(d_g, g.ctypes.data, g.nbytes, 1)
+    rt.cudaDeviceSynchronize()
     t0 = time.perf_counter()
-    ix = swm.Index.build(g, k=w["k"], device=local)
+    ix = swm.Index.build_device(d_g.value, g.size, k=w["k"], device=local)
     index_build_s = time.perf_counter() - t0
+    rt.cudaFree(d_g)
     nreads, stride = reads.shape
     block = min(args.block, nreads)
     # inputs resident in HBM
@@ -483,6 +490,11 @@ def run_gpu(args):
         for sname in STAGES:
             acc["ms_" + sname] = acc.get("ms_" + sname, 0.0) + m.stage_ms(sname) * args.steps
     gcups = tot_cells / tot_elapsed / 1e9
+    # cells the recurrence executed: read bases run x band width (the head
+    # pass stops hopeless candidates early, so this is below the algorithmic
+    # L x (2e + 1) per candidate)
+    e_mean = E if eper is None else float(eper.mean())
+    gcups_exec = acc["myers_steps"] * (2 * e_mean + 1) / elapsed / 1e9
 
     # the plain per-batch launch for comparison: one mapper, blocks of 4,096
     # reads (the plain configuration's batch), each mapped and waited for in turn
@@ -557,6 +569,17 @@ def run_gpu(args):
 
     # roofline of the dominant kernel
     peak, peak_kind, peaks = measured_peaks()
+    # index build against the bytes it must move once: the bases read (1 B
+    # each), the bit planes + N mask written and read back (2 x 3 bits per
+    # base), the count and offset tables written and read (2 x 2 x 4^k x 4 B)
+    # and every entry's position and flank code written (6 B)
+    ib_bytes = g.size + 2 * (3 * g.size / 8) + 4 * (4 << (2 * inf.k)) + 6 * inf.n_seeds
+    index_build = {"seconds": round(index_build_s, 4), "bytes": int(ib_bytes),
+                   "gbs": round(ib_bytes / index_build_s / 1e9, 1), "peak": peak,
+                   "frac": round(ib_bytes / index_build_s / 1e9 / peak, 4),
+                   "model": "bases 1 B + bit planes and N mask written and read 2 x 3/8 B per base + count/offset "
+                            "tables 2 x 2 x 4^k x 4 B + positions and flank codes 6 B per entry; bases already on "
+                            "the device, host clock around swm_index_build_device"}
     L = float(lens.mean())
     e = E if eper is None else float(eper.mean())
     per_step = {k: v / args.steps for k, v in acc.items()}
@@ -641,22 +664,75 @@ def run_gpu(args):
                               f"timed step" if flush else
                               f"inputs larger than L2 (reads {reads.nbytes / 1e6:.0f} MB, index "
                               f"{index_bytes / 1e9:.2f} GB); no flush")},
-            "gcups": round(gcups, 2), "index_build_s": round(index_build_s, 3),
+            "gcups": round(gcups, 2), "gcups_executed": round(gcups_exec, 2),
+            "gcups_model": "gcups: algorithmic (reference-equivalent) cells, L x (2e + 1) per verified candidate; "
+                           "gcups_executed: Myers steps the device ran x (2e + 1)",
+            "index_build_s": round(index_build_s, 3), "index_build": index_build,
             "per_step": {k: int(v) if not k.startswith("ms_") else round(v, 3) for k, v in per_step.items()},
             "stages": stage_rows, "stage_timing": "kernel times of one mapper alone (untimed pass)",
             "clocks": clk, "e2e": e2e,
             "gpu_launches": int(acc["launches"]), "roofline": roofline, "int_pipe": int_pipe, "gather_roofline": gather,
             "plain_per_batch": plain}
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+    if rank == 0 and ws == 1 and (not args.no_cpu_baseline or args.parity_reads):
         arrays = ix.download()
         mix = host_map_index(arrays, w["k"])
         threads = os.cpu_count() or 1
-        v, n, dt, kind = timed_cpu_sample(mix, reads, lens, E, threads, args.cpu_seconds, eper)
-        line["cpu_baseline"] = {"value": round(v, 1), "unit": UNIT, "cores": threads, "kind": kind,
-                                "sample": f"first {n} reads of the workload, {dt:.1f} s, {threads} threads"}
+        if args.parity_reads:
+            line["parity"] = parity_sample(m, mix, reads, lens, E, eper, args.parity_reads, threads)
+        if not args.no_cpu_baseline:
+            v, n, dt, kind = timed_cpu_sample(mix, reads, lens, E, threads, args.cpu_seconds, eper)
+            line["cpu_baseline"] = {"value": round(v, 1), "unit": UNIT, "cores": threads, "kind": kind,
+                                    "sample": f"first {n} reads of the workload, {dt:.1f} s, {threads} threads"}
+    if rank == 0 and ws == 1 and args.serving and w["genome_kind"] == "human":
+        line["serving"] = serving_loads(swm, ix, g, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
+
+
+def parity_sample(m, mix, reads, lens, E, eper, nsample, threads):
+    """After the timing: the first nsample reads of the timed workload mapped
+    by the GPU path (swm_map_batch, blocks of the timed mapper's size) and by
+    the reference's own get_positions() compiled for the host (the oracle
+    restatement where the reference cannot take the reads), on the index the
+    GPU built; records, CIGARs and unmapped ids must be identical."""
+    from oracle import pyoracle as po
+    n = min(nsample, reads.shape[0])
+    got, got_unm = [], []
+    for b0 in range(0, n, m.max_reads):
+        b1 = min(n, b0 + m.max_reads)
+        out = m.map(reads[b0:b1], lens[b0:b1], E, None if eper is None else eper[b0:b1])
+        got.extend((r[0] + 2 * b0,) + r[1:] for r in out.records())
+        got_unm.extend(int(u) + 2 * b0 for u in out.unmapped)
+    in_env = int(lens[:n].max()) + 2 * E <= REF_WINDOW_BASES
+    against = "reference (oracle/_ref/libswref.so: the reference's get_positions compiled for the host)"
+    if eper is None and po.have_ref() and in_env:
+        want, want_unm = [], []
+        for b0 in range(0, n, CPU_BLOCK):
+            b1 = min(n, b0 + CPU_BLOCK)
+            res = po.ref_map_reads(mix, reads[b0:b1], lens[b0:b1], E, nthreads=threads)
+            want.extend((r[0] + 2 * b0,) + r[1:] for r in res.records())
+            want_unm.extend(int(u) + 2 * b0 for u in res.unmapped)
+    else:
+        against = "oracle (oracle/swm_oracle.c restatement; reads outside the reference's window slot)"
+        want, want_unm = [], []
+        groups = [(E, np.arange(n))] if eper is None else [(int(ev), np.nonzero(eper[:n] == ev)[0])
+                                                           for ev in np.unique(eper[:n])]
+        per = {}
+        for ev, idx in groups:
+            res = po.map_reads(mix, reads[idx], lens[idx], ev, nthreads=threads)
+            for rec in res.records():
+                r = int(idx[rec[0] >> 1])
+                per.setdefault(r, []).append((2 * r + (rec[0] & 1),) + rec[1:])
+            for u in res.unmapped:
+                per.setdefault(int(idx[u >> 1]), [])
+        for r in sorted(per):
+            if not per[r]:
+                want_unm.append(2 * r + 1)
+            want.extend(per[r])
+    equal = got == want and got_unm == want_unm
+    return {"reads": int(n), "equal": bool(equal), "records": len(got), "unmapped": len(got_unm),
+            "against": against}
 
 
 def count_mapped(buf, nreads):
@@ -665,103 +741,125 @@ def count_mapped(buf, nreads):
 
 # ------------------------------------------------------------ serving
 
+SERVE = dict(requests=4000, size_max=4096, len_min=50, len_max=250, error_rate=0.03, e_frac=0.05, read_seed=17,
+             block_reads=65536, max_slots=4, loads=(0.25, 0.5, 0.9), runs=3)
+
+
+def serving_loads(swm, ix, g, args):
+    """Serving through the library's request loop (swm_serve_*): requests of
+    log-uniform [1, 4096] reads of 50-250 bp at 3% error, e = ceil(0.05 L),
+    arrive as a Poisson stream; the server coalesces the waiting ones into
+    the next free block slot, admitting slots by free device memory. The peak
+    is all requests submitted at once; then each offered load (a fraction of
+    the peak) runs SERVE['runs'] times. A request's latency runs from its
+    scheduled arrival to the return of the poll that hands over its records
+    (host clock); p50 / p99 per run, and the spread of p99 over the runs."""
+    import threading
+    cfg = SERVE
+    rng = np.random.default_rng(cfg["read_seed"])
+    nreq = args.requests or cfg["requests"]
+    sizes = np.minimum(np.exp(rng.uniform(0.0, math.log(cfg["size_max"]), nreq)).astype(np.int64), cfg["size_max"])
+    sizes = np.maximum(sizes, 1)
+    total = int(sizes.sum())
+    reads, lens, _, _ = synth_reads(g, total, cfg["len_min"], cfg["len_max"], cfg["error_rate"], cfg["read_seed"])
+    eper = np.minimum(np.ceil(cfg["e_frac"] * lens.astype(np.float64) - 1e-9), 15).astype(np.uint8)
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    reqs = [(reads[o:o + n], lens[o:o + n], eper[o:o + n], int(eper[o:o + n].max())) for o, n in zip(offs, sizes)]
+    srv = swm.Server(ix, block_reads=cfg["block_reads"], max_slots=cfg["max_slots"], stride=256,
+                     max_queued_reads=total + cfg["block_reads"])
+
+    def run(arrivals):
+        lat = np.zeros(nreq)
+        done_t = [0.0]
+        id2q = {}
+        lock = threading.Lock()
+
+        def collector():
+            got = 0
+            while got < nreq:
+                res = srv.poll(timeout_ms=120_000)
+                if res is None:
+                    raise RuntimeError("serving: no request finished within two minutes")
+                t = time.perf_counter()
+                with lock:
+                    q = id2q.get(res[0])
+                while q is None:  # the submitting thread has not recorded the id yet
+                    time.sleep(0)
+                    with lock:
+                        q = id2q.get(res[0])
+                lat[q] = t - (t_start + arrivals[q])
+                done_t[0] = t
+                got += 1
+
+        th = threading.Thread(target=collector)
+        t_start = time.perf_counter()
+        th.start()
+        for q in range(nreq):
+            while True:
+                wait = t_start + arrivals[q] - time.perf_counter()
+                if wait <= 0:
+                    break
+                time.sleep(wait if wait > 0.0005 else 0)
+            r, ln, ep, emax = reqs[q]
+            rid = srv.submit(r, ln, emax, errors_per_read=ep)
+            with lock:
+                id2q[rid] = q
+        th.join()
+        return lat, done_t[0] - t_start
+
+    run(np.zeros(min(nreq, 200)))  # warm-up: slots made, graphs captured
+    _, span = run(np.zeros(nreq))  # everything at once: the peak
+    peak = total / span
+    rows = []
+    for load in cfg["loads"]:
+        rate = load * peak / float(sizes.mean())   # requests per second
+        per_run = []
+        for _ in range(cfg["runs"]):
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+            lat, span = run(arrivals)
+            per_run.append({"sustained_reads_per_s": round(total / span, 1),
+                            "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                            "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)})
+        p99s = [x["p99_ms"] for x in per_run]
+        rows.append({"load": load, "offered_reads_per_s": round(load * peak, 1),
+                     "sustained_reads_per_s": round(statistics.median(x["sustained_reads_per_s"] for x in per_run), 1),
+                     "p50_ms": round(statistics.median(x["p50_ms"] for x in per_run), 3),
+                     "p99_ms": round(statistics.median(p99s), 3),
+                     "p99_spread_ms": [min(p99s), max(p99s)], "runs": per_run})
+    st = srv.stats()
+    srv.close()
+    return {"peak_reads_per_s": round(peak, 1), "loads": rows, "requests": nreq,
+            "reads_per_request_mean": round(float(sizes.mean()), 1),
+            "path": "swm_serve_submit / swm_serve_poll (library request loop: continuous batching into block "
+                    "slots admitted by free device memory)",
+            "server": {"block_reads": cfg["block_reads"], "max_slots": cfg["max_slots"], "slots_made": st["slots"],
+                       "slot_bytes": st["slot_bytes"], "blocks": st["blocks"],
+                       "max_blocks_in_flight": st["max_blocks_in_flight"]}}
+
+
+def synth_reads(g, n, lmin, lmax, err, seed):
+    from swmapper_gb300 import synth
+    reads, lens, _, _ = synth.reads(g, n, lmin, lmax, err, seed=seed, stride=256)
+    return reads, lens
+
+
 def run_serving(args):
-    """Batch latency under Poisson arrivals: one host thread coalesces the
-    requests that have arrived (up to one block of reads) into the next free
-    block slot (a mapper: swm_map_submit / swm_map_wait_packed), so requests
-    arriving while others are on the GPU join the next block and overlap with
-    them; the slots are sized by free device memory. A request's latency runs
-    from its arrival to the return of the wait that delivers its records."""
+    """The serving configuration alone: the human-scale index resident, the
+    request loop under Poisson arrivals (serving_loads)."""
     import swmapper_gb300 as swm
     ws, rank, local = dist_env()
     rt = cudart()
     rt.cudaSetDevice(local)
     w = WORKLOAD
-    rng = np.random.default_rng(w["read_seed"])
-    g, reads, lens, eper = make_workload(rank)
+    from swmapper_gb300 import synth
+    g = synth.reference(w["genome_bp"], seed=w["genome_seed"], kind=w["genome_kind"])
     t0 = time.perf_counter()
     ix = swm.Index.build(g, k=w["k"], device=local)
     index_build_s = time.perf_counter() - t0
-    del g
-    nreq = args.requests or w["requests"]
-    sizes = np.minimum(np.exp(rng.uniform(0.0, math.log(4096.0), nreq)).astype(np.int64), 4096)
-    sizes = np.maximum(sizes, 1)
-    starts = np.concatenate([[0], np.cumsum(sizes)[:-1]]) % max(1, reads.shape[0] - 4096)
-    block = args.block
-    # admission by free device memory: as many block slots (mappers, each with
-    # its own buffers) as half of the free memory holds, two to four
-    rt.cudaMemGetInfo.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
-    free0, total = C.c_size_t(), C.c_size_t()
-    rt.cudaMemGetInfo(C.byref(free0), C.byref(total))
-    mappers = [swm.Mapper(ix, max_reads=block)]
-    free1 = C.c_size_t()
-    rt.cudaMemGetInfo(C.byref(free1), C.byref(total))
-    per_slot = max(1, free0.value - free1.value)
-    nslots = int(max(2, min(4, (free1.value // 2) // per_slot + 1)))
-    mappers += [swm.Mapper(ix, max_reads=block) for _ in range(nslots - 1)]
-    bufs = [swm.PackedBuffers(block) for _ in range(nslots)]
-
-    streams = [C.c_void_p(mm.stream()) for mm in mappers]
-    rt.cudaStreamQuery.argtypes = [C.c_void_p]
-
-    def serve(arrivals):
-        """Serve the requests at the given arrival offsets (s); returns the
-        latency of each and the span from the first arrival to the last reply."""
-        nq = len(arrivals)
-        lat = np.zeros(nq)
-        pend = []   # (mapper index, [request ids]), oldest first; mappers are taken in turn
-        nxt = 0
-        slot = 0
-        t_start = time.perf_counter()
-        done_t = t_start
-
-        def complete():
-            nonlocal done_t
-            j, ids = pend.pop(0)
-            mappers[j].wait_packed(bufs[j])
-            done_t = time.perf_counter()
-            for q in ids:
-                lat[q] = done_t - (t_start + arrivals[q])
-
-        while nxt < nq or pend:
-            now = time.perf_counter() - t_start
-            if nxt < nq and arrivals[nxt] <= now and len(pend) < nslots:
-                # coalesce what has arrived, up to one block of reads
-                ids, n = [], 0
-                while nxt < nq and arrivals[nxt] <= now and n + sizes[nxt] <= block:
-                    ids.append(nxt)
-                    n += int(sizes[nxt])
-                    nxt += 1
-                sel = np.concatenate([np.arange(starts[q], starts[q] + sizes[q]) for q in ids])
-                mappers[slot].submit(reads[sel], lens[sel], e_arg(eper), None if eper is None else eper[sel])
-                pend.append((slot, ids))
-                slot = (slot + 1) % nslots
-            elif pend and (len(pend) == nslots or nxt >= nq or rt.cudaStreamQuery(streams[pend[0][0]]) == 0):
-                complete()
-            elif not pend:
-                time.sleep(max(0.0, min(arrivals[nxt] - now, 0.0005)))
-        return lat, done_t - t_start
-
-    serve(np.zeros(min(nreq, 50)))  # warm-up
-    total_reads = int(sizes.sum())
-    _, span = serve(np.zeros(nreq))  # all requests at once: the peak
-    peak = total_reads / span
-    rows = []
-    for load in (0.25, 0.5, 0.9):
-        rate = load * peak / float(sizes.mean())           # requests per second
-        arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
-        lat, span = serve(arrivals)
-        rows.append({"load": load, "offered_reads_per_s": round(load * peak, 1),
-                     "sustained_reads_per_s": round(total_reads / span, 1),
-                     "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
-                     "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)})
-    line = {"metric": "batch latency p99 (serving)", "value": rows[-1]["p99_ms"], "unit": "ms", "n_gpus": 1,
-            "higher_is_better": False, "peak_reads_per_s": round(peak, 1), "loads": rows,
-            "requests": nreq, "reads_per_request_mean": round(float(sizes.mean()), 1),
-            "index_build_s": round(index_build_s, 3), "data": "synthetic",
-            "config": {**WORKLOAD, "block_reads": block, "mappers": nslots,
-                       "admission": f"{nslots} block slots: half of the free device memory "
-                                    f"({free1.value >> 20} MiB) over {per_slot >> 20} MiB per slot"}}
+    res = serving_loads(swm, ix, g, args)
+    line = {"metric": "batch latency p99 (serving)", "value": res["loads"][-1]["p99_ms"], "unit": "ms",
+            "n_gpus": 1, "higher_is_better": False, "index_build_s": round(index_build_s, 3), "data": "synthetic",
+            "config": {**WORKLOAD}, "serving": res}
     print(json.dumps(line), flush=True)
 
 
@@ -836,8 +934,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batched",
-                    help="benchmark configuration (default: batched, the headline line)")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="human",
+                    help="benchmark configuration (default: human, the 3.1 Gbp headline line)")
     ap.add_argument("--block", type=int, default=None, help="reads per mapping block (default: the workload's)")
     ap.add_argument("--mappers", type=int, default=2, help="mappers taking the blocks in turn")
     ap.add_argument("--tune", type=int, default=1, help="autotune reads per block and mappers (1) or not (0)")
@@ -847,9 +945,13 @@ def main():
                     help="passes over the reads in the end-to-end stream (pipeline fill and drain amortised over them)")
     ap.add_argument("--e2e-mappers", type=int, default=4, help="mappers in the end-to-end pipeline (>= 2)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ref-step-seconds", type=float, default=4.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=2.0)
+    ap.add_argument("--parity-reads", type=int, default=20000,
+                    help="reads of the timed workload compared with the reference's own mapper after the timing")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--requests", type=int, default=None, help="requests of the serving workload")
+    ap.add_argument("--serving", type=int, default=1,
+                    help="with the human-scale workload, also run the serving loads on its index (1) or not (0)")
     ap.add_argument("--plain", type=int, default=1, help="also time the plain per-batch launch (1) or not (0)")
     ap.add_argument("--genome-bp", type=int, default=None, help="smaller genome for quick checks")
     ap.add_argument("--nreads", type=int, default=None, help="fewer reads for quick checks")

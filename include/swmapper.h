@@ -88,11 +88,27 @@ int swm_index_get_info(const swm_index *ix, swm_index_info *info);
  * a stream being captured into a CUDA graph, or a host callback. The call
  * allocates nothing: its scratch is a 128 KB static device array, so k <= 13
  * (larger k returns SWM_ERR_ARG). The first call on a device looks up that
- * array's address and should come before any stream capture. All calls on a
+ * array's address and should come before any stream capture; the address is
+ * kept for the life of the process, so the device's primary context must not
+ * be reset (cudaDeviceReset) while the library is in use. All calls on a
  * device share the array: calls that overlap on the GPU (other streams,
  * other threads) race; serialise them. stream is a cudaStream_t (NULL =
  * default stream); the call is asynchronous on it. */
 int swm_hash_offset_noalloc(const uint32_t *d_hash_count, uint32_t *d_hash_offset, uint32_t k, void *stream);
+
+/* No counterpart in the reference (a device-only structure derived from the
+ * index arrays; the files are unchanged). For k = 12 the first mapper made on
+ * an index builds a candidate table when the device has room for it: the
+ * entries of every bucket grouped, for each seed shift, by the 6 flank bits
+ * long_seeds_filter compares (mapper_cpe.c:2090-2123), behind a directly
+ * indexed table of 2^32 + 1 offsets (about 17 GiB, plus 16 bytes per index
+ * entry). The candidate stage then reads only the entries the filter keeps
+ * instead of every entry of the fetched buckets; results are identical
+ * either way. enable = 0 drops the table and keeps it from being built again
+ * (mappers fall back to filtering every entry; call it with no block in
+ * flight), enable = 1 builds it now if it is missing and fits. *bytes (may be
+ * NULL) gets the table's device bytes, 0 when there is none. */
+int swm_index_candidate_table(swm_index *ix, int enable, uint64_t *bytes);
 
 /* Copy the index arrays to host memory in file layout (any pointer may be
  * NULL). hash_offset_end gets the END offsets serial_index writes. */
@@ -226,6 +242,77 @@ int swm_mapper_debug_candidates(const swm_mapper *m, uint32_t *item, uint32_t *p
 int swm_mapper_debug_read_words(const swm_mapper *m, uint32_t *words, uint64_t cap_items);
 
 void swm_mapper_free(swm_mapper *m);
+
+/* ---------------------------------------------------------------- serving */
+
+/* Request loop over a resident index. Replaces the reference's block loop
+ * with spawn / join double buffering (mapper_mpe.c:945-1106), which maps one
+ * fixed block at a time: a server takes requests of any size as they arrive
+ * and an engine thread coalesces the waiting ones into the next block (up to
+ * block_reads reads) whenever a block slot is free, so requests that arrive
+ * while other blocks are on the GPU are admitted as slots free up and their
+ * blocks overlap on the device. A block slot is one mapper (its own CUDA
+ * stream and work buffers); slots are made on demand, each only when the
+ * device reports the memory for it free at that moment and the caller's limit
+ * allows it. Results are the same as mapping each request alone. */
+typedef struct swm_server swm_server;
+
+typedef struct {
+    uint64_t block_reads;       /* reads per block slot (the coalescing limit)   */
+    uint32_t max_slots;         /* block slots at most (blocks in flight)        */
+    uint64_t stride;            /* read stride inside the server (>= the longest
+                                   read; reads are copied to it at submission)  */
+    uint64_t max_queued_reads;  /* reads waiting for a slot at most (>= block_reads);
+                                   a request beyond it is refused               */
+    uint64_t device_mem_limit;  /* device bytes the slots may hold (0 = no limit
+                                   beyond the device's free memory)             */
+    uint64_t device_mem_reserve;/* device bytes to leave free when making a slot */
+} swm_serve_config;
+
+typedef struct {
+    uint64_t slots;                /* block slots made                            */
+    uint64_t slot_bytes;           /* device memory of one slot (measured)        */
+    uint64_t blocks;               /* blocks launched                             */
+    uint64_t max_blocks_in_flight; /* most blocks on the GPU at once              */
+    uint64_t requests_admitted, requests_done, reads_done;
+    uint64_t refused_memory;       /* submissions refused: no slot fits (SWM_ERR_OOM) */
+    uint64_t refused_queue;        /* submissions refused: queue full (SWM_ERR_STATE) */
+    uint64_t queued_reads;         /* reads waiting for a slot now                */
+} swm_serve_counters;
+
+typedef struct {
+    uint64_t id;
+    uint64_t reads;        /* reads of the request                          */
+    uint64_t block_reads;  /* reads of the block it was mapped in           */
+    double latency_ms;     /* submission to results ready (host clock)      */
+} swm_request_info;
+
+/* Start a server on a resident index. Makes the first block slot (which
+ * measures a slot's device memory); SWM_ERR_OOM when the device cannot hold
+ * one. The index must outlive the server. */
+int swm_serve_open(swm_index *ix, const swm_serve_config *cfg, swm_server **out);
+
+/* Admit one request of 1..block_reads reads (host memory; copied before the
+ * call returns) and return its id. Refused with SWM_ERR_OOM when no block slot
+ * can ever be made within the memory allowed, with SWM_ERR_STATE when the
+ * reads already waiting plus these would exceed max_queued_reads (or the
+ * server is closing), with SWM_ERR_ARG for reads outside the envelope. */
+int swm_serve_submit(swm_server *s, const swm_batch *b, uint64_t *id);
+
+/* The next finished request, waiting up to timeout_ms (< 0: no limit; 0: do
+ * not wait): its id, its packed records with read ids relative to the request
+ * (cur_read = 2 * read + strand), and optionally info. SWM_ERR_TIMEOUT when
+ * none finished in time; SWM_ERR_OVERFLOW when r's buffers are too small (the
+ * n_* fields hold the sizes needed and the result stays first in line); a
+ * request whose block failed returns that block's status once. r may be NULL
+ * to drop the records. */
+int swm_serve_poll(swm_server *s, int timeout_ms, uint64_t *id, swm_packed_result *r, swm_request_info *info);
+
+int swm_serve_stats(swm_server *s, swm_serve_counters *out);
+
+/* Stop admitting, finish the requests already admitted, free the slots and
+ * any results not polled. */
+int swm_serve_close(swm_server *s);
 
 /* Rate at which the device serves independent random 32-byte reads from a
  * buffer of the given size (>= 1 MiB; larger than L2 for DRAM, smaller for

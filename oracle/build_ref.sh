@@ -55,7 +55,11 @@ if [ ! -f "$SRC/mapper_ref.c" ]; then
   exit 2
 fi
 
-CFLAGS="-O2 -std=gnu99 -fgnu89-inline -w"
+# -fsigned-char: the reference prints CIGAR run lengths as '0' + (char)v % 10
+# (mapper_cpe.c:223), which depends on char being signed; it is pinned as
+# built on x86, where it is. Arm's default unsigned char would print other
+# bytes for runs of 128 or more.
+CFLAGS="-O2 -std=gnu99 -fgnu89-inline -fsigned-char -w"
 $CC $CFLAGS -I"$SHIM" -I"$SRC" "$SRC/serial_index_verbatim.c" -Wl,--wrap=malloc -o "$OUT/serial_index_verbatim"
 $CC $CFLAGS -I"$SHIM" -I"$SRC" -include "$SHIM/ub_defined.h" "$SRC/serial_index_defined.c" -Wl,--wrap=malloc -o "$OUT/serial_index"
 $CC $CFLAGS -fPIC -ftrivial-auto-var-init=zero -I"$SHIM" -I"$SRC" -include "$SHIM/mapper_prelude.h" \

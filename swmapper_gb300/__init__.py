@@ -54,8 +54,29 @@ class MapStats(C.Structure):
     _fields_ = [(f, C.c_uint64) for f in STAT_FIELDS]
 
 
+class ServeConfig(C.Structure):
+    _fields_ = [("block_reads", C.c_uint64), ("max_slots", C.c_uint32), ("stride", C.c_uint64),
+                ("max_queued_reads", C.c_uint64), ("device_mem_limit", C.c_uint64),
+                ("device_mem_reserve", C.c_uint64)]
+
+
+SERVE_FIELDS = ["slots", "slot_bytes", "blocks", "max_blocks_in_flight", "requests_admitted", "requests_done",
+                "reads_done", "refused_memory", "refused_queue", "queued_reads"]
+
+
+class ServeCounters(C.Structure):
+    _fields_ = [(f, C.c_uint64) for f in SERVE_FIELDS]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("reads", C.c_uint64), ("block_reads", C.c_uint64),
+                ("latency_ms", C.c_double)]
+
+
 class SwmError(RuntimeError):
-    pass
+    def __init__(self, msg, rc=None):
+        super().__init__(msg)
+        self.rc = rc
 
 
 _lib = None
@@ -77,6 +98,7 @@ def lib():
         L.swm_index_save.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_size_t]
         L.swm_index_get_info.argtypes = [vp, C.POINTER(IndexInfo)]
         L.swm_index_download.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.swm_index_candidate_table.argtypes = [vp, C.c_int, C.POINTER(u64)]
         L.swm_index_free.argtypes = [vp]
         L.swm_index_free.restype = None
         L.swm_mapper_create.argtypes = [vp, u64, C.POINTER(vp)]
@@ -100,13 +122,18 @@ def lib():
         L.swm_mapper_free.argtypes = [vp]
         L.swm_mapper_free.restype = None
         L.swm_probe_random_reads.argtypes = [C.c_int, u64, C.POINTER(C.c_double)]
+        L.swm_serve_open.argtypes = [vp, C.POINTER(ServeConfig), C.POINTER(vp)]
+        L.swm_serve_submit.argtypes = [vp, C.POINTER(Batch), C.POINTER(u64)]
+        L.swm_serve_poll.argtypes = [vp, C.c_int, C.POINTER(u64), C.POINTER(PackedResult), C.POINTER(RequestInfo)]
+        L.swm_serve_stats.argtypes = [vp, C.POINTER(ServeCounters)]
+        L.swm_serve_close.argtypes = [vp]
         _lib = L
     return _lib
 
 
 def _check(rc: int, what: str) -> None:
     if rc != 0:
-        raise SwmError(f"{what} failed ({rc}): {lib().swm_last_error().decode(errors='replace')}")
+        raise SwmError(f"{what} failed ({rc}): {lib().swm_last_error().decode(errors='replace')}", rc)
 
 
 def probe_random_reads(nbytes: int, device: int = 0) -> float:
@@ -129,6 +156,13 @@ class Index:
                                    dtype=np.uint8)
         h = C.c_void_p()
         _check(lib().swm_index_build(seq.ctypes.data, seq.size, k, device, C.byref(h)), "swm_index_build")
+        return cls(h)
+
+    @classmethod
+    def build_device(cls, d_seq: int, n: int, k: int = 12, device: int = 0) -> "Index":
+        """Index n bases already in device memory (swm_index_build_device)."""
+        h = C.c_void_p()
+        _check(lib().swm_index_build_device(d_seq, n, k, device, C.byref(h)), "swm_index_build_device")
         return cls(h)
 
     @classmethod
@@ -159,6 +193,14 @@ class Index:
                                                    ("hash_count", "hash_offset", "positions", "pos_lseeds",
                                                     "base_2bits", "base_3bits"))), "swm_index_download")
         return out
+
+    def candidate_table(self, enable: bool) -> int:
+        """Build (True) or drop (False) the device-only candidate table
+        (swm_index_candidate_table); returns its device bytes (0: none)."""
+        nbytes = C.c_uint64()
+        _check(lib().swm_index_candidate_table(self._h, 1 if enable else 0, C.byref(nbytes)),
+               "swm_index_candidate_table")
+        return int(nbytes.value)
 
     def close(self) -> None:
         if self._h:
@@ -331,3 +373,68 @@ class PackedBuffers:
             cp += ln
         return out
 
+
+
+class Server:
+    """Request loop over a resident index (swm_serve_*): continuous batching of
+    requests into block slots, slots admitted by free device memory."""
+
+    def __init__(self, index: Index, block_reads: int = 65536, max_slots: int = 4, stride: int = 256,
+                 max_queued_reads: int | None = None, device_mem_limit: int = 0, device_mem_reserve: int = 1 << 30):
+        self.index = index
+        self.stride = stride
+        cfg = ServeConfig(block_reads, max_slots, stride, max_queued_reads or 4 * block_reads * max_slots,
+                          device_mem_limit, device_mem_reserve)
+        h = C.c_void_p()
+        _check(lib().swm_serve_open(index._h, C.byref(cfg), C.byref(h)), "swm_serve_open")
+        self._h = h
+        self.block_reads = block_reads
+
+    def submit(self, reads: np.ndarray, lens: np.ndarray, errors: int, errors_per_read=None) -> int:
+        """Admit one request; returns its id (raises SwmError with .rc on refusal)."""
+        reads = np.ascontiguousarray(reads, np.uint8)
+        lens = np.ascontiguousarray(lens, np.uint32)
+        n, stride = reads.shape
+        epr = None if errors_per_read is None else np.ascontiguousarray(errors_per_read, np.uint8)
+        b = Batch(reads.ctypes.data, lens.ctypes.data, stride, n, errors, epr.ctypes.data if epr is not None else None)
+        rid = C.c_uint64()
+        _check(lib().swm_serve_submit(self._h, C.byref(b), C.byref(rid)), "swm_serve_submit")
+        return int(rid.value)
+
+    def poll(self, timeout_ms: int = -1, out: "PackedBuffers | None" = None):
+        """(id, records or None, info dict) of the next finished request, or
+        None when none finished within timeout_ms."""
+        rid = C.c_uint64()
+        info = RequestInfo()
+        if out is None:
+            out = self._buf = getattr(self, "_buf", None) or PackedBuffers(self.block_reads)
+        while True:
+            rc = lib().swm_serve_poll(self._h, timeout_ms, C.byref(rid), C.byref(out.c), C.byref(info))
+            if rc == -6:
+                return None
+            if rc == -5:   # grow the buffers to the sizes reported and take it again
+                c = out.c
+                out = PackedBuffers(self.block_reads, words_per_read=1 + int(c.n_words) // max(1, self.block_reads),
+                                    cigar_per_read=1 + int(c.n_cigar) // max(1, self.block_reads),
+                                    records_per_read=1 + int(c.n_records) // max(1, self.block_reads))
+                self._buf = out
+                continue
+            _check(rc, "swm_serve_poll")
+            return int(rid.value), out.records(), {"reads": int(info.reads), "block_reads": int(info.block_reads),
+                                                   "latency_ms": float(info.latency_ms)}
+
+    def stats(self) -> dict:
+        s = ServeCounters()
+        _check(lib().swm_serve_stats(self._h, C.byref(s)), "swm_serve_stats")
+        return {f: int(getattr(s, f)) for f in SERVE_FIELDS}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().swm_serve_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -22,7 +22,7 @@ BIN_INDEX = os.path.join(PKG, "swm_index")
 BIN_MAP = os.path.join(PKG, "swm_mapper")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["swm_index.cu", "swm_map.cu", "swm_probe.cu"]
+CUDA_SOURCES = ["swm_index.cu", "swm_map.cu", "swm_probe.cu", "swm_serve.cu"]
 HOST_SOURCES = ["swm_files.c", "swm_sam.c"]
 
 

@@ -38,7 +38,30 @@ struct swm_index {
     uint16_t *d_ls;        // n_seeds (+8): their 12-bit flank codes (.pos_lseeds)
     uint32_t *d_b2;        // n_words2 + SWM_PAD_WORDS
     uint32_t *d_b3;        // n_words3 + SWM_PAD_WORDS
+    // Candidate table (k = 12 only; device-only, derived from the arrays
+    // above): the entries of every bucket grouped, for each seed shift t, by
+    // the 6 flank bits the filter of shift t compares, so that the entries a
+    // read's seed keeps form one contiguous, position-ordered range.
+    uint32_t *d_ctab_off;  // SWM_CTAB_KEYS + 1 start offsets into d_ctab_pos
+    uint32_t *d_ctab_pos;  // 4 * n_seeds (+8) positions
+    uint32_t ctab_gen;     // bumped whenever the table is built or dropped
+    int ctab_off;          // the caller dropped the table: no automatic build
 };
+
+// Key of the candidate table: seed code << 8 | shift << 6 | flank, where
+// flank = rl | rh << 3 are the lo / hi bits of the 3 long-seed bases outside
+// the 12-mer (the bits long_seeds_filter compares, mapper_cpe.c:2107-2112).
+#define SWM_CTAB_KEYS (1ull << 32)
+__host__ __device__ __forceinline__ uint32_t swm_ctab_key(uint32_t seed, uint32_t shift, uint32_t flank) {
+    return (seed << 8) | (shift << 6) | flank;
+}
+// The flank value an index entry with flank code ls offers to shift t.
+__host__ __device__ __forceinline__ uint32_t swm_ctab_flank(uint32_t ls, uint32_t t) {
+    const uint32_t sh = SWM_SEED_STEP - 1 - t;
+    return ((ls >> sh) & 7u) | (((ls >> (6 + sh)) & 7u) << 3);
+}
+// Build / drop the table (swm_index.cu); the mapper builds it on demand.
+int swm_ctab_build(swm_index *ix);
 
 // Exclusive scan of n u32 values (n read from *d_n when d_n is not NULL,
 // else n_host; clamped to n_cap); out gets n + 1 entries, out[n] = total,

@@ -385,6 +385,95 @@ __global__ void kb_split(const unsigned long long *__restrict__ keys, uint64_t S
     }
 }
 
+// ---------------------------------------------------- candidate table
+//
+// long_seeds_filter (mapper_cpe.c:2090-2123) keeps an entry of a seed's
+// bucket when the 3 flank bits of each plane at the seed's shift equal the
+// read's, i.e. when the whole 15-base long seed matches. The table groups, for
+// every bucket and every shift t, the bucket's entries by that 6-bit flank
+// value (stable: ascending position inside a group), so that the entries one
+// (seed, shift, read flank) keeps are one contiguous range of positions, found
+// with a single offset lookup. Segment (bucket B, shift t) starts at
+// 4 * off[B] + t * count[B]; ctab_off[key(B, t, v)] is where flank value v
+// starts in it, and ctab_off[key + 1] where it ends (the next key's start,
+// also across shifts and buckets; the last entry holds 4 * n_seeds).
+
+#define CTAB_WARPS 8
+
+// One warp per bucket: for each shift a 64-bin histogram of the flank values,
+// its exclusive scan (the 64 offsets, written as one coalesced 256-byte row)
+// and a stable scatter of the positions (rank among equal values from a
+// match mask, chunk by chunk in position order).
+__global__ void __launch_bounds__(CTAB_WARPS * 32) kb_ctab(const uint32_t *__restrict__ off, uint64_t nb,
+                                                           const uint32_t *__restrict__ pos,
+                                                           const uint16_t *__restrict__ ls,
+                                                           uint32_t *__restrict__ ctab_off,
+                                                           uint32_t *__restrict__ ctab_pos) {
+    __shared__ uint32_t hist_all[CTAB_WARPS][64];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t *hist = hist_all[wib];
+    uint32_t lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    const uint64_t nwarps = (uint64_t)gridDim.x * CTAB_WARPS;
+    for (uint64_t b = (uint64_t)blockIdx.x * CTAB_WARPS + wib; b < nb; b += nwarps) {
+        const uint32_t o = off[b], c = off[b + 1] - o;
+        uint32_t *row = ctab_off + (b << 8);
+        if (c == 0) { // every key of an empty bucket starts (and ends) at its segment
+            const uint32_t v = 4u * o;
+            reinterpret_cast<uint4 *>(row)[lane] = make_uint4(v, v, v, v);
+            reinterpret_cast<uint4 *>(row)[lane + 32] = make_uint4(v, v, v, v);
+            continue;
+        }
+        // small buckets keep their entries in registers across the 4 shifts
+        const uint32_t l0 = lane < c ? ls[o + lane] : 0u;
+        const uint32_t p0 = lane < c ? pos[o + lane] : 0u;
+        for (uint32_t t = 0; t < SWM_SEED_STEP; t++) {
+            const uint32_t base = 4u * o + t * c;
+            hist[lane] = 0;
+            hist[lane + 32] = 0;
+            __syncwarp();
+            for (uint32_t j0 = 0; j0 < c; j0 += 32) {
+                const bool in = j0 + lane < c;
+                const uint32_t l = c <= 32 ? l0 : (in ? (uint32_t)ls[o + j0 + lane] : 0u);
+                const uint32_t v = in ? swm_ctab_flank(l, t) : 64u + lane; // out-of-range lanes match nobody
+                const uint32_t mm = __match_any_sync(0xffffffffu, v);
+                if (in && (mm & lt) == 0) hist[v] += __popc(mm); // one leader per value
+                __syncwarp();
+            }
+            // exclusive scan of the 64 bins, two per lane
+            const uint32_t a = hist[2 * lane], d = hist[2 * lane + 1];
+            uint32_t inc = a + d;
+#pragma unroll
+            for (int k = 1; k < 32; k <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, k);
+                if ((int)lane >= k) inc += y;
+            }
+            const uint32_t s0 = base + inc - (a + d);
+            reinterpret_cast<uint2 *>(row + (t << 6))[lane] = make_uint2(s0, s0 + a);
+            __syncwarp();
+            hist[2 * lane] = s0; // now the running cursor of each value
+            hist[2 * lane + 1] = s0 + a;
+            __syncwarp();
+            for (uint32_t j0 = 0; j0 < c; j0 += 32) {
+                const bool in = j0 + lane < c;
+                const uint32_t l = c <= 32 ? l0 : (in ? (uint32_t)ls[o + j0 + lane] : 0u);
+                const uint32_t p = c <= 32 ? p0 : (in ? pos[o + j0 + lane] : 0u);
+                const uint32_t v = in ? swm_ctab_flank(l, t) : 64u + lane;
+                const uint32_t mm = __match_any_sync(0xffffffffu, v);
+                uint32_t at = 0;
+                if (in) at = hist[v] + __popc(mm & lt);
+                __syncwarp();
+                if (in) {
+                    ctab_pos[at] = p;
+                    if ((mm & lt) == 0) hist[v] += __popc(mm);
+                }
+                __syncwarp();
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------- host helpers
 // ----------------------------------------------------------- host helpers
 
 static int sm_count(int device) {
@@ -402,6 +491,8 @@ static unsigned grid_for(uint64_t work, unsigned threads, int device, int per_sm
 
 static void index_release(swm_index *ix) {
     if (!ix) return;
+    cudaFree(ix->d_ctab_off);
+    cudaFree(ix->d_ctab_pos);
     cudaFree(ix->d_count);
     cudaFree(ix->d_off);
     cudaFree(ix->d_pos);
@@ -879,6 +970,78 @@ extern "C" void swm_index_free(swm_index *ix) {
     index_release(ix);
 }
 
+static std::mutex g_ctab_mu;
+
+// Device bytes of the candidate table of ix.
+static uint64_t ctab_bytes(const swm_index *ix) { return (SWM_CTAB_KEYS + 1) * 4 + (4 * ix->n_seeds + 8) * 4; }
+
+// Build the candidate table when it is missing, k is 12, the caller has not
+// dropped it, and the device holds it with a margin (8 GiB) to spare. Not
+// building it is not an error: the mapper then filters the buckets entry by
+// entry. Returns SWM_OK in both cases; a CUDA error while building is returned.
+int swm_ctab_build(swm_index *ix) {
+    std::lock_guard<std::mutex> lk(g_ctab_mu);
+    if (ix->d_ctab_off || ix->ctab_off || ix->k != 12 || 4 * ix->n_seeds + 8 >= 0xffffffffull) return SWM_OK;
+    SWM_CUDA(cudaSetDevice(ix->device));
+    size_t fr = 0, total = 0;
+    if (cudaMemGetInfo(&fr, &total) != cudaSuccess || fr < ctab_bytes(ix) + (8ull << 30)) {
+        cudaGetLastError();
+        return SWM_OK;
+    }
+    uint32_t *d_o = nullptr, *d_p = nullptr;
+    if (cudaMalloc(&d_o, (SWM_CTAB_KEYS + 1) * 4) != cudaSuccess ||
+        cudaMalloc(&d_p, (4 * ix->n_seeds + 8) * 4) != cudaSuccess) {
+        cudaFree(d_o);
+        cudaGetLastError();
+        return SWM_OK;
+    }
+    const uint64_t nb = 1ull << (2 * ix->k);
+    const uint32_t last = (uint32_t)(4 * ix->n_seeds);
+    cudaError_t e = cudaMemcpy(d_o + SWM_CTAB_KEYS, &last, 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(d_p + 4 * ix->n_seeds, 0, 32);
+    if (e == cudaSuccess) {
+        kb_ctab<<<grid_for(nb * 32, CTAB_WARPS * 32, ix->device, 8), CTAB_WARPS * 32>>>(ix->d_off, nb, ix->d_pos,
+                                                                                       ix->d_ls, d_o, d_p);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        cudaFree(d_o);
+        cudaFree(d_p);
+        swm_set_error("building the candidate table: %s", cudaGetErrorString(e));
+        return SWM_ERR_CUDA;
+    }
+    ix->d_ctab_off = d_o;
+    ix->d_ctab_pos = d_p;
+    ix->ctab_gen++;
+    return SWM_OK;
+}
+
+extern "C" int swm_index_candidate_table(swm_index *ix, int enable, uint64_t *bytes) {
+    if (!ix) return SWM_ERR_ARG;
+    if (enable) {
+        {
+            std::lock_guard<std::mutex> lk(g_ctab_mu);
+            ix->ctab_off = 0;
+        }
+        const int rc = swm_ctab_build(ix);
+        if (rc) return rc;
+    } else {
+        std::lock_guard<std::mutex> lk(g_ctab_mu);
+        ix->ctab_off = 1;
+        if (ix->d_ctab_off) {
+            SWM_CUDA(cudaSetDevice(ix->device));
+            cudaDeviceSynchronize(); // no block may still read the table
+            cudaFree(ix->d_ctab_off);
+            cudaFree(ix->d_ctab_pos);
+            ix->d_ctab_off = ix->d_ctab_pos = nullptr;
+            ix->ctab_gen++;
+        }
+    }
+    if (bytes) *bytes = ix->d_ctab_off ? ctab_bytes(ix) : 0;
+    return SWM_OK;
+}
+
 // ------------------------------------------------ allocation-free offsets
 
 // Scratch of swm_hash_offset_noalloc: the scan's block partial sums, one word
@@ -895,7 +1058,9 @@ static uint32_t *g_noalloc_addr[NOALLOC_MAX_DEVICES]; // device address of the a
 // arrays, and the scan's partial sums go to the static array above instead of
 // a cudaMalloc'ed buffer. Its first call on a device looks up the array's
 // device address (cudaGetSymbolAddress) with that device current; make that
-// first call before any stream capture.
+// first call before any stream capture. The address is cached for the life of
+// the process: a cudaDeviceReset of the primary context would leave it stale,
+// so resetting a device the library uses is not supported.
 extern "C" int swm_hash_offset_noalloc(const uint32_t *d_hash_count, uint32_t *d_hash_offset, uint32_t k,
                                        void *stream) {
     if (!d_hash_count || !d_hash_offset || k < 1 || k > 16) {

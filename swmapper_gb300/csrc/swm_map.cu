@@ -96,6 +96,7 @@ struct MapBufs {
     uint32_t *it_w;        // items * 32: [0..15] Myers planes, [16..31] Hamming planes
     uint2 *sel;            // items * 64: (bucket start, count) of the seed of long seed l, shift t at 4 l + t
     uint8_t *sel_fl;       // items * 64: its read flank bits rl | rh << 3 (rl, rh: 3 bits each)
+    uint32_t *sel_key;     // items * 64: its candidate-table key (k = 12)
     unsigned long long *it_perm; // items: selected slot i is record 4 * nibble(i / 4) + i % 4
     uint8_t *it_nsel, *it_e;
     uint32_t *it_nch, *it_nel, *it_nbat;
@@ -182,6 +183,7 @@ struct swm_mapper {
     cudaGraphExec_t gexec;
     int gclass;                // k_seed variant the graph was captured with
     uint32_t gen, ggen;        // buffer generation now / when the graph was captured
+    uint32_t gctab;            // candidate-table generation of the index when captured
 };
 
 // ======================================================================
@@ -635,7 +637,8 @@ __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const u
                                                const uint32_t (&phi)[8], const uint32_t (&pok)[8], uint32_t nl,
                                                const uint32_t *__restrict__ off, uint64_t pol,
                                                uint2 *__restrict__ rec, uint32_t *__restrict__ flw,
-                                               uint32_t (&cnt)[NL], uint32_t (&nref)[NL]) {
+                                               uint32_t *__restrict__ keys, uint32_t (&cnt)[NL],
+                                               uint32_t (&nref)[NL]) {
     static_assert(NL % 2 == 0, "flank words are stored in pairs");
     uint32_t pf = 0;
 #pragma unroll
@@ -645,7 +648,7 @@ __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const u
         const uint32_t nlo = wj0 + 1 < 8 ? plo[wj0 + 1] : 0u, nhi = wj0 + 1 < 8 ? phi[wj0 + 1] : 0u;
         const uint32_t lr = (sh0 ? __funnelshift_r(plo[wj0], nlo, sh0) : plo[wj0]) & 0x7fffu;
         const uint32_t hr = (sh0 ? __funnelshift_r(phi[wj0], nhi, sh0) : phi[wj0]) & 0x7fffu;
-        uint32_t csum = 0, rsum = 0, f = 0, po = 0, pc = 0;
+        uint32_t csum = 0, rsum = 0, f = 0, po = 0, pc = 0, kk4[SWM_SEED_STEP];
 #pragma unroll
         for (uint32_t sft = 0; sft < SWM_SEED_STEP; sft++) {
             const uint32_t o = ob + sft, w = o >> 4;
@@ -666,10 +669,12 @@ __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const u
             po = o0;
             pc = c;
             f |= (rl | (rh << 3)) << (8 * sft);
+            kk4[sft] = swm_ctab_key(sd, sft, rl | (rh << 3));
             csum += c;
             rsum += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
         }
         if (l & 1) reinterpret_cast<uint2 *>(flw)[l >> 1] = make_uint2(pf, f); // two long seeds per store
+        reinterpret_cast<uint4 *>(keys)[l] = make_uint4(kk4[0], kk4[1], kk4[2], kk4[3]);
         pf = f;
         cnt[l] = act ? csum : 0u;
         nref[l] = act ? rsum : 0u;
@@ -924,8 +929,9 @@ __global__ void SEED12_BOUNDS k_seed12(const uint32_t *__restrict__ off, MapBufs
         const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
         uint32_t CNT[NL], IDX[NL], REF[NL];
         uint32_t *flw = reinterpret_cast<uint32_t *>(B.sel_fl + sb);
-        if (has_n) seed12_records<NL, true>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, CNT, REF);
-        else seed12_records<NL, false>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, CNT, REF);
+        uint32_t *keys = B.sel_key + sb;
+        if (has_n) seed12_records<NL, true>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, keys, CNT, REF);
+        else seed12_records<NL, false>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, keys, CNT, REF);
 #pragma unroll
         for (int l = 0; l < NL; l++) IDX[l] = l;
         // exchange sort (1391-1399), unrolled
@@ -1453,6 +1459,71 @@ __device__ __forceinline__ uint32_t warp_sort_unique(const uint32_t *buf, uint32
     return u;
 }
 
+// The kept (adjusted) positions of one batch, sorted ascending and unique,
+// written to dst (merge + unique of block_heap_sort, mapper_cpe.c:1999-2089);
+// returns how many. They sit in sc (shared memory) or, when spilled, in the
+// warp's global scratch gs (room for SWM_BATCH_POSITIONS).
+__device__ __forceinline__ uint32_t batch_sort_unique(uint32_t *sc, uint32_t *gs, bool spilled, uint32_t kept,
+                                                      uint32_t *dst) {
+    const uint32_t lane = lane_id();
+    uint32_t u = 0;
+    if (kept <= 32) {
+        // survivors are mostly copies of a few positions: take the
+        // distinct values smallest first (up to 8), sort what is left
+        uint32_t v = lane < kept ? sc[lane] : 0xffffffffu, res = 0;
+        for (;;) {
+            const uint32_t m = __reduce_min_sync(0xffffffffu, v);
+            if (m == 0xffffffffu || u == 8) break;
+            res = lane == u ? m : res;
+            v = v == m ? 0xffffffffu : v;
+            u++;
+        }
+        if (lane < u) dst[lane] = res;
+        if (__any_sync(0xffffffffu, v != 0xffffffffu)) {
+            warp_sort_k<32>(v);
+            const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
+            const bool keep = v != 0xffffffffu && (lane == 0 || prev != v);
+            const uint32_t m = __ballot_sync(0xffffffffu, keep);
+            if (keep) dst[u + __popc(m & lanemask_lt())] = v;
+            u += __popc(m);
+        }
+    } else if (kept <= 64) {
+        u = warp_sort_unique<2>(sc, kept, dst);
+    } else if (kept <= 128) {
+        u = warp_sort_unique<4>(gs, kept, dst);
+    } else if (kept <= 256) {
+        u = warp_sort_unique<8>(gs, kept, dst);
+    } else { // bitonic sort in the warp's global scratch
+        uint32_t n2 = 512;
+        while (n2 < kept) n2 <<= 1;
+        uint32_t *buf = spilled ? gs : sc;
+        for (uint32_t i = kept + lane; i < n2; i += 32) buf[i] = 0xffffffffu;
+        __syncwarp();
+        for (uint32_t size = 2; size <= n2; size <<= 1) {
+            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t i = lane; i < n2 / 2; i += 32) {
+                    const uint32_t lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
+                    const bool up = ((lo & size) == 0);
+                    const uint32_t a = buf[lo], d = buf[hi];
+                    if ((a > d) == up) {
+                        buf[lo] = d;
+                        buf[hi] = a;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        for (uint32_t i0 = 0; i0 < kept; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool keep = i < kept && (i == 0 || buf[i - 1] != buf[i]);
+            const uint32_t m = __ballot_sync(0xffffffffu, keep);
+            if (keep) dst[u + __popc(m & lanemask_lt())] = buf[i];
+            u += __popc(m);
+        }
+    }
+    return u;
+}
+
 #define CAND_MAXCH 128 // chunks (runs) per batch: block_size < 256 allows at most 128
 
 #define CAND_SMEM_KEEP 64 // survivors of a batch held in shared memory (more go to global scratch)
@@ -1590,62 +1661,193 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
                     kept += __popc(m);
                 }
                 __syncwarp();
-                uint32_t u = 0;
-                uint32_t *dst = B.cand_ub + e0;
-                if (kept <= 32) {
-                    // survivors are mostly copies of a few positions: take the
-                    // distinct values smallest first (up to 8), sort what is left
-                    uint32_t v = lane < kept ? S.sc[lane] : 0xffffffffu, res = 0;
-                    for (;;) {
-                        const uint32_t m = __reduce_min_sync(0xffffffffu, v);
-                        if (m == 0xffffffffu || u == 8) break;
-                        res = lane == u ? m : res;
-                        v = v == m ? 0xffffffffu : v;
-                        u++;
-                    }
-                    if (lane < u) dst[lane] = res;
-                    if (__any_sync(0xffffffffu, v != 0xffffffffu)) {
-                        warp_sort_k<32>(v);
-                        const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
-                        const bool keep = v != 0xffffffffu && (lane == 0 || prev != v);
-                        const uint32_t m = __ballot_sync(0xffffffffu, keep);
-                        if (keep) dst[u + __popc(m & lanemask_lt())] = v;
-                        u += __popc(m);
-                    }
-                } else if (kept <= 64) {
-                    u = warp_sort_unique<2>(S.sc, kept, dst);
-                } else if (kept <= 128) {
-                    u = warp_sort_unique<4>(gscratch(), kept, dst);
-                } else if (kept <= 256) {
-                    u = warp_sort_unique<8>(gscratch(), kept, dst);
-                } else { // bitonic sort in the warp's global scratch
-                    uint32_t n2 = 512;
-                    while (n2 < kept) n2 <<= 1;
-                    uint32_t *buf = spilled ? gscratch() : S.sc;
-                    for (uint32_t i = kept + lane; i < n2; i += 32) buf[i] = 0xffffffffu;
-                    __syncwarp();
-                    for (uint32_t size = 2; size <= n2; size <<= 1) {
-                        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-                            for (uint32_t i = lane; i < n2 / 2; i += 32) {
-                                const uint32_t lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
-                                const bool up = ((lo & size) == 0);
-                                const uint32_t a = buf[lo], d = buf[hi];
-                                if ((a > d) == up) {
-                                    buf[lo] = d;
-                                    buf[hi] = a;
-                                }
-                            }
-                            __syncwarp();
+                const uint32_t u = batch_sort_unique(S.sc, gscratch(), spilled, kept, B.cand_ub + e0);
+                if (lane == 0) B.bt_cnt[sbase + b] = u;
+                total += u;
+                __syncwarp();
+            }
+        }
+        if (lane == 0) B.it_ncand[item] = total;
+    }
+}
+
+// ======================================================================
+// k_cand_table: the same batches from the candidate table (k = 12)
+// ======================================================================
+//
+// With the candidate table, the entries a seed's flank filter keeps are one
+// position-ordered range of the table (key: seed code, shift, read flank), so
+// a batch reads only its survivors instead of every entry of its chunks. A
+// batch's survivors of seed i are the range's entries whose bucket rank is
+// among the ranks the batch fetched for that seed: all of them when the item
+// has one batch; otherwise those after the previous batches' and at or below
+// the position of the last rank fetched so far (positions are unique and
+// ascending in a bucket, so position bounds are rank bounds). Element 0 of a
+// batch (the first entry of its first chunk, mapper_cpe.c:2113) is dropped
+// when it passes the filter; it is then the first survivor of its seed in that
+// batch.
+
+struct CandTabSmem {
+    uint32_t st[SWM_MAX_SEL];        // bucket start of each selected seed
+    uint32_t cn[SWM_MAX_SEL];        // bucket count
+    uint32_t sel[SWM_MAX_SEL];       // base | shift << 16 | rl << 20 | rh << 24
+    uint32_t cur[SWM_MAX_SEL];       // next table index of the seed's range
+    uint32_t end[SWM_MAX_SEL];       // end of the seed's range
+    uint32_t r1[SWM_MAX_SEL];        // bucket ranks fetched through this batch
+    uint32_t rst[SWM_MAX_SEL + 1];   // first element of each run of this batch
+    uint32_t ri[SWM_MAX_SEL];        // its first table index
+    uint32_t rb[SWM_MAX_SEL];        // its seed's base (position adjust)
+    uint32_t sc[CAND_SMEM_KEEP];     // kept positions of a batch, while they fit
+};
+
+// First index in [a, z) whose position is above p1 (positions ascending).
+__device__ __forceinline__ uint32_t upper_pos(const uint32_t *__restrict__ tp, uint32_t a, uint32_t z, uint32_t p1) {
+    while (a < z) {
+        const uint32_t mid = a + ((z - a) >> 1);
+        if (tp[mid] <= p1) a = mid + 1;
+        else z = mid;
+    }
+    return a;
+}
+
+__global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS)
+    k_cand_table(const uint32_t *__restrict__ pos, const uint16_t *__restrict__ lsd,
+                 const uint32_t *__restrict__ ctab_off, const uint32_t *__restrict__ ctab_pos, MapBufs B,
+                 uint64_t cap_chunks, uint64_t cap_elems, uint32_t klong) {
+    const uint32_t nitems = B.par->nitems;
+    __shared__ CandTabSmem sm_all[CAND_WARPS];
+    if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
+    CandTabSmem &S = sm_all[wib];
+    auto gscratch = [&]() { return B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS; };
+    for (uint32_t item = blockIdx.x * CAND_WARPS + wib; item < nitems; item += gridDim.x * CAND_WARPS) {
+        const uint32_t nb = B.it_nbat[item];
+        uint32_t total = 0;
+        if (nb) {
+            const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
+            const uint32_t ns = B.it_nsel[item], nref = B.it_nch[item];
+            const unsigned long long perm = B.it_perm[item];
+            const uint32_t sbase = B.it_choff[item] + item;
+            for (uint32_t i = lane; i < ns; i += 32) {
+                const uint32_t rs = sel_slot(perm, i), l = rs / SWM_SEED_STEP, sft = rs % SWM_SEED_STEP;
+                const uint2 sv = B.sel[sb + rs];
+                const uint32_t fb = B.sel_fl[sb + rs];
+                const uint32_t key = B.sel_key[sb + rs];
+                S.sel[i] = (l * klong + sft) | ((SWM_SEED_STEP - 1 - sft) << 16) | ((fb & 7u) << 20) | ((fb >> 3) << 24);
+                S.st[i] = sv.x;
+                S.cn[i] = sv.y;
+                uint32_t d0 = 0, d1 = 0;
+                if (sv.y) {
+                    d0 = ctab_off[key];
+                    d1 = ctab_off[(uint64_t)key + 1];
+                }
+                S.cur[i] = d0;
+                S.end[i] = d1;
+                S.r1[i] = sv.y < SWM_PER_FETCH ? sv.y : SWM_PER_FETCH; // batch 0 holds every seed's first chunk
+            }
+            __syncwarp();
+            // element 0 of batch 0: the first entry of the first seed (rank order) with positions
+            uint32_t s0 = 0xffffffffu;
+            for (uint32_t i0 = 0; i0 < ns && s0 == 0xffffffffu; i0 += 32) {
+                const uint32_t m = __ballot_sync(0xffffffffu, i0 + lane < ns && S.cn[i0 + lane] != 0);
+                if (m) s0 = i0 + __ffs(m) - 1;
+            }
+            uint32_t g0 = s0 != 0xffffffffu ? S.st[s0] : 0u;
+            for (uint32_t b = 0; b < nb; b++) {
+                uint32_t c0 = 0, c1 = 0, e0;
+                if (nref == 0) {
+                    e0 = B.it_eloff[item];
+                } else {
+                    c0 = B.bt_c0[sbase + b];
+                    c1 = B.bt_c1[sbase + b];
+                    e0 = B.bt_e0[sbase + b];
+                }
+                if (nb > 1) {
+                    // the batch's refill chunks raise their seed's fetched rank
+                    for (uint32_t q0 = c0; q0 < c1; q0 += 32) {
+                        const uint32_t c = q0 + lane;
+                        if (c < c1) {
+                            const uint32_t meta = B.ch_meta[c], si = meta >> 8;
+                            atomicMax(&S.r1[si], B.ch_g[c] - S.st[si] + (meta & 0xffu));
                         }
                     }
-                    for (uint32_t i0 = 0; i0 < kept; i0 += 32) {
-                        const uint32_t i = i0 + lane;
-                        const bool keep = i < kept && (i == 0 || buf[i - 1] != buf[i]);
-                        const uint32_t m = __ballot_sync(0xffffffffu, keep);
-                        if (keep) dst[u + __popc(m & lanemask_lt())] = buf[i];
-                        u += __popc(m);
+                    if (b > 0) { // element 0: the first entry of the batch's first chunk
+                        uint32_t gg = 0, ss = 0;
+                        if (lane == 0 && c0 < c1) {
+                            gg = B.ch_g[c0];
+                            ss = B.ch_meta[c0] >> 8;
+                        }
+                        g0 = __shfl_sync(0xffffffffu, gg, 0);
+                        s0 = c0 < c1 ? __shfl_sync(0xffffffffu, ss, 0) : 0xffffffffu;
                     }
+                    __syncwarp();
                 }
+                // each seed's survivors in this batch, as runs of the table
+                uint32_t nruns = 0, carry = 0;
+                for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
+                    const uint32_t i = i0 + lane;
+                    uint32_t a = 0, z = 0;
+                    if (i < ns) {
+                        a = S.cur[i];
+                        z = S.end[i];
+                        const uint32_t r1 = S.r1[i], cn = S.cn[i];
+                        if (nb > 1 && r1 < cn && a < z) z = upper_pos(ctab_pos, a, z, pos[S.st[i] + r1 - 1]);
+                        S.cur[i] = z;
+                        if (i == s0 && a < z) { // element 0 passes the filter: then it is this run's first entry
+                            const uint32_t sm = S.sel[i], shift = (sm >> 16) & 0xfu, rl = (sm >> 20) & 0xfu,
+                                           rh = (sm >> 24) & 0xfu;
+                            const uint32_t ls = lsd[g0];
+                            if (((((ls >> shift) ^ rl) | ((ls >> (6 + shift)) ^ rh)) & 7u) == 0) a++; // 2107-2113
+                        }
+                    }
+                    const uint32_t len = z - a;
+                    const uint32_t m = __ballot_sync(0xffffffffu, len != 0);
+                    const uint32_t inc = warp_scan_incl(len);
+                    if (len) {
+                        const uint32_t q = nruns + __popc(m & lanemask_lt());
+                        S.rst[q] = carry + inc - len;
+                        S.ri[q] = a;
+                        S.rb[q] = S.sel[i] & 0xffffu;
+                    }
+                    nruns += __popc(m);
+                    carry += __shfl_sync(0xffffffffu, inc, 31);
+                }
+                const uint32_t K = carry;
+                if (lane == 0) S.rst[nruns] = K;
+                __syncwarp();
+                // gather the survivors' positions, adjusted (adjust_ref_pos_rmdup, 1893-1917)
+                bool spilled = false;
+                uint32_t kept = 0, rdone = 0;
+                for (uint32_t eb = 0; eb < K; eb += 32) {
+                    const uint32_t el = eb + lane;
+                    // runs are non-empty: at most 32 start in [eb, eb + 32)
+                    const uint32_t cs = rdone + lane < nruns ? S.rst[rdone + lane] : eb + 32;
+                    const uint32_t bits = __reduce_or_sync(0xffffffffu, cs < eb + 32 ? 1u << (cs - eb) : 0u);
+                    const uint32_t q = rdone + __popc(bits & (0xffffffffu >> (31 - lane))) - 1; // run of el
+                    rdone += __popc(bits);
+                    const bool ok = el < K;
+                    uint32_t p = 0;
+                    if (ok) {
+                        const uint32_t raw = ctab_pos[S.ri[q] + (el - S.rst[q])];
+                        const uint32_t base = S.rb[q];
+                        p = raw > base ? raw - base : 0u;
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, ok);
+                    if (!spilled && kept + __popc(m) > CAND_SMEM_KEEP) {
+                        uint32_t *gs = gscratch();
+                        for (uint32_t i = lane; i < kept; i += 32) gs[i] = S.sc[i];
+                        spilled = true;
+                        __syncwarp();
+                    }
+                    if (ok) {
+                        const uint32_t at = kept + __popc(m & lanemask_lt());
+                        if (spilled) gscratch()[at] = p;
+                        else S.sc[at] = p;
+                    }
+                    kept += __popc(m);
+                }
+                __syncwarp();
+                const uint32_t u = batch_sort_unique(S.sc, gscratch(), spilled, kept, B.cand_ub + e0);
                 if (lane == 0) B.bt_cnt[sbase + b] = u;
                 total += u;
                 __syncwarp();
@@ -2584,7 +2786,7 @@ static int dmalloc(T **p, uint64_t count) {
 }
 
 static void free_bufs(MapBufs &B) {
-    void *ps[] = {B.par, B.it_w, B.sel, B.sel_fl, B.it_perm, B.unm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
+    void *ps[] = {B.par, B.it_w, B.sel, B.sel_fl, B.sel_key, B.it_perm, B.unm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand, B.plan_list,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
                   B.cc_item, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
@@ -2605,6 +2807,7 @@ static int alloc_items(swm_mapper *m) {
     rc |= dmalloc(&B.it_w, I * 32);
     rc |= dmalloc(&B.sel, I * SWM_MAX_SEL);
     rc |= dmalloc(&B.sel_fl, I * SWM_MAX_SEL);
+    rc |= dmalloc(&B.sel_key, I * SWM_MAX_SEL);
     rc |= dmalloc(&B.it_perm, I);
     rc |= dmalloc(&B.unm, I / 32 + 1);
     rc |= dmalloc(&B.it_nsel, I);
@@ -2677,6 +2880,9 @@ static int alloc_work(swm_mapper *m) {
 extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper **out) {
     if (!ix || !out || max_reads == 0 || max_reads > (1ull << 30)) return SWM_ERR_ARG;
     SWM_CUDA(cudaSetDevice(ix->device));
+    // the index's candidate table (k = 12), built once when the device has room
+    const int trc = swm_ctab_build(ix);
+    if (trc) return trc;
     swm_mapper *m = (swm_mapper *)calloc(1, sizeof(swm_mapper));
     if (!m) return SWM_ERR_OOM;
     m->ix = ix;
@@ -2790,8 +2996,12 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     m->launches += 3;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[2], st, cudaEventRecordExternal));
-    k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(ix->d_pos, ix->d_ls, B, m->cap_chunks, m->cap_elems,
-                                                     ix->k + SWM_SEED_STEP - 1);
+    if (ix->d_ctab_off && ix->k == K12)
+        k_cand_table<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(ix->d_pos, ix->d_ls, ix->d_ctab_off, ix->d_ctab_pos, B,
+                                                               m->cap_chunks, m->cap_elems, ix->k + SWM_SEED_STEP - 1);
+    else
+        k_cand<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(ix->d_pos, ix->d_ls, B, m->cap_chunks, m->cap_elems,
+                                                         ix->k + SWM_SEED_STEP - 1);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[3], st, cudaEventRecordExternal));
@@ -2859,7 +3069,7 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     P->nitems = 2 * nreads;
     P->errors = errors;
     P->pad = 0;
-    if (!m->gexec || m->gclass != gclass || m->ggen != m->gen) {
+    if (!m->gexec || m->gclass != gclass || m->ggen != m->gen || m->gctab != m->ix->ctab_gen) {
         drop_graph(m);
         cudaGraph_t g = nullptr;
         SWM_CUDA(cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal));
@@ -2880,6 +3090,7 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
         }
         m->gclass = gclass;
         m->ggen = m->gen;
+        m->gctab = m->ix->ctab_gen;
     }
     SWM_CUDA(cudaGraphLaunch(m->gexec, m->st));
     return SWM_OK;
@@ -2911,15 +3122,17 @@ static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *a
                       SWM_MAX_READ_LEN, SWM_MAX_ERRORS);
         return SWM_ERR_ARG;
     }
-    static const int kSums[] = {TOT_CHUNKS, TOT_ELEMS, TOT_CANDS, TOT_RECS, TOT_WORDS, TOT_BYTES};
-    static const char *kSumNames[] = {"refill chunks", "fetched positions", "candidates", "records", "record words",
-                                      "CIGAR bytes"};
-    for (int i = 0; i < 6; i++)
-        if (m->tot[kSums[i]] == SWM_SCAN_SATURATED) {
-            swm_set_error("the block's %s reach 2^32 - 1, past the 32-bit offsets of the work buffers: map it in "
-                          "smaller blocks (%u reads here)", kSumNames[i], nreads);
-            return SWM_ERR_OVERFLOW;
-        }
+    // A scan total that saturated means the block's work does not fit the
+    // 32-bit offsets at all. Each total is checked once the stage that feeds
+    // its scan is known to have run in full (a stage skips its work once an
+    // earlier buffer overflowed, leaving its per-item counts stale).
+    auto saturated = [&](int t, const char *what) {
+        if (m->tot[t] != SWM_SCAN_SATURATED) return false;
+        swm_set_error("the block's %s reach 2^32 - 1, past the 32-bit offsets of the work buffers: map it in "
+                      "smaller blocks (%u reads here)", what, nreads);
+        return true;
+    };
+    if (saturated(TOT_CHUNKS, "refill chunks") || saturated(TOT_ELEMS, "fetched positions")) return SWM_ERR_OVERFLOW;
     bool need = false;
     // totals from the item scans are exact even when a later buffer overflowed
     if (m->tot[TOT_CHUNKS] > m->cap_chunks) {
@@ -2930,7 +3143,8 @@ static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *a
         grow(&m->cap_elems, m->tot[TOT_ELEMS]);
         need = true;
     }
-    if (!need) {
+    if (!need) { // the candidate stage ran in full
+        if (saturated(TOT_CANDS, "candidates")) return SWM_ERR_OVERFLOW;
         if ((fl & OV_CANDS) || m->tot[TOT_CANDS] > m->cap_cands) {
             grow(&m->cap_cands, m->tot[TOT_CANDS]);
             need = true;
@@ -2939,12 +3153,17 @@ static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *a
             grow(&m->cap_arena, (uint64_t)m->tot[TOT_ARENA] + 1);
             need = true;
         }
-        if (!need && ((fl & OV_RECS) || m->tot[TOT_RECS] > m->cap_recs || m->tot[TOT_WORDS] > m->cap_words ||
-                      m->tot[TOT_BYTES] > m->cap_bytes)) {
-            grow(&m->cap_recs, m->tot[TOT_RECS]);
-            grow(&m->cap_words, m->tot[TOT_WORDS]);
-            grow(&m->cap_bytes, m->tot[TOT_BYTES]);
-            need = true;
+        if (!need) { // so did the records' count pass
+            if (saturated(TOT_RECS, "records") || saturated(TOT_WORDS, "record words") ||
+                saturated(TOT_BYTES, "CIGAR bytes"))
+                return SWM_ERR_OVERFLOW;
+            if ((fl & OV_RECS) || m->tot[TOT_RECS] > m->cap_recs || m->tot[TOT_WORDS] > m->cap_words ||
+                m->tot[TOT_BYTES] > m->cap_bytes) {
+                grow(&m->cap_recs, m->tot[TOT_RECS]);
+                grow(&m->cap_words, m->tot[TOT_WORDS]);
+                grow(&m->cap_bytes, m->tot[TOT_BYTES]);
+                need = true;
+            }
         }
     }
     if (need) {

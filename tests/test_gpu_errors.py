@@ -110,15 +110,17 @@ def test_small_packed_buffers_report_overflow(cuda_lib):
 
 
 def test_buffer_growth_retry_gives_oracle_records(cuda_lib):
-    """A mapper sized for 64 reads on a repeat-heavy genome: the first pass
-    outgrows its work buffers, the host grows them and re-runs the block
-    (swm_map_device / swm_map_wait), and the records equal the oracle's."""
-    g = genome(3_000_000, 11, "human", nrun_min=2000, nrun_max=20000, copies_per_family=300)
-    reads, lens, _, _ = synth.reads(g, 64, 150, 150, 0.03, seed=12)
+    """A mapper sized for 16 reads on a genome of close repeat copies (items
+    fetch thousands of positions): the first pass outgrows its work buffers,
+    the host grows them and re-runs the block, and the records equal the
+    oracle's."""
+    g = genome(3_000_000, 11, "human", copies_per_family=1000, div_min=0.005, div_max=0.03, repeat_frac=0.6,
+               rep_len_max=3000)
+    reads, lens, _, _ = synth.reads(g, 16, 150, 150, 0.03, seed=12)
     _, mix = oracle_index(g)
     ref = po.map_reads(mix, reads, lens, 7, nthreads=8)
     ix = cuda_lib.Index.build(g)
-    m = cuda_lib.Mapper(ix, max_reads=64)
+    m = cuda_lib.Mapper(ix, max_reads=16)
     out = m.map(reads, lens, 7)
     assert m.stats()["retries"] > 0
     d = first_diff(out.records(), ref.records())
@@ -139,7 +141,7 @@ def test_block_totals_past_32_bits_are_an_error(cuda_lib):
     n = 10_000_000
     g = np.frombuffer(b"ACGT" * (n // 4), np.uint8).copy()
     ix = cuda_lib.Index.build(g)
-    assert ix.download()["hash_count"].max() == n // 4
+    assert ix.download()["hash_count"].max() == (n - 12) // 4 + 1
     reads = np.tile(g[:250], (64, 1))
     lens = np.full(64, 250, np.uint32)
     m = cuda_lib.Mapper(ix, max_reads=64)

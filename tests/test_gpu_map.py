@@ -14,8 +14,12 @@ pytestmark = pytest.mark.gpu
 GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_outputs.json")))
 
 
-def _gpu(swm, g, reads, lens, e, eper=None, max_reads=None):
+def _gpu(swm, g, reads, lens, e, eper=None, max_reads=None, table=True):
+    """Map on the GPU; table=False drops the index's candidate table first, so
+    the candidate stage filters every fetched entry (the path for k != 12)."""
     ix = swm.Index.build(g)
+    if not table:
+        assert ix.candidate_table(False) == 0
     m = swm.Mapper(ix, max_reads=max_reads or max(1, reads.shape[0]))
     out = m.map(reads, lens, e, errors_per_read=eper)
     return out, m, ix
@@ -57,19 +61,22 @@ def test_gpu_plain_1mbp(cuda_lib):
     assert st["myers_steps"] >= 64 * st["candidates"] // 2
 
 
-def test_gpu_repeats_multibatch(cuda_lib):
-    """Heavy repeats: refills, several batches per strand, buffer growth."""
+@pytest.mark.parametrize("table", [True, False])
+def test_gpu_repeats_multibatch(cuda_lib, table):
+    """Heavy repeats: refills, several batches per strand, buffer growth; with
+    the candidate table and with entry-by-entry filtering."""
     g = genome(3_000_000, 7, "human", nrun_min=2000, nrun_max=20000, copies_per_family=300)
     reads, lens, _, _ = synth.reads(g, 3000, 150, 150, 0.03, seed=8)
     _, mix = oracle_index(g)
     for e in (7, 12):
         ref = po.map_reads(mix, reads, lens, e, nthreads=8)
-        out, m, _ = _gpu(cuda_lib, g, reads, lens, e)
+        out, m, _ = _gpu(cuda_lib, g, reads, lens, e, table=table)
         _check(out, ref.records(), ref.unmapped)
         assert m.stats()["batches"] == ref.stats["batches"]
 
 
-def test_gpu_single_batch_items_near_the_limit(cuda_lib):
+@pytest.mark.parametrize("table", [True, False])
+def test_gpu_single_batch_items_near_the_limit(cuda_lib, table):
     """Close repeat copies: many items with refills on both sides of the
     single-batch limit (2017 selected positions), which the planner handles
     without the seed heap below it and with the heap above it."""
@@ -79,7 +86,7 @@ def test_gpu_single_batch_items_near_the_limit(cuda_lib):
     _, mix = oracle_index(g)
     for e in (7, 12):
         ref = po.map_reads(mix, reads, lens, e, nthreads=8)
-        out, m, _ = _gpu(cuda_lib, g, reads, lens, e)
+        out, m, _ = _gpu(cuda_lib, g, reads, lens, e, table=table)
         _check(out, ref.records(), ref.unmapped)
         assert m.stats()["batches"] == ref.stats["batches"]
         assert m.stats()["candidates"] == ref.stats["candidates"]
@@ -126,11 +133,12 @@ def test_gpu_reads_at_genome_ends(cuda_lib):
     _check(out, ref.records(), ref.unmapped)
 
 
-def test_gpu_candidates_equal_oracle_trace(cuda_lib):
+@pytest.mark.parametrize("table", [True, False])
+def test_gpu_candidates_equal_oracle_trace(cuda_lib, table):
     g = genome(1_000_000, 14, "repeats100m", copies_per_family=20)
     reads, lens, _, _ = synth.reads(g, 64, 150, 150, 0.03, seed=15)
     _, mix = oracle_index(g)
-    out, m, _ = _gpu(cuda_lib, g, reads, lens, 7)
+    out, m, _ = _gpu(cuda_lib, g, reads, lens, 7, table=table)
     item, pos, err, loc = m.debug_candidates()
     for it in range(128):
         r, strand = it >> 1, it & 1
@@ -357,3 +365,20 @@ def test_gpu_requests_same_alone_and_in_the_mix(cuda_lib):
         n_mix = sum(len(got_mix.get(r, [])) for r in range(off, off + int(sz)))
         assert n_alone == n_mix
         off += int(sz)
+
+
+@pytest.mark.parametrize("k,e", [(10, 7), (11, 5), (13, 7), (14, 3)])
+def test_gpu_mapping_other_seed_lengths(cuda_lib, k, e):
+    """-s other than 12: the generic seed kernel (long seeds of k + 3 bases,
+    one warp per 32 items) and the rest of the pipeline, against the oracle."""
+    g = genome(2_000_000, 70 + k, "repeats100m", copies_per_family=40)
+    lmax = min(250, 17 * (k + 3) - 1)  # at most 16 long seeds of k + 3 bases (mapper_cpe.c:2515)
+    reads, lens, _, _ = synth.reads(g, 2000, 50, lmax, 0.03, seed=80 + k, stride=250)
+    reads[::9, 33] = ord("N")
+    hix, mix = oracle_index(g, k)
+    ref = po.map_reads(mix, reads, lens, e, nthreads=8)
+    ix = cuda_lib.Index.build(g, k=k)
+    m = cuda_lib.Mapper(ix, max_reads=reads.shape[0])
+    out = m.map(reads, lens, e)
+    _check(out, ref.records(), ref.unmapped)
+    assert m.stats()["candidates"] == ref.stats["candidates"]

@@ -29,7 +29,7 @@ def _cudart():
     raise RuntimeError("libcudart not found")
 
 
-@pytest.mark.parametrize("k,kind", [(12, "uniform"), (10, "repeats100m")])
+@pytest.mark.parametrize("k,kind", [(12, "uniform"), (10, "repeats100m"), (13, "uniform")])
 def test_hash_offset_noalloc_matches_index_build(cuda_lib, k, kind):
     rt = _cudart()
     L = cuda_lib.lib()
