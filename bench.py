@@ -324,11 +324,13 @@ def timed_cpu_sample(mix, reads, lens, e, threads, target_s, eper=None):
 STAGES = ["seed", "plan", "candidates", "compact", "verify", "traceback", "records"]
 
 
-def stage_bytes(stage, st, L, e):
+def stage_bytes(stage, st, L, e, table=False):
     """Algorithmic DRAM bytes of one stage over a whole step: what the stage must
-    read and write once (index entries: 2-byte flank codes read for every
-    fetched entry, 4-byte positions for the survivors; `chunks` counts refill
-    chunks)."""
+    read and write once. Candidates without the candidate table: the 2-byte
+    flank code of every fetched entry and the 4-byte position of each kept
+    one; with it: two 4-byte offsets per selected seed and the 4-byte position
+    of each kept entry (plus, in both, the seed records, refill chunks and the
+    candidates written)."""
     nl = L // 15
     items = st["items"]
     ns = min(e + 1, nl) * 4
@@ -336,9 +338,12 @@ def stage_bytes(stage, st, L, e):
         return items * (L + nl * 4 * 8 + 128 + ns * 12 + 16)
     if stage == "plan":   # items with refills only: seed table, refill chunks, batch records
         return st["chunks"] * (8 + 8) + st["batches"] * 12 + items * 8
-    if stage == "candidates":  # flank codes of every fetched entry, positions of the survivors, seed
-        # records (8 B + flank byte), refill chunks, candidates written
-        return st["fetched"] * 2 + st["candidates"] * 4 + items * ns * 9 + st["chunks"] * 8 + st["candidates"] * 4
+    if stage == "candidates":
+        kept = st.get("kept", st["candidates"])
+        common = items * ns * 9 + st["chunks"] * 8 + st["candidates"] * 4
+        if table:  # seed records with their table keys (13 B), table offsets, kept positions
+            return items * ns * (4 + 8) + kept * 4 + common
+        return st["fetched"] * 2 + kept * 4 + common
     if stage == "compact":
         return st["candidates"] * 12 + st["batches"] * 12
     if stage == "verify":
@@ -411,7 +416,7 @@ def run_gpu(args):
     rt.cudaStreamWaitEvent.argtypes = [C.c_void_p, C.c_void_p, C.c_uint]
     blocks = [(b0, min(block, nreads - b0)) for b0 in range(0, nreads, block)]
     COUNTERS = ("mapped_reads", "candidates", "cells", "passed", "fetched", "chunks", "batches", "items",
-                "locations", "records", "retries", "myers_steps")
+                "locations", "records", "retries", "myers_steps", "kept")
 
     def run_steps(nsteps, acc):
         """nsteps passes over the reads as one continuous stream of blocks."""
@@ -569,6 +574,7 @@ def run_gpu(args):
 
     # roofline of the dominant kernel
     peak, peak_kind, peaks = measured_peaks()
+    table = ix.candidate_table(None) > 0
     # index build against the bytes it must move once: the bases read (1 B
     # each), the bit planes + N mask written and read back (2 x 3 bits per
     # base), the count and offset tables written and read (2 x 2 x 4^k x 4 B)
@@ -586,21 +592,23 @@ def run_gpu(args):
     stage_rows = {}
     for sname in STAGES:
         t_ms = per_step["ms_" + sname]
-        byts = stage_bytes(sname, per_step, L, e)
+        byts = stage_bytes(sname, per_step, L, e, table)
         stage_rows[sname] = {"ms_per_step": round(t_ms, 3),
                              "gbs": round(byts / (t_ms / 1e3) / 1e9, 1) if t_ms > 0 else None,
                              "bytes_per_step": int(byts)}
     dom = max(STAGES, key=lambda s: per_step["ms_" + s])
-    kern = {"seed": "k_seed12" if w["k"] == 12 else "k_seed", "plan": "k_plan", "candidates": "k_cand", "compact": "k_compact",
+    kern = {"seed": "k_seed12" if w["k"] == 12 else "k_seed", "plan": "k_plan",
+            "candidates": "k_cand_table" if table else "k_cand", "compact": "k_compact",
             "verify": "k_verify", "traceback": "k_traceback", "records": "k_records"}[dom]
     launches_per_step = per_step["blocks"]
     avg_launch_s = per_step["ms_" + dom] / 1e3 / launches_per_step
-    alg_bytes_launch = stage_bytes(dom, per_step, L, e) / launches_per_step
+    alg_bytes_launch = stage_bytes(dom, per_step, L, e, table) / launches_per_step
     achieved = alg_bytes_launch / avg_launch_s / 1e9
     tr = profile_traffic(kern)
     traffic = None
     if tr:
-        unit_key = {"k_verify": "candidates", "k_cand": "fetched", "k_seed": "items", "k_seed12": "items",
+        unit_key = {"k_verify": "candidates", "k_cand": "fetched", "k_cand_table": "items", "k_seed": "items",
+                    "k_seed12": "items",
                     "k_plan": "chunks", "k_traceback": "passed"}.get(kern)
         for key, val in tr.items():
             if key.startswith("dram_bytes_per_") and unit_key and key.endswith(unit_key):
@@ -761,7 +769,7 @@ def serving_loads(swm, ix, g, args):
     sizes = np.minimum(np.exp(rng.uniform(0.0, math.log(cfg["size_max"]), nreq)).astype(np.int64), cfg["size_max"])
     sizes = np.maximum(sizes, 1)
     total = int(sizes.sum())
-    reads, lens, _, _ = synth_reads(g, total, cfg["len_min"], cfg["len_max"], cfg["error_rate"], cfg["read_seed"])
+    reads, lens = synth_reads(g, total, cfg["len_min"], cfg["len_max"], cfg["error_rate"], cfg["read_seed"])
     eper = np.minimum(np.ceil(cfg["e_frac"] * lens.astype(np.float64) - 1e-9), 15).astype(np.uint8)
     offs = np.concatenate([[0], np.cumsum(sizes)[:-1]])
     reqs = [(reads[o:o + n], lens[o:o + n], eper[o:o + n], int(eper[o:o + n].max())) for o, n in zip(offs, sizes)]
@@ -769,15 +777,16 @@ def serving_loads(swm, ix, g, args):
                      max_queued_reads=total + cfg["block_reads"])
 
     def run(arrivals):
-        lat = np.zeros(nreq)
+        nq = len(arrivals)
+        lat = np.zeros(nq)
         done_t = [0.0]
         id2q = {}
         lock = threading.Lock()
 
         def collector():
             got = 0
-            while got < nreq:
-                res = srv.poll(timeout_ms=120_000)
+            while got < nq:
+                res = srv.poll(timeout_ms=120_000, records=False)
                 if res is None:
                     raise RuntimeError("serving: no request finished within two minutes")
                 t = time.perf_counter()
@@ -794,7 +803,7 @@ def serving_loads(swm, ix, g, args):
         th = threading.Thread(target=collector)
         t_start = time.perf_counter()
         th.start()
-        for q in range(nreq):
+        for q in range(nq):
             while True:
                 wait = t_start + arrivals[q] - time.perf_counter()
                 if wait <= 0:

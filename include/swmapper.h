@@ -106,8 +106,9 @@ int swm_hash_offset_noalloc(const uint32_t *d_hash_count, uint32_t *d_hash_offse
  * instead of every entry of the fetched buckets; results are identical
  * either way. enable = 0 drops the table and keeps it from being built again
  * (mappers fall back to filtering every entry; call it with no block in
- * flight), enable = 1 builds it now if it is missing and fits. *bytes (may be
- * NULL) gets the table's device bytes, 0 when there is none. */
+ * flight), enable = 1 builds it now if it is missing and fits, enable < 0
+ * only reports. *bytes (may be NULL) gets the table's device bytes, 0 when
+ * there is none. */
 int swm_index_candidate_table(swm_index *ix, int enable, uint64_t *bytes);
 
 /* Copy the index arrays to host memory in file layout (any pointer may be
@@ -163,6 +164,8 @@ typedef struct {
     uint64_t d2h_bytes;         /* device -> host bytes of the block's results   */
     uint64_t myers_steps;       /* read bases run through the Myers recurrence,
                                    summed over candidates and both passes       */
+    uint64_t kept;              /* positions the flank filter kept, before each
+                                   batch's merge and dedup                       */
 } swm_map_stats;
 
 /* Create a mapping context on the index's device with its own CUDA stream and

@@ -47,7 +47,7 @@ class PackedResult(C.Structure):
 
 
 STAT_FIELDS = ["reads", "items", "chunks", "batches", "fetched", "candidates", "cells", "passed", "records",
-               "locations", "mapped_reads", "retries", "h2d_bytes", "d2h_bytes", "myers_steps"]
+               "locations", "mapped_reads", "retries", "h2d_bytes", "d2h_bytes", "myers_steps", "kept"]
 
 
 class MapStats(C.Structure):
@@ -194,12 +194,13 @@ class Index:
                                                     "base_2bits", "base_3bits"))), "swm_index_download")
         return out
 
-    def candidate_table(self, enable: bool) -> int:
-        """Build (True) or drop (False) the device-only candidate table
-        (swm_index_candidate_table); returns its device bytes (0: none)."""
+    def candidate_table(self, enable: bool | None = None) -> int:
+        """Build (True) or drop (False) the device-only candidate table, or
+        only report it (None) (swm_index_candidate_table); returns its device
+        bytes (0: none)."""
         nbytes = C.c_uint64()
-        _check(lib().swm_index_candidate_table(self._h, 1 if enable else 0, C.byref(nbytes)),
-               "swm_index_candidate_table")
+        mode = -1 if enable is None else (1 if enable else 0)
+        _check(lib().swm_index_candidate_table(self._h, mode, C.byref(nbytes)), "swm_index_candidate_table")
         return int(nbytes.value)
 
     def close(self) -> None:
@@ -401,9 +402,10 @@ class Server:
         _check(lib().swm_serve_submit(self._h, C.byref(b), C.byref(rid)), "swm_serve_submit")
         return int(rid.value)
 
-    def poll(self, timeout_ms: int = -1, out: "PackedBuffers | None" = None):
-        """(id, records or None, info dict) of the next finished request, or
-        None when none finished within timeout_ms."""
+    def poll(self, timeout_ms: int = -1, out: "PackedBuffers | None" = None, records: bool = True):
+        """(id, records, info dict) of the next finished request, or None when
+        none finished within timeout_ms; records=False leaves the records in
+        the buffers (self.last) instead of decoding them."""
         rid = C.c_uint64()
         info = RequestInfo()
         if out is None:
@@ -420,8 +422,9 @@ class Server:
                 self._buf = out
                 continue
             _check(rc, "swm_serve_poll")
-            return int(rid.value), out.records(), {"reads": int(info.reads), "block_reads": int(info.block_reads),
-                                                   "latency_ms": float(info.latency_ms)}
+            self.last = out
+            return int(rid.value), out.records() if records else None, {
+                "reads": int(info.reads), "block_reads": int(info.block_reads), "latency_ms": float(info.latency_ms)}
 
     def stats(self) -> dict:
         s = ServeCounters()

@@ -1019,6 +1019,11 @@ int swm_ctab_build(swm_index *ix) {
 
 extern "C" int swm_index_candidate_table(swm_index *ix, int enable, uint64_t *bytes) {
     if (!ix) return SWM_ERR_ARG;
+    if (enable < 0) { // query only
+        std::lock_guard<std::mutex> lk(g_ctab_mu);
+        if (bytes) *bytes = ix->d_ctab_off ? ctab_bytes(ix) : 0;
+        return SWM_OK;
+    }
     if (enable) {
         {
             std::lock_guard<std::mutex> lk(g_ctab_mu);

@@ -45,6 +45,7 @@ enum {
     ST_LOCS,
     ST_MAPPED,
     ST_STEPS, // Myers steps (read bases) run by k_verify
+    ST_KEPT,  // positions the flank filter kept, before each batch's merge
     ST_N
 };
 // device totals (u32), written by the scans
@@ -1555,6 +1556,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
     CandSmem &S = sm_all[wib];
     // a warp's survivors past CAND_SMEM_KEEP go to its slice of global scratch
     auto gscratch = [&]() { return B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS; };
+    unsigned long long kept_all = 0; // this warp's kept positions, added to the block's count once
     for (uint32_t item = blockIdx.x * CAND_WARPS + wib; item < nitems; item += gridDim.x * CAND_WARPS) {
         const uint32_t nb = B.it_nbat[item];
         uint32_t total = 0;
@@ -1664,11 +1666,13 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
                 const uint32_t u = batch_sort_unique(S.sc, gscratch(), spilled, kept, B.cand_ub + e0);
                 if (lane == 0) B.bt_cnt[sbase + b] = u;
                 total += u;
+                kept_all += kept;
                 __syncwarp();
             }
         }
         if (lane == 0) B.it_ncand[item] = total;
     }
+    if (lane == 0 && kept_all) atomicAdd(&B.stat[ST_KEPT], kept_all);
 }
 
 // ======================================================================
@@ -1720,6 +1724,7 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS)
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     CandTabSmem &S = sm_all[wib];
     auto gscratch = [&]() { return B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS; };
+    unsigned long long kept_all = 0; // this warp's kept positions, added to the block's count once
     for (uint32_t item = blockIdx.x * CAND_WARPS + wib; item < nitems; item += gridDim.x * CAND_WARPS) {
         const uint32_t nb = B.it_nbat[item];
         uint32_t total = 0;
@@ -1850,11 +1855,13 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS)
                 const uint32_t u = batch_sort_unique(S.sc, gscratch(), spilled, kept, B.cand_ub + e0);
                 if (lane == 0) B.bt_cnt[sbase + b] = u;
                 total += u;
+                kept_all += kept;
                 __syncwarp();
             }
         }
         if (lane == 0) B.it_ncand[item] = total;
     }
+    if (lane == 0 && kept_all) atomicAdd(&B.stat[ST_KEPT], kept_all);
 }
 
 // Dense candidate list: item by item, batch by batch, in verification order.
@@ -3191,6 +3198,7 @@ static int finish_block(swm_mapper *m, uint32_t nreads, uint64_t retries, int *a
     S.locations = stat[ST_LOCS];
     S.mapped_reads = stat[ST_MAPPED];
     S.myers_steps = stat[ST_STEPS];
+    S.kept = stat[ST_KEPT];
     S.retries = retries;
     S.h2d_bytes = m->h2d_pending;
     m->h2d_pending = 0;
