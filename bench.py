@@ -357,6 +357,19 @@ def stage_bytes(stage, st, L, e, table=False):
     return 0
 
 
+def block_plan(nreads, block, tuned):
+    """(first read, reads, verification head bases) of every block: blocks of
+    `block` reads with a 64-base head, or, with per-bucket tuning, each
+    length bucket's reads in blocks of its own size with its own head."""
+    if not tuned or not tuned.get("buckets"):
+        return [(b0, min(block, nreads - b0), 64) for b0 in range(0, nreads, block)]
+    out = []
+    for bk in tuned["buckets"]:
+        lo, n, bs = bk["first"], bk["reads"], min(bk["block"], bk["reads"])
+        out += [(b0, min(bs, lo + n - b0), bk["head"]) for b0 in range(lo, lo + n, bs)]
+    return out
+
+
 def run_gpu(args):
     import swmapper_gb300 as swm
     ws, rank, local = dist_env()
@@ -384,6 +397,8 @@ def run_gpu(args):
     ix = swm.Index.build_device(d_g.value, g.size, k=w["k"], device=local)
     index_build_s = time.perf_counter() - t0
     rt.cudaFree(d_g)
+    if not args.table:
+        ix.candidate_table(False)
     nreads, stride = reads.shape
     block = min(args.block, nreads)
     # inputs resident in HBM
@@ -407,6 +422,13 @@ def run_gpu(args):
         tuned = swtune.tune(ix, d_reads.value + o_t * stride, d_lens.value + o_t * 4, stride, n_t, E,
                             d_e.value + o_t if eper is not None else None)
         block, args.mappers = min(tuned["block"], nreads), tuned["mappers"]
+        # per 32-bp length bucket (reads grouped by bucket): verification head
+        # length and reads per block
+        if bucketed or int(lens.min()) == int(lens.max()):
+            tuned["buckets"] = swtune.tune_buckets(ix, d_reads.value, d_lens.value, stride, lens, E,
+                                                   d_e.value if eper is not None else None, args.mappers)
+    blocks = block_plan(nreads, block, tuned)
+    block = max(nb for _, nb, _ in blocks)
     mappers = [swm.Mapper(ix, max_reads=block) for _ in range(args.mappers)]
     m = mappers[0]
     streams = [C.c_void_p(mm.stream()) for mm in mappers]
@@ -414,7 +436,6 @@ def run_gpu(args):
     for ev in (ev0, ev1, evq):
         rt.cudaEventCreate(C.byref(ev))
     rt.cudaStreamWaitEvent.argtypes = [C.c_void_p, C.c_void_p, C.c_uint]
-    blocks = [(b0, min(block, nreads - b0)) for b0 in range(0, nreads, block)]
     COUNTERS = ("mapped_reads", "candidates", "cells", "passed", "fetched", "chunks", "batches", "items",
                 "locations", "records", "retries", "myers_steps", "kept")
 
@@ -433,10 +454,11 @@ def run_gpu(args):
                 acc["blocks"] = acc.get("blocks", 0) + 1
 
         for i in range(nsteps * len(blocks)):
-            b0, nb = blocks[i % len(blocks)]
+            b0, nb, hd = blocks[i % len(blocks)]
             if len(pend) == len(mappers):
                 drain()
             mm = mappers[i % len(mappers)]
+            mm.set_head(hd)
             mm.submit_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, nb, E,
                              d_e.value + b0 if eper is not None else None)
             pend.append(mm)
@@ -489,7 +511,8 @@ def run_gpu(args):
     value = tot_mapped / tot_elapsed
     # kernel times in isolation (one mapper, one block at a time) for the
     # stage breakdown and the roofline: one untimed pass over the reads
-    for b0, nb in blocks:
+    for b0, nb, hd in blocks:
+        m.set_head(hd)
         m.map_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, nb, E,
                      d_e.value + b0 if eper is not None else None)
         for sname in STAGES:
@@ -531,7 +554,6 @@ def run_gpu(args):
     pinned = [reads, lens] + [a for bf in bufs for a in (bf.words, bf.cigar, bf.rlen)]
     for a in pinned:
         rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0)
-    blocks = [(b0, min(block, nreads - b0)) for b0 in range(0, nreads, block)]
 
     def e2e_run(nsteps, acc2):
         """nsteps passes over the reads as one continuous stream of blocks:
@@ -547,9 +569,10 @@ def run_gpu(args):
             acc2["d2h"] += st["d2h_bytes"]
 
         for i in range(nsteps * len(blocks)):
-            b0, nb = blocks[i % len(blocks)]
+            b0, nb, hd = blocks[i % len(blocks)]
             if len(pend) == ne:
                 drain()
+            mappers[i % ne].set_head(hd)
             mappers[i % ne].submit(reads[b0:b0 + nb], lens[b0:b0 + nb], E,
                                   None if eper is None else eper[b0:b0 + nb])
             pend.append((i, mappers[i % ne]))
@@ -889,10 +912,17 @@ def run_reference(args):
     with tempfile.TemporaryDirectory() as td:
         if po.have_ref() and os.path.exists(exe):
             fa = os.path.join(td, "g.fa")
+            # records of at most 100 Mbp: serial_index reads each record with
+            # kseq_read, whose int return value turns negative past 2^31 - 1
+            # bases (kseq.h), and the builder then stops before indexing
+            # anything. It indexes the concatenation of the records as one
+            # stream, so the files equal those of a single record.
+            rec = 100_000_000
             with open(fa, "wb") as f:
-                f.write(b">chrS synthetic\n")
-                for i in range(0, g.size, 100_000):
-                    f.write(g[i:i + 100_000].tobytes() + b"\n")
+                for r0 in range(0, g.size, rec):
+                    f.write(b">chr%d synthetic\n" % (r0 // rec + 1))
+                    for i in range(r0, min(g.size, r0 + rec), 100_000):
+                        f.write(g[i:min(i + 100_000, r0 + rec)].tobytes() + b"\n")
             prefix = os.path.join(td, "ix")
             subprocess.run([exe, "-i" + fa, "-p" + prefix, f"-s{w['k']}"], check=True, capture_output=True)
             arrays = {}
@@ -959,6 +989,8 @@ def main():
                     help="reads of the timed workload compared with the reference's own mapper after the timing")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--requests", type=int, default=None, help="requests of the serving workload")
+    ap.add_argument("--table", type=int, default=1,
+                    help="keep the index's candidate table (1) or drop it before the mappers are made (0)")
     ap.add_argument("--serving", type=int, default=1,
                     help="with the human-scale workload, also run the serving loads on its index (1) or not (0)")
     ap.add_argument("--plain", type=int, default=1, help="also time the plain per-batch launch (1) or not (0)")

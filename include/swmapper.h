@@ -225,6 +225,18 @@ int swm_mapper_stats(const swm_mapper *m, swm_map_stats *s);
  * unknown name. */
 int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float *ms);
 
+/* Settings of a mapper that change its speed, never its results (no
+ * reference counterpart; the autotuner sets them per read-length bucket). */
+typedef struct {
+    uint32_t verify_head_bases; /* bases of every candidate the first verification
+                                   pass runs before the exact stop test: 32 or 64
+                                   (default 64)                                 */
+} swm_tuning;
+
+/* Apply *set (may be NULL) and report the current settings in *get (may be
+ * NULL); SWM_ERR_STATE while a block is in flight. */
+int swm_mapper_tuning(swm_mapper *m, const swm_tuning *set, swm_tuning *get);
+
 /* Kernel launches queued for the last block. */
 uint64_t swm_mapper_launches(const swm_mapper *m);
 

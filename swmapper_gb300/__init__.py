@@ -113,6 +113,7 @@ def lib():
         L.swm_map_wait_packed.argtypes = [vp, C.POINTER(PackedResult)]
         L.swm_mapper_stats.argtypes = [vp, C.POINTER(MapStats)]
         L.swm_mapper_stage_ms.argtypes = [vp, C.c_char_p, C.POINTER(C.c_float)]
+        L.swm_mapper_tuning.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.swm_mapper_launches.argtypes = [vp]
         L.swm_mapper_launches.restype = u64
         L.swm_mapper_stream.argtypes = [vp]
@@ -311,6 +312,16 @@ class Mapper:
         v = C.c_float()
         _check(lib().swm_mapper_stage_ms(self._h, stage.encode(), C.byref(v)), "swm_mapper_stage_ms")
         return float(v.value)
+
+    def set_head(self, bases: int) -> None:
+        """Bases of the first verification pass (32 or 64; swm_mapper_tuning)."""
+        v = C.c_uint32(bases)
+        _check(lib().swm_mapper_tuning(self._h, C.byref(v), None), "swm_mapper_tuning")
+
+    def head(self) -> int:
+        v = C.c_uint32()
+        _check(lib().swm_mapper_tuning(self._h, None, C.byref(v)), "swm_mapper_tuning")
+        return int(v.value)
 
     def launches(self) -> int:
         return int(lib().swm_mapper_launches(self._h))

@@ -89,6 +89,10 @@ struct BlockParams {
     const uint8_t *e;      // per-read thresholds, or null
     uint64_t stride;
     uint32_t nreads, nitems, errors, pad;
+    // multipliers of the integer multiply-adds in the Myers step: 1, 2 and
+    // 2^31, read from memory so that they stay multiplies (the FMA pipe)
+    // instead of being folded into shifts and adds (the ALU pipe)
+    uint32_t one, two, half, pad2;
 };
 
 struct MapBufs {
@@ -181,10 +185,12 @@ struct swm_mapper {
     // the block's launch sequence, captured once per buffer set and read
     // length class; the block's inputs reach it through B.par
     BlockParams *h_par;        // pinned
-    cudaGraphExec_t gexec;
-    int gclass;                // k_seed variant the graph was captured with
-    uint32_t gen, ggen;        // buffer generation now / when the graph was captured
-    uint32_t gctab;            // candidate-table generation of the index when captured
+    // one captured graph per (seed-kernel class, verification head length),
+    // with the buffer and candidate-table generations it was captured with
+    cudaGraphExec_t gx[3][2];
+    uint32_t gx_gen[3][2], gx_tab[3][2];
+    uint32_t gen;              // buffer generation now
+    uint32_t head_blocks;      // 32-base blocks of the verification head (1 or 2)
 };
 
 // ======================================================================
@@ -1962,12 +1968,41 @@ __device__ __forceinline__ uint32_t window_start(uint32_t base_pos, uint32_t L, 
 // reference keeps in peq[read[i]]. myers_blocks runs the 32-base blocks
 // b0 .. b1 - 1 (the last one may be partial) from the state (VP, VN, ones =
 // steps whose D0 bit 0 was set); cp gets (VP, VN) at the start of each.
+// Integer multiply-adds issue on the FMA pipe while the logic ops of the
+// recurrence keep the ALU pipe busy.
+__device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+__device__ __forceinline__ uint32_t mulhi_u32(uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("mul.hi.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+__device__ __forceinline__ uint32_t mulhi_s32(uint32_t a, uint32_t b) {
+    int32_t d;
+    asm("mul.hi.s32 %0, %1, %2;" : "=r"(d) : "r"((int32_t)a), "r"((int32_t)b));
+    return (uint32_t)d;
+}
+
+// The multipliers the step takes from memory: 1, 2 and 2^31.
+struct MadK {
+    uint32_t one, two, half;
+};
+
+// Banded Myers over 32-base blocks b0 .. b1 - 1 (banded_myers_simd,
+// mapper_cpe.c:519-660, 32-bit lanes). Per step the read base's bits are
+// broadcast to all-ones / all-zeros as the sign of a bit-reversed read word
+// (mul.hi.s32 by 1) that doubles each step (mad by 2); the carry add
+// VP + (X & VP) is a mad by 1 and D0 >> 1 a mul.hi by 2^31 -- the same
+// integers as the shifts and adds they replace, on the FMA pipe.
 __device__ __forceinline__ void myers_blocks(const uint32_t *WL, const uint32_t *WH, const uint32_t *RW, uint32_t L,
                                              uint32_t MASK, uint32_t b0, uint32_t b1, uint32_t &vp, uint32_t &vn,
-                                             uint32_t &ones, uint32_t *cp) {
+                                             uint32_t &ones, uint32_t *cp, const MadK &K) {
     for (uint32_t b = b0; b < b1; b++) {
         const uint32_t wl0 = WL[b], wl1 = WL[b + 1], wh0 = WH[b], wh1 = WH[b + 1];
-        const uint32_t rlw = RW[2 * b], rhw = RW[2 * b + 1];
+        uint32_t rrl = __brev(RW[2 * b]), rrh = __brev(RW[2 * b + 1]); // read base t at bit 31 - t
         const uint32_t steps = min(32u, L - 32 * b);
         cp[4 * b] = vp; // (VP, VN) before bases 32 b and 32 b + 16, for the traceback
         cp[4 * b + 1] = vn;
@@ -1980,14 +2015,15 @@ __device__ __forceinline__ void myers_blocks(const uint32_t *WL, const uint32_t 
                     cp[4 * b + 3] = vn;
                 }
                 const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
-                const uint32_t mL = (uint32_t)((int32_t)(rlw << (31 - t)) >> 31);
-                const uint32_t mH = (uint32_t)((int32_t)(rhw << (31 - t)) >> 31);
+                const uint32_t mL = mulhi_s32(rrl, K.one), mH = mulhi_s32(rrh, K.one);
+                rrl = mad_u32(rrl, K.two, 0u);
+                rrh = mad_u32(rrh, K.two, 0u);
                 const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
                 uint32_t x = eq | vn;
-                const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;
+                const uint32_t d0 = (mad_u32(x & vp, K.one, vp) ^ vp) | x;
                 const uint32_t hn = vp & d0;
                 const uint32_t hp = vn | ~(vp | d0);
-                x = d0 >> 1;
+                x = mulhi_u32(d0, K.half);
                 vn = x & hp;
                 vp = hn | ~(x | hp);
                 acc = __funnelshift_r(acc, d0, 1);
@@ -1999,13 +2035,15 @@ __device__ __forceinline__ void myers_blocks(const uint32_t *WL, const uint32_t 
                     cp[4 * b + 3] = vn;
                 }
                 const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
-                const uint32_t mL = 0u - ((rlw >> t) & 1u), mH = 0u - ((rhw >> t) & 1u);
+                const uint32_t mL = mulhi_s32(rrl, K.one), mH = mulhi_s32(rrh, K.one);
+                rrl = mad_u32(rrl, K.two, 0u);
+                rrh = mad_u32(rrh, K.two, 0u);
                 const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
                 uint32_t x = eq | vn;
-                const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;
+                const uint32_t d0 = (mad_u32(x & vp, K.one, vp) ^ vp) | x;
                 const uint32_t hn = vp & d0;
                 const uint32_t hp = vn | ~(vp | d0);
-                x = d0 >> 1;
+                x = mulhi_u32(d0, K.half);
                 vn = x & hp;
                 vp = hn | ~(x | hp);
                 acc = __funnelshift_r(acc, d0, 1);
@@ -2102,8 +2140,8 @@ __device__ __forceinline__ void load_window(const uint32_t *__restrict__ b2, uin
 
 #define TB_TEXT_MAX 2304 // >= 4 bytes x every route entry a bounded walk can make
 
-// Verification in two passes. The head runs the first VERIFY_HEAD_BLOCKS
-// 32-base blocks of every candidate, the tail finishes the ones that can
+// Verification in two passes. The head runs the first HB (1 or 2) 32-base
+// blocks of every candidate, the tail finishes the ones that can
 // still end at or below e, queued with their state.
 //
 // The band of step i holds the edit-distance cells of read prefix i against
@@ -2118,8 +2156,6 @@ __device__ __forceinline__ void load_window(const uint32_t *__restrict__ b2, uin
 // already above e after the head, the full run would return
 // (SWM_MAXERROR, -1), and the head writes that result at once. On the
 // human-scale genome most candidates stop there.
-#define VERIFY_HEAD_BLOCKS 2
-
 // Minimum over cells 0 .. lh of a band: site error err, vertical steps VP /
 // VN (the reference's final scan, taking the minimum instead of the first
 // hit). A fixed-length loop: early exits measured slower.
@@ -2132,13 +2168,16 @@ __device__ __forceinline__ int band_scan_min(int err, uint32_t vp, uint32_t vn, 
     return m;
 }
 
-template <bool HEAD>
+// HB: 32-base blocks the head pass runs (1 or 2; the autotuner picks it per
+// read-length bucket). Any HB gives the same results: the stop is exact.
+template <bool HEAD, int HB>
 __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *__restrict__ b2,
                                                 uint64_t b2_words, uint64_t ref_length, MapBufs B,
                                                 uint64_t cap_chunks, uint64_t cap_elems, uint64_t cap_cands,
                                                 uint64_t cap_arena) {
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
     const uint32_t *__restrict__ lens = B.par->lens;
+    const MadK K{B.par->one, B.par->two, B.par->half};
     uint64_t n;
     if (HEAD) {
         const uint64_t nc_all = B.tot[TOT_CANDS];
@@ -2160,17 +2199,19 @@ __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *_
             c = j;
         } else {
             const uint2 x = B.vt_x[j];
-            const uint4 st = B.vt_st[j], st2 = B.vt_cp[j];
+            const uint4 st = B.vt_st[j], st2 = HB >= 2 ? B.vt_cp[j] : make_uint4(0u, 0u, 0u, 0u);
             c = x.x;
             ones = x.y;
             vp = st.x;
             vn = st.y;
             cp[2] = st.z;
             cp[3] = st.w;
-            cp[4] = st2.x;
-            cp[5] = st2.y;
-            cp[6] = st2.z;
-            cp[7] = st2.w;
+            if (HB >= 2) {
+                cp[4] = st2.x;
+                cp[5] = st2.y;
+                cp[6] = st2.z;
+                cp[7] = st2.w;
+            }
         }
         const uint32_t item = B.cc_item[c], p = B.cc_pos[c];
         const uint32_t L = lens[item >> 1], e = B.it_e[item];
@@ -2183,20 +2224,20 @@ __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *_
             continue;
         }
         const uint32_t nblk = (L + 31) >> 5;
-        const bool head_only = HEAD && nblk > VERIFY_HEAD_BLOCKS;
+        const bool head_only = HEAD && nblk > HB;
         uint32_t WL[SWM_WIN_WORDS], WH[SWM_WIN_WORDS];
-        // the head reads window words 0 .. VERIFY_HEAD_BLOCKS only
-        load_window(b2, b2_words, ws, head_only ? 32 * VERIFY_HEAD_BLOCKS - 2 * e : L, e, WL, WH);
+        // the head reads window words 0 .. HB only
+        load_window(b2, b2_words, ws, head_only ? 32 * HB - 2 * e : L, e, WL, WH);
         const uint32_t *RW = B.it_w + (uint64_t)item * 32;
         uint32_t rw[16];
 #pragma unroll
-        for (int i = 0; i < 16; i++) rw[i] = (HEAD && i >= 2 * VERIFY_HEAD_BLOCKS) ? 0u : RW[i];
+        for (int i = 0; i < 16; i++) rw[i] = (HEAD && i >= 2 * HB) ? 0u : RW[i];
         const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
-        const uint32_t b0 = HEAD ? 0u : VERIFY_HEAD_BLOCKS, b1 = HEAD ? min(nblk, (uint32_t)VERIFY_HEAD_BLOCKS) : nblk;
+        const uint32_t b0 = HEAD ? 0u : HB, b1 = HEAD ? min(nblk, (uint32_t)HB) : nblk;
         steps += min(L, 32 * b1) - 32 * b0;
-        myers_blocks(WL, WH, rw, L, MASK, b0, b1, vp, vn, ones, cp);
+        myers_blocks(WL, WH, rw, L, MASK, b0, b1, vp, vn, ones, cp, K);
         if (head_only) {
-            if (band_scan_min(32 * VERIFY_HEAD_BLOCKS - (int)ones, vp, vn, (int)rl - (int)L) > (int)e) {
+            if (band_scan_min(32 * HB - (int)ones, vp, vn, (int)rl - (int)L) > (int)e) {
                 cells += (unsigned long long)L * (2 * e + 1);
                 B.vr_err[c] = SWM_MAXERROR;
                 B.vr_mloc[c] = -1;
@@ -2205,7 +2246,7 @@ __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *_
                 const uint32_t at = atomicAdd(&B.tot[TOT_VT], 1u);
                 B.vt_x[at] = make_uint2((uint32_t)c, ones);
                 B.vt_st[at] = make_uint4(vp, vn, cp[2], cp[3]);
-                B.vt_cp[at] = make_uint4(cp[4], cp[5], cp[6], cp[7]);
+                if (HB >= 2) B.vt_cp[at] = make_uint4(cp[4], cp[5], cp[6], cp[7]);
             }
             continue;
         }
@@ -2904,6 +2945,7 @@ extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper *
     m->cap_bytes = cap_clamp(m->cap_items * 32 + 4096);
     m->cap_arena = ARENA_CAP_DEFAULT;
     m->stride_cap = 0;
+    m->head_blocks = 2;
     int rc = SWM_OK;
     if (cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking) != cudaSuccess) rc = SWM_ERR_CUDA;
     for (int i = 0; i < 9 && rc == SWM_OK; i++)
@@ -2931,7 +2973,9 @@ extern "C" void swm_mapper_free(swm_mapper *m) {
     if (!m) return;
     cudaSetDevice(m->device);
     if (m->st) cudaStreamSynchronize(m->st);
-    if (m->gexec) cudaGraphExecDestroy(m->gexec);
+    for (int a = 0; a < 3; a++)
+        for (int h = 0; h < 2; h++)
+            if (m->gx[a][h]) cudaGraphExecDestroy(m->gx[a][h]);
     free_bufs(m->b);
     cudaFree(m->d_reads);
     cudaFree(m->d_lens);
@@ -3019,12 +3063,15 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[4], st, cudaEventRecordExternal));
-    k_verify<true><<<grid_cap(m->cap_cands, 128, 16), 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
-                                                                     ix->ref_length, B, m->cap_chunks, m->cap_elems,
-                                                                     m->cap_cands, m->cap_arena);
-    k_verify<false><<<grid_cap(m->cap_cands, 128, 16), 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS,
-                                                                      ix->ref_length, B, m->cap_chunks, m->cap_elems,
-                                                                      m->cap_cands, m->cap_arena);
+    {
+        auto head = m->head_blocks == 1 ? k_verify<true, 1> : k_verify<true, 2>;
+        auto tail = m->head_blocks == 1 ? k_verify<false, 1> : k_verify<false, 2>;
+        const unsigned vg = grid_cap(m->cap_cands, 128, 16);
+        head<<<vg, 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks,
+                                 m->cap_elems, m->cap_cands, m->cap_arena);
+        tail<<<vg, 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks,
+                                 m->cap_elems, m->cap_cands, m->cap_arena);
+    }
     m->launches += 2;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[5], st, cudaEventRecordExternal));
@@ -3056,9 +3103,9 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     return SWM_OK;
 }
 
-static void drop_graph(swm_mapper *m) {
-    if (m->gexec) cudaGraphExecDestroy(m->gexec);
-    m->gexec = nullptr;
+static void drop_graph(swm_mapper *m, int gclass, int h) {
+    if (m->gx[gclass][h]) cudaGraphExecDestroy(m->gx[gclass][h]);
+    m->gx[gclass][h] = nullptr;
 }
 
 // Queue one block on m->st: its inputs into the pinned parameter block, then
@@ -3076,8 +3123,13 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     P->nitems = 2 * nreads;
     P->errors = errors;
     P->pad = 0;
-    if (!m->gexec || m->gclass != gclass || m->ggen != m->gen || m->gctab != m->ix->ctab_gen) {
-        drop_graph(m);
+    P->one = 1;
+    P->two = 2;
+    P->half = 0x80000000u;
+    P->pad2 = 0;
+    const int h = m->head_blocks == 1 ? 0 : 1;
+    if (!m->gx[gclass][h] || m->gx_gen[gclass][h] != m->gen || m->gx_tab[gclass][h] != m->ix->ctab_gen) {
+        drop_graph(m, gclass, h);
         cudaGraph_t g = nullptr;
         SWM_CUDA(cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal));
         const int rc = enqueue_ops(m, m->st, gclass);
@@ -3088,18 +3140,17 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
             cudaGetLastError();
             return rc != SWM_OK ? rc : SWM_ERR_CUDA;
         }
-        const cudaError_t ie = cudaGraphInstantiate(&m->gexec, g, 0);
+        const cudaError_t ie = cudaGraphInstantiate(&m->gx[gclass][h], g, 0);
         cudaGraphDestroy(g);
         if (ie != cudaSuccess) {
-            m->gexec = nullptr;
+            m->gx[gclass][h] = nullptr;
             swm_set_error("instantiating the block pipeline: %s", cudaGetErrorString(ie));
             return SWM_ERR_CUDA;
         }
-        m->gclass = gclass;
-        m->ggen = m->gen;
-        m->gctab = m->ix->ctab_gen;
+        m->gx_gen[gclass][h] = m->gen;
+        m->gx_tab[gclass][h] = m->ix->ctab_gen;
     }
-    SWM_CUDA(cudaGraphLaunch(m->gexec, m->st));
+    SWM_CUDA(cudaGraphLaunch(m->gx[gclass][h], m->st));
     return SWM_OK;
 }
 
@@ -3560,6 +3611,20 @@ extern "C" int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float
             return SWM_OK;
         }
     return SWM_ERR_ARG;
+}
+
+extern "C" int swm_mapper_tuning(swm_mapper *m, const swm_tuning *set, swm_tuning *get) {
+    if (!m) return SWM_ERR_ARG;
+    if (set) {
+        if (set->verify_head_bases != 32 && set->verify_head_bases != 64) {
+            swm_set_error("swm_mapper_tuning: verify_head_bases must be 32 or 64 (got %u)", set->verify_head_bases);
+            return SWM_ERR_ARG;
+        }
+        if (m->pending) return SWM_ERR_STATE;
+        m->head_blocks = set->verify_head_bases / 32;
+    }
+    if (get) get->verify_head_bases = 32 * m->head_blocks;
+    return SWM_OK;
 }
 
 extern "C" uint64_t swm_mapper_launches(const swm_mapper *m) { return m ? m->launches : 0; }

@@ -1,16 +1,23 @@
-"""Autotuner for the batched form: reads per block, mappers and length buckets.
+"""Autotuner for the batched form: reads per block, mappers, length buckets
+and, per 32-bp length bucket, the verification head and the block size.
 
 Verification runs the lanes of a warp in lockstep over their candidates'
 read lengths, so reads of very different lengths side by side waste lanes.
 The autotuner
 
 * groups reads into length buckets of 32 bp (`length_buckets`), so a block
-  holds reads of similar length, and
+  holds reads of similar length,
 * times a sample of resident reads under every (reads per block, mappers)
   candidate and keeps the fastest (`tune`), with an optional cache key
-  (for example GPU, k, length bucket, e).
+  (for example GPU, k, length bucket, e), and
+* for each length bucket, times that bucket's reads under every (bases of
+  the first verification pass, reads per block) pair and keeps the fastest
+  (`tune_buckets`): how many candidates the exact stop after the first pass
+  removes, against how many steps that pass costs, depends on the read
+  length.
 
-Results do not depend on the choice: every read maps the same in any block.
+Results do not depend on any choice: every read maps the same in any block,
+with either head length.
 """
 from __future__ import annotations
 
@@ -22,6 +29,8 @@ import numpy as np
 BUCKET_BP = 32
 BLOCKS = (65536, 131072, 262144, 524288)
 MAPPERS = (1, 2, 3)
+HEADS = (32, 64)                 # bases of the first verification pass
+BUCKET_BLOCKS = (131072, 524288)  # reads per block tried for each length bucket
 
 _cache: dict = {}
 
@@ -51,9 +60,10 @@ def _cudart():
 
 
 def run_blocks(mappers, d_reads: int, d_lens: int, stride: int, nreads: int, e: int, d_e: int | None, block: int,
-               on_done=None):
+               on_done=None, head: int | None = None):
     """Map nreads device-resident reads in blocks taken by the mappers in turn
-    (swm_map_device_submit / swm_map_device_wait); on_done(mapper) after each."""
+    (swm_map_device_submit / swm_map_device_wait); on_done(mapper) after each.
+    head: bases of the first verification pass for every block (None: keep)."""
     pend = []
     for i, b0 in enumerate(range(0, nreads, block)):
         nb = min(block, nreads - b0)
@@ -63,6 +73,8 @@ def run_blocks(mappers, d_reads: int, d_lens: int, stride: int, nreads: int, e: 
             if on_done:
                 on_done(pm)
         m = mappers[i % len(mappers)]
+        if head is not None:
+            m.set_head(head)
         m.submit_device(d_reads + b0 * stride, d_lens + b0 * 4, stride, nb, e,
                         None if d_e is None else d_e + b0)
         pend.append(m)
@@ -104,3 +116,40 @@ def tune(index, d_reads: int, d_lens: int, stride: int, nreads: int, e: int, d_e
     if key is not None:
         _cache[key] = res
     return res
+
+
+def tune_buckets(index, d_reads: int, d_lens: int, stride: int, lens: np.ndarray, e: int, d_e: int | None,
+                 nmappers: int, heads=HEADS, blocks=BUCKET_BLOCKS, sample: int = 524288) -> list[dict]:
+    """For every 32-bp length bucket of device-resident reads already grouped
+    by bucket (contiguous, in `length_buckets` order), the fastest (head,
+    block) pair, timed on up to `sample` reads of the bucket with nmappers
+    mappers (a warm-up pass, then a timed one)."""
+    import swmapper_gb300 as swm
+    rt = _cudart()
+    out = []
+    b0 = 0
+    for bucket, idx in length_buckets(lens):
+        n_b = idx.size
+        n = min(n_b, sample)
+        o = b0 + (n_b - n) // 2  # a window from the middle of the bucket
+        trials = []
+        for blk in blocks:
+            bs = min(blk, n)
+            if blk != blocks[0] and blk > n:
+                continue
+            ms = [swm.Mapper(index, max_reads=bs) for _ in range(nmappers)]
+            for hd in heads:
+                args = (d_reads + o * stride, d_lens + o * 4, stride, n, e, None if d_e is None else d_e + o, bs)
+                run_blocks(ms, *args, head=hd)
+                rt.cudaDeviceSynchronize()
+                t0 = time.perf_counter()
+                run_blocks(ms, *args, head=hd)
+                rt.cudaDeviceSynchronize()
+                trials.append({"head": hd, "block": blk, "reads_per_s": round(n / (time.perf_counter() - t0), 1)})
+            del ms
+        best = max(trials, key=lambda t: t["reads_per_s"])
+        lo = bucket * BUCKET_BP + 1
+        out.append({"bucket": int(bucket), "lengths": [lo, lo + BUCKET_BP - 1], "reads": int(n_b), "first": int(b0),
+                    "head": best["head"], "block": best["block"], "trials": trials})
+        b0 += n_b
+    return out

@@ -382,3 +382,22 @@ def test_gpu_mapping_other_seed_lengths(cuda_lib, k, e):
     out = m.map(reads, lens, e)
     _check(out, ref.records(), ref.unmapped)
     assert m.stats()["candidates"] == ref.stats["candidates"]
+
+
+@pytest.mark.parametrize("head", [32, 64])
+def test_gpu_verify_head_lengths(cuda_lib, head):
+    """The first verification pass's length (an autotuner knob) changes no
+    result: reads of 50-250 bp, per-read e, against the oracle."""
+    g = genome(2_000_000, 90, "human", nrun_min=2000, nrun_max=20000, copies_per_family=200)
+    reads, lens, _, _ = synth.reads(g, 3000, 50, 250, 0.04, seed=91, stride=250)
+    eper = np.array([math.ceil(0.05 * int(L)) for L in lens], np.uint8)
+    _, mix = oracle_index(g)
+    ref_recs, ref_unm = records_by_e(mix, reads, lens, eper)
+    ix = cuda_lib.Index.build(g)
+    m = cuda_lib.Mapper(ix, max_reads=reads.shape[0])
+    m.set_head(head)
+    assert m.head() == head
+    out = m.map(reads, lens, 0, errors_per_read=eper)
+    _check(out, ref_recs, ref_unm)
+    with pytest.raises(cuda_lib.SwmError):
+        m.set_head(48)
