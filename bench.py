@@ -357,16 +357,16 @@ def stage_bytes(stage, st, L, e, table=False):
     return 0
 
 
-def block_plan(nreads, block, tuned):
-    """(first read, reads, verification head bases) of every block: blocks of
-    `block` reads with a 64-base head, or, with per-bucket tuning, each
-    length bucket's reads in blocks of its own size with its own head."""
+def block_plan(nreads, block, tuned, verify="stream16"):
+    """(first read, reads, verification form) of every block: blocks of
+    `block` reads with the given form, or, with per-bucket tuning, each
+    length bucket's reads in blocks of its own size with its own form."""
     if not tuned or not tuned.get("buckets"):
-        return [(b0, min(block, nreads - b0), 64) for b0 in range(0, nreads, block)]
+        return [(b0, min(block, nreads - b0), verify) for b0 in range(0, nreads, block)]
     out = []
     for bk in tuned["buckets"]:
         lo, n, bs = bk["first"], bk["reads"], min(bk["block"], bk["reads"])
-        out += [(b0, min(bs, lo + n - b0), bk["head"]) for b0 in range(lo, lo + n, bs)]
+        out += [(b0, min(bs, lo + n - b0), bk["verify"]) for b0 in range(lo, lo + n, bs)]
     return out
 
 
@@ -422,12 +422,12 @@ def run_gpu(args):
         tuned = swtune.tune(ix, d_reads.value + o_t * stride, d_lens.value + o_t * 4, stride, n_t, E,
                             d_e.value + o_t if eper is not None else None)
         block, args.mappers = min(tuned["block"], nreads), tuned["mappers"]
-        # per 32-bp length bucket (reads grouped by bucket): verification head
-        # length and reads per block
+        # per 32-bp length bucket (reads grouped by bucket): verification form
+        # and reads per block
         if bucketed or int(lens.min()) == int(lens.max()):
             tuned["buckets"] = swtune.tune_buckets(ix, d_reads.value, d_lens.value, stride, lens, E,
                                                    d_e.value if eper is not None else None, args.mappers)
-    blocks = block_plan(nreads, block, tuned)
+    blocks = block_plan(nreads, block, tuned, args.verify)
     block = max(nb for _, nb, _ in blocks)
     mappers = [swm.Mapper(ix, max_reads=block) for _ in range(args.mappers)]
     m = mappers[0]
@@ -458,7 +458,7 @@ def run_gpu(args):
             if len(pend) == len(mappers):
                 drain()
             mm = mappers[i % len(mappers)]
-            mm.set_head(hd)
+            mm.set_verify(hd)
             mm.submit_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, nb, E,
                              d_e.value + b0 if eper is not None else None)
             pend.append(mm)
@@ -512,7 +512,7 @@ def run_gpu(args):
     # kernel times in isolation (one mapper, one block at a time) for the
     # stage breakdown and the roofline: one untimed pass over the reads
     for b0, nb, hd in blocks:
-        m.set_head(hd)
+        m.set_verify(hd)
         m.map_device(d_reads.value + b0 * stride, d_lens.value + b0 * 4, stride, nb, E,
                      d_e.value + b0 if eper is not None else None)
         for sname in STAGES:
@@ -572,7 +572,7 @@ def run_gpu(args):
             b0, nb, hd = blocks[i % len(blocks)]
             if len(pend) == ne:
                 drain()
-            mappers[i % ne].set_head(hd)
+            mappers[i % ne].set_verify(hd)
             mappers[i % ne].submit(reads[b0:b0 + nb], lens[b0:b0 + nb], E,
                                   None if eper is None else eper[b0:b0 + nb])
             pend.append((i, mappers[i % ne]))
@@ -989,6 +989,8 @@ def main():
                     help="reads of the timed workload compared with the reference's own mapper after the timing")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--requests", type=int, default=None, help="requests of the serving workload")
+    ap.add_argument("--verify", choices=["head64", "head32", "stream8", "stream16"], default="stream16",
+                    help="form of the verification stage when the autotuner does not choose it per length bucket")
     ap.add_argument("--table", type=int, default=1,
                     help="keep the index's candidate table (1) or drop it before the mappers are made (0)")
     ap.add_argument("--serving", type=int, default=1,

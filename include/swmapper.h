@@ -228,13 +228,20 @@ int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float *ms);
 /* Settings of a mapper that change its speed, never its results (no
  * reference counterpart; the autotuner sets them per read-length bucket). */
 typedef struct {
-    uint32_t verify_head_bases; /* bases of every candidate the first verification
-                                   pass runs before the exact stop test: 32 or 64
-                                   (default 64)                                 */
+    uint32_t verify_head_bases; /* two-pass verification: bases of every candidate
+                                   the first pass runs before its exact stop test,
+                                   32 or 64                                       */
+    uint32_t verify_chunk;      /* 0: two-pass verification; 8 or 16 (default 16):
+                                   streaming verification, each lane running its
+                                   own candidate and testing the stop bound every
+                                   8 / 16 bases, refilled from the queue as
+                                   candidates stop (verify_head_bases is then
+                                   ignored)                                       */
 } swm_tuning;
 
 /* Apply *set (may be NULL) and report the current settings in *get (may be
- * NULL); SWM_ERR_STATE while a block is in flight. */
+ * NULL); SWM_ERR_ARG for a value outside the lists above, SWM_ERR_STATE while a
+ * block is in flight. */
 int swm_mapper_tuning(swm_mapper *m, const swm_tuning *set, swm_tuning *get);
 
 /* Kernel launches queued for the last block. */

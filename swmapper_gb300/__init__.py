@@ -82,6 +82,15 @@ class SwmError(RuntimeError):
 _lib = None
 
 
+class Tuning(C.Structure):
+    """swm_tuning (include/swmapper.h)."""
+    _fields_ = [("verify_head_bases", C.c_uint32), ("verify_chunk", C.c_uint32)]
+
+
+# verification forms: name -> (verify_head_bases, verify_chunk)
+VERIFY_MODES = {"head32": (32, 0), "head64": (64, 0), "stream8": (64, 8), "stream16": (64, 16)}
+
+
 def lib():
     """Load the CUDA library; raise if it was not built (no fallback path)."""
     global _lib
@@ -113,7 +122,7 @@ def lib():
         L.swm_map_wait_packed.argtypes = [vp, C.POINTER(PackedResult)]
         L.swm_mapper_stats.argtypes = [vp, C.POINTER(MapStats)]
         L.swm_mapper_stage_ms.argtypes = [vp, C.c_char_p, C.POINTER(C.c_float)]
-        L.swm_mapper_tuning.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.swm_mapper_tuning.argtypes = [vp, C.POINTER(Tuning), C.POINTER(Tuning)]
         L.swm_mapper_launches.argtypes = [vp]
         L.swm_mapper_launches.restype = u64
         L.swm_mapper_stream.argtypes = [vp]
@@ -313,15 +322,24 @@ class Mapper:
         _check(lib().swm_mapper_stage_ms(self._h, stage.encode(), C.byref(v)), "swm_mapper_stage_ms")
         return float(v.value)
 
-    def set_head(self, bases: int) -> None:
-        """Bases of the first verification pass (32 or 64; swm_mapper_tuning)."""
-        v = C.c_uint32(bases)
-        _check(lib().swm_mapper_tuning(self._h, C.byref(v), None), "swm_mapper_tuning")
+    def set_verify(self, mode: str) -> None:
+        """Form of the verification stage (swm_mapper_tuning): "head32" /
+        "head64" (a first pass over that many bases of every candidate, then
+        the rest), or "stream8" / "stream16" (each lane runs its own candidate
+        and tests the stop bound every 8 / 16 bases). Results never change."""
+        if mode not in VERIFY_MODES:
+            raise SwmError(f"unknown verification form {mode!r} (one of {', '.join(VERIFY_MODES)})", -1)
+        head, chunk = VERIFY_MODES[mode]
+        t = Tuning(verify_head_bases=head, verify_chunk=chunk)
+        _check(lib().swm_mapper_tuning(self._h, C.byref(t), None), "swm_mapper_tuning")
 
-    def head(self) -> int:
-        v = C.c_uint32()
-        _check(lib().swm_mapper_tuning(self._h, None, C.byref(v)), "swm_mapper_tuning")
-        return int(v.value)
+    def verify(self) -> str:
+        t = Tuning()
+        _check(lib().swm_mapper_tuning(self._h, None, C.byref(t)), "swm_mapper_tuning")
+        for name, (head, chunk) in VERIFY_MODES.items():
+            if chunk == t.verify_chunk and (chunk or head == t.verify_head_bases):
+                return name
+        raise SwmError(f"unexpected tuning {t.verify_head_bases}/{t.verify_chunk}", -1)
 
     def launches(self) -> int:
         return int(lib().swm_mapper_launches(self._h))

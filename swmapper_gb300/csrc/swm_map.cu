@@ -55,8 +55,19 @@ enum {
     TOT_VT, TOT_VTQ, // candidates alive after the head of verification, and their queue head
     TOT_PLN, TOT_PLQ,  // items with refills and at most 32 selected seeds, queue head of k_plan_lanes
     TOT_PLW, TOT_PLWQ, // items with refills and more selected seeds, queue head of k_plan
+    TOT_CQ,            // queue head of the candidate stage (items)
     TOT_N
 };
+
+// Next CAND_TAKE items of a warp in the candidate stage (head *q): items differ
+// by a factor of a hundred in work (kept positions, batches), so warps take
+// them from a queue in small groups instead of a fixed stride.
+#define CAND_TAKE 4
+__device__ __forceinline__ uint32_t warp_take_items(uint32_t *q) {
+    uint32_t b = 0;
+    if ((threadIdx.x & 31) == 0) b = atomicAdd(q, (uint32_t)CAND_TAKE);
+    return __shfl_sync(0xffffffffu, b, 0);
+}
 
 // Next 32 work units of a warp from a device work queue (head *q): every lane
 // gets the same base; the warp is done when it reaches n.
@@ -89,10 +100,6 @@ struct BlockParams {
     const uint8_t *e;      // per-read thresholds, or null
     uint64_t stride;
     uint32_t nreads, nitems, errors, pad;
-    // multipliers of the integer multiply-adds in the Myers step: 1, 2 and
-    // 2^31, read from memory so that they stay multiplies (the FMA pipe)
-    // instead of being folded into shifts and adds (the ALU pipe)
-    uint32_t one, two, half, pad2;
 };
 
 struct MapBufs {
@@ -143,6 +150,13 @@ struct MapBufs {
     uint32_t *scan_tmp;
 };
 
+// Forms of the verification stage (swm_mapper_tuning); all give the same
+// results. HEAD32 / HEAD64: a head pass over the first 32 / 64 bases of every
+// candidate, then a tail pass over the ones still alive. STREAM8 / STREAM16:
+// k_verify_stream with its stop test every 8 / 16 bases, then the finishing
+// pass.
+enum { VMODE_HEAD32 = 0, VMODE_HEAD64, VMODE_STREAM8, VMODE_STREAM16, VMODE_N };
+
 struct swm_mapper {
     swm_index *ix;
     int device;
@@ -187,10 +201,10 @@ struct swm_mapper {
     BlockParams *h_par;        // pinned
     // one captured graph per (seed-kernel class, verification head length),
     // with the buffer and candidate-table generations it was captured with
-    cudaGraphExec_t gx[3][2];
-    uint32_t gx_gen[3][2], gx_tab[3][2];
+    cudaGraphExec_t gx[3][VMODE_N];
+    uint32_t gx_gen[3][VMODE_N], gx_tab[3][VMODE_N];
     uint32_t gen;              // buffer generation now
-    uint32_t head_blocks;      // 32-base blocks of the verification head (1 or 2)
+    int vmode;                 // verification form (VMODE_*)
 };
 
 // ======================================================================
@@ -1563,7 +1577,13 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS) k_cand(const
     // a warp's survivors past CAND_SMEM_KEEP go to its slice of global scratch
     auto gscratch = [&]() { return B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS; };
     unsigned long long kept_all = 0; // this warp's kept positions, added to the block's count once
-    for (uint32_t item = blockIdx.x * CAND_WARPS + wib; item < nitems; item += gridDim.x * CAND_WARPS) {
+    for (uint32_t g0 = warp_take_items(&B.tot[TOT_CQ]), gi = 0; g0 < nitems;) {
+        const uint32_t item = g0 + gi;
+        if (++gi == CAND_TAKE || item + 1 >= nitems) {
+            gi = 0;
+            g0 = warp_take_items(&B.tot[TOT_CQ]);
+        }
+        if (item >= nitems) break;
         const uint32_t nb = B.it_nbat[item];
         uint32_t total = 0;
         if (nb) {
@@ -1731,7 +1751,13 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS)
     CandTabSmem &S = sm_all[wib];
     auto gscratch = [&]() { return B.sort_scratch + (uint64_t)(blockIdx.x * CAND_WARPS + wib) * SWM_BATCH_POSITIONS; };
     unsigned long long kept_all = 0; // this warp's kept positions, added to the block's count once
-    for (uint32_t item = blockIdx.x * CAND_WARPS + wib; item < nitems; item += gridDim.x * CAND_WARPS) {
+    for (uint32_t g0 = warp_take_items(&B.tot[TOT_CQ]), gi = 0; g0 < nitems;) {
+        const uint32_t item = g0 + gi;
+        if (++gi == CAND_TAKE || item + 1 >= nitems) {
+            gi = 0;
+            g0 = warp_take_items(&B.tot[TOT_CQ]);
+        }
+        if (item >= nitems) break;
         const uint32_t nb = B.it_nbat[item];
         uint32_t total = 0;
         if (nb) {
@@ -1968,41 +1994,12 @@ __device__ __forceinline__ uint32_t window_start(uint32_t base_pos, uint32_t L, 
 // reference keeps in peq[read[i]]. myers_blocks runs the 32-base blocks
 // b0 .. b1 - 1 (the last one may be partial) from the state (VP, VN, ones =
 // steps whose D0 bit 0 was set); cp gets (VP, VN) at the start of each.
-// Integer multiply-adds issue on the FMA pipe while the logic ops of the
-// recurrence keep the ALU pipe busy.
-__device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t d;
-    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
-}
-__device__ __forceinline__ uint32_t mulhi_u32(uint32_t a, uint32_t b) {
-    uint32_t d;
-    asm("mul.hi.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
-    return d;
-}
-__device__ __forceinline__ uint32_t mulhi_s32(uint32_t a, uint32_t b) {
-    int32_t d;
-    asm("mul.hi.s32 %0, %1, %2;" : "=r"(d) : "r"((int32_t)a), "r"((int32_t)b));
-    return (uint32_t)d;
-}
-
-// The multipliers the step takes from memory: 1, 2 and 2^31.
-struct MadK {
-    uint32_t one, two, half;
-};
-
-// Banded Myers over 32-base blocks b0 .. b1 - 1 (banded_myers_simd,
-// mapper_cpe.c:519-660, 32-bit lanes). Per step the read base's bits are
-// broadcast to all-ones / all-zeros as the sign of a bit-reversed read word
-// (mul.hi.s32 by 1) that doubles each step (mad by 2); the carry add
-// VP + (X & VP) is a mad by 1 and D0 >> 1 a mul.hi by 2^31 -- the same
-// integers as the shifts and adds they replace, on the FMA pipe.
 __device__ __forceinline__ void myers_blocks(const uint32_t *WL, const uint32_t *WH, const uint32_t *RW, uint32_t L,
                                              uint32_t MASK, uint32_t b0, uint32_t b1, uint32_t &vp, uint32_t &vn,
-                                             uint32_t &ones, uint32_t *cp, const MadK &K) {
+                                             uint32_t &ones, uint32_t *cp) {
     for (uint32_t b = b0; b < b1; b++) {
         const uint32_t wl0 = WL[b], wl1 = WL[b + 1], wh0 = WH[b], wh1 = WH[b + 1];
-        uint32_t rrl = __brev(RW[2 * b]), rrh = __brev(RW[2 * b + 1]); // read base t at bit 31 - t
+        const uint32_t rlw = RW[2 * b], rhw = RW[2 * b + 1];
         const uint32_t steps = min(32u, L - 32 * b);
         cp[4 * b] = vp; // (VP, VN) before bases 32 b and 32 b + 16, for the traceback
         cp[4 * b + 1] = vn;
@@ -2015,15 +2012,14 @@ __device__ __forceinline__ void myers_blocks(const uint32_t *WL, const uint32_t 
                     cp[4 * b + 3] = vn;
                 }
                 const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
-                const uint32_t mL = mulhi_s32(rrl, K.one), mH = mulhi_s32(rrh, K.one);
-                rrl = mad_u32(rrl, K.two, 0u);
-                rrh = mad_u32(rrh, K.two, 0u);
+                const uint32_t mL = (uint32_t)((int32_t)(rlw << (31 - t)) >> 31);
+                const uint32_t mH = (uint32_t)((int32_t)(rhw << (31 - t)) >> 31);
                 const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
                 uint32_t x = eq | vn;
-                const uint32_t d0 = (mad_u32(x & vp, K.one, vp) ^ vp) | x;
+                const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;
                 const uint32_t hn = vp & d0;
                 const uint32_t hp = vn | ~(vp | d0);
-                x = mulhi_u32(d0, K.half);
+                x = d0 >> 1;
                 vn = x & hp;
                 vp = hn | ~(x | hp);
                 acc = __funnelshift_r(acc, d0, 1);
@@ -2035,15 +2031,13 @@ __device__ __forceinline__ void myers_blocks(const uint32_t *WL, const uint32_t 
                     cp[4 * b + 3] = vn;
                 }
                 const uint32_t wls = __funnelshift_r(wl0, wl1, t), whs = __funnelshift_r(wh0, wh1, t);
-                const uint32_t mL = mulhi_s32(rrl, K.one), mH = mulhi_s32(rrh, K.one);
-                rrl = mad_u32(rrl, K.two, 0u);
-                rrh = mad_u32(rrh, K.two, 0u);
+                const uint32_t mL = 0u - ((rlw >> t) & 1u), mH = 0u - ((rhw >> t) & 1u);
                 const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
                 uint32_t x = eq | vn;
-                const uint32_t d0 = (mad_u32(x & vp, K.one, vp) ^ vp) | x;
+                const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;
                 const uint32_t hn = vp & d0;
                 const uint32_t hp = vn | ~(vp | d0);
-                x = mulhi_u32(d0, K.half);
+                x = d0 >> 1;
                 vn = x & hp;
                 vp = hn | ~(x | hp);
                 acc = __funnelshift_r(acc, d0, 1);
@@ -2170,6 +2164,8 @@ __device__ __forceinline__ int band_scan_min(int err, uint32_t vp, uint32_t vn, 
 
 // HB: 32-base blocks the head pass runs (1 or 2; the autotuner picks it per
 // read-length bucket). Any HB gives the same results: the stop is exact.
+// The tail with HB = 0 is the finishing pass of the streaming form
+// (k_verify_stream): it runs its candidates from the first base.
 template <bool HEAD, int HB>
 __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *__restrict__ b2,
                                                 uint64_t b2_words, uint64_t ref_length, MapBufs B,
@@ -2177,7 +2173,6 @@ __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *_
                                                 uint64_t cap_arena) {
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
     const uint32_t *__restrict__ lens = B.par->lens;
-    const MadK K{B.par->one, B.par->two, B.par->half};
     uint64_t n;
     if (HEAD) {
         const uint64_t nc_all = B.tot[TOT_CANDS];
@@ -2197,6 +2192,8 @@ __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *_
         cp[0] = cp[1] = 0;
         if (HEAD) {
             c = j;
+        } else if (HB == 0) { // finishing pass: run from the first base
+            c = B.vt_x[j].x;
         } else {
             const uint2 x = B.vt_x[j];
             const uint4 st = B.vt_st[j], st2 = HB >= 2 ? B.vt_cp[j] : make_uint4(0u, 0u, 0u, 0u);
@@ -2235,7 +2232,7 @@ __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *_
         const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
         const uint32_t b0 = HEAD ? 0u : HB, b1 = HEAD ? min(nblk, (uint32_t)HB) : nblk;
         steps += min(L, 32 * b1) - 32 * b0;
-        myers_blocks(WL, WH, rw, L, MASK, b0, b1, vp, vn, ones, cp, K);
+        myers_blocks(WL, WH, rw, L, MASK, b0, b1, vp, vn, ones, cp);
         if (head_only) {
             if (band_scan_min(32 * HB - (int)ones, vp, vn, (int)rl - (int)L) > (int)e) {
                 cells += (unsigned long long)L * (2 * e + 1);
@@ -2298,6 +2295,178 @@ __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *_
     warp_add_u64(&B.stat[ST_STEPS], steps);
 }
 
+
+// Streaming verification. Every lane runs its own candidate, CH read bases at
+// a time, and after each chunk tests whether the band can still end at or
+// below e: cell 0 of the band is i - ones after i steps and each of the cells
+// 1 .. last_high is at least cell 0 minus the down steps (VN bits) below it,
+// so when (i - ones) - popc(VN & cells 0 .. last_high - 1) > e every cell of
+// the band, and by the argument above every cell of every later step, is
+// above e: the full run would return (SWM_MAXERROR, -1) and the lane writes
+// that at once. A lane whose candidate stopped or reached its last base takes
+// the next one from the warp's share of the queue (ranges of 32 taken with one
+// atomic), so lanes are not held by the slowest candidate of a group. The
+// candidates that reach their last base (about 2% on the human-scale genome)
+// are queued for the finishing pass k_verify<false, 0>, which runs them again
+// from the first base with checkpoints, the final scan (634-650), the Hamming
+// check and the traceback queue.
+//
+// Each lane keeps a sliding window of the packed genome in registers: the
+// (lo, hi) word pairs k .. k + 2 that hold window bases i .. i + 95, where k
+// is the pair of the chunk's first base, and pair k + 3 loaded ahead; the
+// read's word pair of the current 32-base block and the next one likewise.
+// A chunk of 16 bases moves k by at most one, so every genome and read word
+// is loaded once per candidate, a chunk before it is needed.
+template <int CH>
+__global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__restrict__ b2, uint64_t b2_words,
+                                                           uint64_t ref_length, MapBufs B, uint64_t cap_chunks,
+                                                           uint64_t cap_elems, uint64_t cap_cands) {
+    static_assert(CH == 8 || CH == 16, "a chunk moves the window by at most one word pair");
+    if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint32_t *__restrict__ lens = B.par->lens;
+    const uint2 *__restrict__ b2p = reinterpret_cast<const uint2 *>(b2); // (lo, hi) word pairs
+    const uint64_t npairs = b2_words / 2;
+    auto pair_at = [&](uint64_t q) { return q < npairs ? b2p[q] : make_uint2(0u, 0u); };
+    const uint64_t nc_all = B.tot[TOT_CANDS];
+    const uint32_t n = (uint32_t)(nc_all < cap_cands ? nc_all : cap_cands);
+    const uint32_t lane = lane_id();
+    // per-lane counts fit 32 bits: a lane runs at most ceil(cap_cands / lanes of
+    // the grid) candidates of at most 254 x 31 cells
+    uint32_t cells = 0, nsteps = 0;
+    uint32_t qn = 0, qe = 0; // the warp's queue entries not handed out yet: [qn, qe)
+    bool drained = false;    // the queue has no more ranges
+    bool act = false;
+    // meta: read length | e << 8 | (last_high + 1, 0 when last_high < 0) << 16
+    uint32_t c = 0, meta = 0, i = 0, vp = 0, vn = 0, ones = 0, ws = 0;
+    uint2 a0 = {0, 0}, a1 = {0, 0}, a2 = {0, 0}, nx = {0, 0}, rr = {0, 0}, nrr = {0, 0};
+    const uint2 *rwp = nullptr; // the item's read word pairs (lo, hi) per 32-base block
+    for (;;) {
+        const unsigned need = __ballot_sync(0xffffffffu, !act);
+        if (need) {
+            const uint32_t k = __popc(need), r = __popc(need & lanemask_lt()), avail = qe - qn;
+            uint32_t jb = qe, je = qe; // a new range, empty unless taken
+            if (k > avail && !drained) {
+                const uint32_t t = warp_take(&B.tot[TOT_VQ]);
+                if (t >= n) {
+                    drained = true;
+                } else {
+                    jb = t;
+                    je = min(t + 32u, n);
+                }
+            }
+            uint32_t j = 0xffffffffu;
+            if (r < avail) j = qn + r;
+            else if (jb + (r - avail) < je) j = jb + (r - avail);
+            if (k <= avail) {
+                qn += k;
+            } else {
+                qn = min(jb + (k - avail), je);
+                qe = je;
+            }
+            if (!act && j != 0xffffffffu) {
+                c = j;
+                const uint32_t item = B.cc_item[c], p = B.cc_pos[c];
+                const uint32_t L = lens[item >> 1], e = B.it_e[item];
+                uint32_t rl;
+                ws = window_start(p, L, e, ref_length, &rl);
+                if (ws == 0xffffffffu) {
+                    B.vr_flag[c] = VR_INVALID;
+                    B.vr_err[c] = SWM_MAXERROR;
+                    B.vr_mloc[c] = -1;
+                } else {
+                    act = true;
+                    i = vp = vn = ones = 0;
+                    const int lh = (int)rl - (int)L; // last_high: cells 0 .. lh of the final scan
+                    meta = L | e << 8 | (uint32_t)(lh > 0 ? lh : 0) << 16;
+                    const uint64_t q = ws >> 5;
+                    a0 = pair_at(q);
+                    a1 = pair_at(q + 1);
+                    a2 = pair_at(q + 2);
+                    nx = pair_at(q + 3);
+                    rwp = reinterpret_cast<const uint2 *>(B.it_w + (uint64_t)item * 32);
+                    rr = rwp[0];
+                    nrr = L > 32 ? rwp[1] : make_uint2(0u, 0u);
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, act)) {
+            if (drained && qn >= qe) break;
+            continue;
+        }
+        bool fin = false, dead = false;
+        if (act) {
+            const uint32_t L = meta & 0xffu, e = (meta >> 8) & 0xffu;
+            const uint32_t MASK = (1u << (2 * e + 1)) - 1u, lhm = (1u << (meta >> 16)) - 1u;
+            const uint32_t sh = (ws + i) & 31; // window bit of the chunk's first step within pair k
+            const uint32_t xl0 = __funnelshift_r(a0.x, a1.x, sh), xl1 = __funnelshift_r(a1.x, a2.x, sh);
+            const uint32_t xh0 = __funnelshift_r(a0.y, a1.y, sh), xh1 = __funnelshift_r(a1.y, a2.y, sh);
+            const uint32_t rlw = rr.x >> (i & 31), rhw = rr.y >> (i & 31);
+            const uint32_t nst = min((uint32_t)CH, L - i);
+            uint32_t acc = 0;
+#define SWM_STREAM_STEP(t)                                                                                        \
+    {                                                                                                             \
+        const uint32_t wls = __funnelshift_r(xl0, xl1, (t)), whs = __funnelshift_r(xh0, xh1, (t));              \
+        const uint32_t mL = (uint32_t)((int32_t)(rlw << (31 - (t))) >> 31);                                      \
+        const uint32_t mH = (uint32_t)((int32_t)(rhw << (31 - (t))) >> 31);                                      \
+        const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;                                                   \
+        uint32_t x = eq | vn;                                                                                     \
+        const uint32_t d0 = ((vp + (x & vp)) ^ vp) | x;                                                          \
+        const uint32_t hn = vp & d0;                                                                              \
+        const uint32_t hp = vn | ~(vp | d0);                                                                      \
+        x = d0 >> 1;                                                                                              \
+        vn = x & hp;                                                                                              \
+        vp = hn | ~(x | hp);                                                                                      \
+        acc = __funnelshift_r(acc, d0, 1);                                                                        \
+    }
+            if (nst == CH) {
+#pragma unroll
+                for (uint32_t t = 0; t < CH; t++) SWM_STREAM_STEP(t)
+            } else {
+                for (uint32_t t = 0; t < nst; t++) SWM_STREAM_STEP(t)
+            }
+#undef SWM_STREAM_STEP
+            ones += __popc(acc);
+            i += nst;
+            nsteps += nst;
+            if (i >= L) {
+                fin = true;
+            } else if ((int)(i - ones) - (int)__popc(vn & lhm) > (int)e) {
+                dead = true;
+            } else {
+                if (sh + CH >= 32) { // the next chunk starts in pair k + 1
+                    a0 = a1;
+                    a1 = a2;
+                    a2 = nx;
+                    nx = pair_at((uint64_t)((ws + i) >> 5) + 3);
+                }
+                if ((i & 31) == 0) { // the next chunk starts a new 32-base block of the read
+                    rr = nrr;
+                    nrr = (i >> 5) + 1 < 8 ? rwp[(i >> 5) + 1] : make_uint2(0u, 0u);
+                }
+            }
+        }
+        const unsigned fm = __ballot_sync(0xffffffffu, fin);
+        if (fm) {
+            const uint32_t leader = __ffs(fm) - 1;
+            uint32_t at = 0;
+            if (lane == leader) at = atomicAdd(&B.tot[TOT_VT], (uint32_t)__popc(fm));
+            at = __shfl_sync(0xffffffffu, at, leader);
+            if (fin) {
+                B.vt_x[at + __popc(fm & lanemask_lt())] = make_uint2(c, 0u);
+                act = false;
+            }
+        }
+        if (dead) {
+            cells += (meta & 0xffu) * (2 * ((meta >> 8) & 0xffu) + 1);
+            B.vr_err[c] = SWM_MAXERROR;
+            B.vr_mloc[c] = -1;
+            B.vr_flag[c] = VR_FAIL;
+            act = false;
+        }
+    }
+    warp_add_u64(&B.stat[ST_CELLS], (unsigned long long)cells);
+    warp_add_u64(&B.stat[ST_STEPS], (unsigned long long)nsteps);
+}
 
 // Traceback of the passing candidates that the Hamming check did not resolve
 // (align_reads, mapper_cpe.c:288-509): walk back from (L - 1, location)
@@ -2730,8 +2899,29 @@ __global__ void __launch_bounds__(128) k_records(MapBufs B, uint64_t cap_chunks,
         for (uint32_t s = s0; s < s0 + nb; s++) {
             const uint32_t cbeg = cnext, cn = B.bt_cnt[s];
             cnext += cn;
-            uint32_t g = 0;
-            for (uint32_t c = cbeg; c < cbeg + cn; c++) {
+            uint32_t g = 0; // candidates of the batch's current group of 8 (failed and passing, not invalid)
+            const uint32_t cend = cbeg + cn;
+            for (uint32_t c = cbeg; c < cend; c++) {
+                // Runs of failed candidates (flag 0: no location, one group
+                // slot each) are taken 16 or 4 at a time. Between two
+                // locations the flush test at a group boundary sees the same
+                // (num, len) every time, and after a flush it is false, so a
+                // run that crosses one or more boundaries needs one test.
+                if ((c & 15) == 0 && c + 16 <= cend) {
+                    const uint4 w = *reinterpret_cast<const uint4 *>(vflag + c);
+                    if ((w.x | w.y | w.z | w.w) == 0) {
+                        if (g + 16 >= 8 && (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16)) put();
+                        g = (g + 16) & 7;
+                        c += 15;
+                        continue;
+                    }
+                }
+                if ((c & 3) == 0 && c + 4 <= cend && *reinterpret_cast<const uint32_t *>(vflag + c) == 0) {
+                    if (g + 4 >= 8 && (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16)) put();
+                    g = (g + 4) & 7;
+                    c += 3;
+                    continue;
+                }
                 const uint8_t f = vflag[c];
                 if (f == VR_INVALID) continue;
                 if (f == VR_HAM || f == VR_TB) {
@@ -2945,7 +3135,7 @@ extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper *
     m->cap_bytes = cap_clamp(m->cap_items * 32 + 4096);
     m->cap_arena = ARENA_CAP_DEFAULT;
     m->stride_cap = 0;
-    m->head_blocks = 2;
+    m->vmode = VMODE_STREAM16;
     int rc = SWM_OK;
     if (cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking) != cudaSuccess) rc = SWM_ERR_CUDA;
     for (int i = 0; i < 9 && rc == SWM_OK; i++)
@@ -2974,7 +3164,7 @@ extern "C" void swm_mapper_free(swm_mapper *m) {
     cudaSetDevice(m->device);
     if (m->st) cudaStreamSynchronize(m->st);
     for (int a = 0; a < 3; a++)
-        for (int h = 0; h < 2; h++)
+        for (int h = 0; h < VMODE_N; h++)
             if (m->gx[a][h]) cudaGraphExecDestroy(m->gx[a][h]);
     free_bufs(m->b);
     cudaFree(m->d_reads);
@@ -3064,13 +3254,22 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[4], st, cudaEventRecordExternal));
     {
-        auto head = m->head_blocks == 1 ? k_verify<true, 1> : k_verify<true, 2>;
-        auto tail = m->head_blocks == 1 ? k_verify<false, 1> : k_verify<false, 2>;
         const unsigned vg = grid_cap(m->cap_cands, 128, 16);
-        head<<<vg, 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks,
-                                 m->cap_elems, m->cap_cands, m->cap_arena);
-        tail<<<vg, 128, 0, st>>>(ix->d_b2, ix->n_words2 + SWM_PAD_WORDS, ix->ref_length, B, m->cap_chunks,
-                                 m->cap_elems, m->cap_cands, m->cap_arena);
+        const uint64_t nw = ix->n_words2 + SWM_PAD_WORDS;
+        if (m->vmode == VMODE_STREAM8 || m->vmode == VMODE_STREAM16) {
+            auto stream = m->vmode == VMODE_STREAM8 ? k_verify_stream<8> : k_verify_stream<16>;
+            stream<<<grid_cap(m->cap_cands, 128, 10), 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks,
+                                                                     m->cap_elems, m->cap_cands);
+            k_verify<false, 0><<<vg, 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks, m->cap_elems,
+                                                   m->cap_cands, m->cap_arena);
+        } else {
+            auto head = m->vmode == VMODE_HEAD32 ? k_verify<true, 1> : k_verify<true, 2>;
+            auto tail = m->vmode == VMODE_HEAD32 ? k_verify<false, 1> : k_verify<false, 2>;
+            head<<<vg, 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
+                                     m->cap_arena);
+            tail<<<vg, 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
+                                     m->cap_arena);
+        }
     }
     m->launches += 2;
     LAUNCH_CHECK();
@@ -3123,11 +3322,7 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     P->nitems = 2 * nreads;
     P->errors = errors;
     P->pad = 0;
-    P->one = 1;
-    P->two = 2;
-    P->half = 0x80000000u;
-    P->pad2 = 0;
-    const int h = m->head_blocks == 1 ? 0 : 1;
+    const int h = m->vmode;
     if (!m->gx[gclass][h] || m->gx_gen[gclass][h] != m->gen || m->gx_tab[gclass][h] != m->ix->ctab_gen) {
         drop_graph(m, gclass, h);
         cudaGraph_t g = nullptr;
@@ -3616,14 +3811,25 @@ extern "C" int swm_mapper_stage_ms(const swm_mapper *m, const char *stage, float
 extern "C" int swm_mapper_tuning(swm_mapper *m, const swm_tuning *set, swm_tuning *get) {
     if (!m) return SWM_ERR_ARG;
     if (set) {
-        if (set->verify_head_bases != 32 && set->verify_head_bases != 64) {
+        int mode;
+        if (set->verify_chunk == 8) mode = VMODE_STREAM8;
+        else if (set->verify_chunk == 16) mode = VMODE_STREAM16;
+        else if (set->verify_chunk != 0) {
+            swm_set_error("swm_mapper_tuning: verify_chunk must be 0, 8 or 16 (got %u)", set->verify_chunk);
+            return SWM_ERR_ARG;
+        } else if (set->verify_head_bases == 32 || set->verify_head_bases == 64) {
+            mode = set->verify_head_bases == 32 ? VMODE_HEAD32 : VMODE_HEAD64;
+        } else {
             swm_set_error("swm_mapper_tuning: verify_head_bases must be 32 or 64 (got %u)", set->verify_head_bases);
             return SWM_ERR_ARG;
         }
         if (m->pending) return SWM_ERR_STATE;
-        m->head_blocks = set->verify_head_bases / 32;
+        m->vmode = mode;
     }
-    if (get) get->verify_head_bases = 32 * m->head_blocks;
+    if (get) {
+        get->verify_head_bases = m->vmode == VMODE_HEAD32 ? 32u : 64u;
+        get->verify_chunk = m->vmode == VMODE_STREAM8 ? 8u : m->vmode == VMODE_STREAM16 ? 16u : 0u;
+    }
     return SWM_OK;
 }
 

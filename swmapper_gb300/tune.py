@@ -1,23 +1,26 @@
 """Autotuner for the batched form: reads per block, mappers, length buckets
-and, per 32-bp length bucket, the verification head and the block size.
+and, per 32-bp length bucket, the form of the verification stage and the
+block size.
 
-Verification runs the lanes of a warp in lockstep over their candidates'
-read lengths, so reads of very different lengths side by side waste lanes.
-The autotuner
+Verification runs the lanes of a warp over their candidates' read lengths,
+so reads of very different lengths side by side waste lanes. The autotuner
 
 * groups reads into length buckets of 32 bp (`length_buckets`), so a block
   holds reads of similar length,
 * times a sample of resident reads under every (reads per block, mappers)
   candidate and keeps the fastest (`tune`), with an optional cache key
   (for example GPU, k, length bucket, e), and
-* for each length bucket, times that bucket's reads under every (bases of
-  the first verification pass, reads per block) pair and keeps the fastest
-  (`tune_buckets`): how many candidates the exact stop after the first pass
-  removes, against how many steps that pass costs, depends on the read
-  length.
+* for each length bucket, times that bucket's reads under every
+  (verification form, reads per block) pair and keeps the fastest
+  (`tune_buckets`). The forms: a first pass over 64 or 32 bases of every
+  candidate with an exact stop test, then the rest ("head64", "head32"), or
+  lanes that each run their own candidate and test a stop bound every 8 or
+  16 bases, taking the next candidate as soon as theirs stops ("stream8",
+  "stream16"). Which is faster depends on how early the candidates of that
+  read length can be ruled out, against the per-chunk cost of the test.
 
-Results do not depend on any choice: every read maps the same in any block,
-with either head length.
+Results do not depend on any choice: every read maps the same in any block
+and under every form.
 """
 from __future__ import annotations
 
@@ -29,7 +32,7 @@ import numpy as np
 BUCKET_BP = 32
 BLOCKS = (65536, 131072, 262144, 524288)
 MAPPERS = (1, 2, 3)
-HEADS = (32, 64)                 # bases of the first verification pass
+VERIFY = ("head64", "head32", "stream8", "stream16")  # forms of the verification stage
 BUCKET_BLOCKS = (131072, 524288)  # reads per block tried for each length bucket
 
 _cache: dict = {}
@@ -60,10 +63,10 @@ def _cudart():
 
 
 def run_blocks(mappers, d_reads: int, d_lens: int, stride: int, nreads: int, e: int, d_e: int | None, block: int,
-               on_done=None, head: int | None = None):
+               on_done=None, verify: str | None = None):
     """Map nreads device-resident reads in blocks taken by the mappers in turn
     (swm_map_device_submit / swm_map_device_wait); on_done(mapper) after each.
-    head: bases of the first verification pass for every block (None: keep)."""
+    verify: form of the verification stage for every block (None: keep)."""
     pend = []
     for i, b0 in enumerate(range(0, nreads, block)):
         nb = min(block, nreads - b0)
@@ -73,8 +76,8 @@ def run_blocks(mappers, d_reads: int, d_lens: int, stride: int, nreads: int, e: 
             if on_done:
                 on_done(pm)
         m = mappers[i % len(mappers)]
-        if head is not None:
-            m.set_head(head)
+        if verify is not None:
+            m.set_verify(verify)
         m.submit_device(d_reads + b0 * stride, d_lens + b0 * 4, stride, nb, e,
                         None if d_e is None else d_e + b0)
         pend.append(m)
@@ -119,10 +122,10 @@ def tune(index, d_reads: int, d_lens: int, stride: int, nreads: int, e: int, d_e
 
 
 def tune_buckets(index, d_reads: int, d_lens: int, stride: int, lens: np.ndarray, e: int, d_e: int | None,
-                 nmappers: int, heads=HEADS, blocks=BUCKET_BLOCKS, sample: int = 524288) -> list[dict]:
+                 nmappers: int, forms=VERIFY, blocks=BUCKET_BLOCKS, sample: int = 524288) -> list[dict]:
     """For every 32-bp length bucket of device-resident reads already grouped
-    by bucket (contiguous, in `length_buckets` order), the fastest (head,
-    block) pair, timed on up to `sample` reads of the bucket with nmappers
+    by bucket (contiguous, in `length_buckets` order), the fastest
+    (verification form, block) pair, timed on up to `sample` reads of the bucket with nmappers
     mappers (a warm-up pass, then a timed one)."""
     import swmapper_gb300 as swm
     rt = _cudart()
@@ -138,18 +141,18 @@ def tune_buckets(index, d_reads: int, d_lens: int, stride: int, lens: np.ndarray
             if blk != blocks[0] and blk > n:
                 continue
             ms = [swm.Mapper(index, max_reads=bs) for _ in range(nmappers)]
-            for hd in heads:
+            for vf in forms:
                 args = (d_reads + o * stride, d_lens + o * 4, stride, n, e, None if d_e is None else d_e + o, bs)
-                run_blocks(ms, *args, head=hd)
+                run_blocks(ms, *args, verify=vf)
                 rt.cudaDeviceSynchronize()
                 t0 = time.perf_counter()
-                run_blocks(ms, *args, head=hd)
+                run_blocks(ms, *args, verify=vf)
                 rt.cudaDeviceSynchronize()
-                trials.append({"head": hd, "block": blk, "reads_per_s": round(n / (time.perf_counter() - t0), 1)})
+                trials.append({"verify": vf, "block": blk, "reads_per_s": round(n / (time.perf_counter() - t0), 1)})
             del ms
         best = max(trials, key=lambda t: t["reads_per_s"])
         lo = bucket * BUCKET_BP + 1
         out.append({"bucket": int(bucket), "lengths": [lo, lo + BUCKET_BP - 1], "reads": int(n_b), "first": int(b0),
-                    "head": best["head"], "block": best["block"], "trials": trials})
+                    "verify": best["verify"], "block": best["block"], "trials": trials})
         b0 += n_b
     return out

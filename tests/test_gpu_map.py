@@ -384,10 +384,10 @@ def test_gpu_mapping_other_seed_lengths(cuda_lib, k, e):
     assert m.stats()["candidates"] == ref.stats["candidates"]
 
 
-@pytest.mark.parametrize("head", [32, 64])
-def test_gpu_verify_head_lengths(cuda_lib, head):
-    """The first verification pass's length (an autotuner knob) changes no
-    result: reads of 50-250 bp, per-read e, against the oracle."""
+@pytest.mark.parametrize("mode", ["head32", "head64", "stream8", "stream16"])
+def test_gpu_verify_forms(cuda_lib, mode):
+    """The form of the verification stage (an autotuner knob) changes no
+    result: reads of 50-250 bp, per-read e up to 13, against the oracle."""
     g = genome(2_000_000, 90, "human", nrun_min=2000, nrun_max=20000, copies_per_family=200)
     reads, lens, _, _ = synth.reads(g, 3000, 50, 250, 0.04, seed=91, stride=250)
     eper = np.array([math.ceil(0.05 * int(L)) for L in lens], np.uint8)
@@ -395,9 +395,35 @@ def test_gpu_verify_head_lengths(cuda_lib, head):
     ref_recs, ref_unm = records_by_e(mix, reads, lens, eper)
     ix = cuda_lib.Index.build(g)
     m = cuda_lib.Mapper(ix, max_reads=reads.shape[0])
-    m.set_head(head)
-    assert m.head() == head
+    m.set_verify(mode)
+    assert m.verify() == mode
     out = m.map(reads, lens, 0, errors_per_read=eper)
     _check(out, ref_recs, ref_unm)
     with pytest.raises(cuda_lib.SwmError):
-        m.set_head(48)
+        m.set_verify("head48")
+    assert m.verify() == mode
+
+
+@pytest.mark.parametrize("mode", ["stream8", "stream16"])
+def test_gpu_streaming_verify_uniform_e(cuda_lib, mode):
+    """Streaming verification at one e for every read (150 bp, e = 7) on a
+    repeat-rich genome: records, candidate counts and passing counts equal the
+    oracle's and the two-pass form's."""
+    g = genome(3_000_000, 93, "human", nrun_min=2000, nrun_max=20000, copies_per_family=300)
+    reads, lens, _, _ = synth.reads(g, 4000, 150, 150, 0.03, seed=94, stride=160)
+    ref, mix = oracle_index(g)
+    want = po.map_reads(mix, reads, lens, 7)
+    ix = cuda_lib.Index.build(g)
+    m = cuda_lib.Mapper(ix, max_reads=reads.shape[0])
+    m.set_verify("head64")
+    base = m.map(reads, lens, 7)
+    st64 = m.stats()
+    m.set_verify(mode)
+    out = m.map(reads, lens, 7)
+    st = m.stats()
+    _check(out, want.records(), want.unmapped)
+    _check(out, base.records(), base.unmapped)
+    assert st["candidates"] == st64["candidates"] == want.stats["candidates"]
+    assert st["passed"] == st64["passed"]
+    assert st["cells"] == st64["cells"]
+    assert st["myers_steps"] < st64["myers_steps"]
