@@ -125,6 +125,7 @@ struct MapBufs {
     uint32_t *cand_ub;
     // dense candidates (cap_cands)
     uint32_t *cc_pos, *cc_item;
+    uint32_t *cc_ws, *cc_meta; // window start (0xffffffff: invalid) and L | e << 8 | max(last_high, 0) << 16
     uint8_t *vr_flag;
     uint32_t *vr_loc;
     int32_t *vr_err, *vr_mloc;
@@ -1020,7 +1021,10 @@ __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t v) {
 // independent): items with at most PLAN_LANE_SEEDS selected seeds from the
 // front for k_plan_lanes, the others from the back for k_plan.
 #define PLAN_LANE_SEEDS 32
-__global__ void __launch_bounds__(256) k_plan_list(MapBufs B, uint64_t cap_chunks) {
+// chunks: write the refill chunks of the single-batch items (the candidate
+// kernel without the candidate table gathers from them; k_cand_table reads
+// chunks only of items with several batches).
+__global__ void __launch_bounds__(256) k_plan_list(MapBufs B, uint64_t cap_chunks, bool chunks) {
     const uint32_t nitems = B.par->nitems;
     const uint32_t lane = lane_id();
     for (uint32_t base = blockIdx.x * 256 + (threadIdx.x & ~31u); base < nitems; base += gridDim.x * 256) {
@@ -1052,7 +1056,7 @@ __global__ void __launch_bounds__(256) k_plan_list(MapBufs B, uint64_t cap_chunk
             const unsigned long long perm = B.it_perm[it];
             const uint64_t sb = (uint64_t)it * SWM_MAX_SEL;
             uint32_t q = 0;
-            for (uint32_t i0 = 0; i0 < ns; i0 += 32) {
+            for (uint32_t i0 = 0; chunks && i0 < ns; i0 += 32) {
                 const uint32_t i = i0 + lane;
                 const uint2 sv = i < ns ? B.sel[sb + sel_slot(perm, i)] : make_uint2(0u, 0u);
                 const uint32_t r = sv.y > SWM_PER_FETCH ? (sv.y - 1) / SWM_PER_FETCH : 0u;
@@ -1899,8 +1903,21 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS)
 // Dense candidate list: item by item, batch by batch, in verification order.
 #define COMPACT_HEAVY 16 // candidates above which an item is copied by its whole warp
 
+// Each candidate also gets its window start and (L, e, last_high) for the
+// streaming verification (window_start, adjust_ref_len 1403-1435).
+__device__ __forceinline__ uint32_t window_start(uint32_t base_pos, uint32_t L, uint32_t e, uint64_t ref_length,
+                                                 uint32_t *rl_out);
+__device__ __forceinline__ void put_window(MapBufs &B, uint64_t o, uint32_t p, uint32_t L, uint32_t e,
+                                           uint64_t ref_length) {
+    uint32_t rl;
+    const uint32_t ws = window_start(p, L, e, ref_length, &rl);
+    const int lh = (int)rl - (int)L;
+    B.cc_ws[o] = ws;
+    B.cc_meta[o] = L | e << 8 | (uint32_t)(lh > 0 ? lh : 0) << 16;
+}
+
 __global__ void __launch_bounds__(256) k_compact(MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
-                                                 uint64_t cap_cands) {
+                                                 uint64_t cap_cands, uint64_t ref_length) {
     const uint32_t nitems = B.par->nitems;
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     const uint32_t lane = lane_id();
@@ -1926,13 +1943,16 @@ __global__ void __launch_bounds__(256) k_compact(MapBufs B, uint64_t cap_chunks,
             }
             heavy = nb && nc > COMPACT_HEAVY;
             if (nb && !heavy) {
+                const uint32_t L = B.par->lens[item >> 1], e = B.it_e[item];
                 uint32_t o = o0;
                 for (uint32_t b = 0; b < nb; b++) {
                     const uint32_t n = nref ? B.bt_cnt[sbase + b] : nc; // one batch when there are no refills
                     const uint32_t e0 = nref ? B.bt_e0[sbase + b] : eloff;
                     for (uint32_t j = 0; j < n; j++) {
-                        B.cc_pos[o + j] = B.cand_ub[e0 + j];
+                        const uint32_t p = B.cand_ub[e0 + j];
+                        B.cc_pos[o + j] = p;
                         B.cc_item[o + j] = item;
+                        put_window(B, o + j, p, L, e, ref_length);
                     }
                     o += n;
                 }
@@ -1946,12 +1966,15 @@ __global__ void __launch_bounds__(256) k_compact(MapBufs B, uint64_t cap_chunks,
             const uint32_t hnc = __shfl_sync(0xffffffffu, nc, src), hsb = __shfl_sync(0xffffffffu, sbase, src);
             const uint32_t hel = __shfl_sync(0xffffffffu, eloff, src);
             uint32_t o = __shfl_sync(0xffffffffu, o0, src);
+            const uint32_t hit = item0 + src, hL = B.par->lens[hit >> 1], he = B.it_e[hit];
             for (uint32_t b = 0; b < hnb; b++) {
                 const uint32_t n = hnref ? B.bt_cnt[hsb + b] : hnc;
                 const uint32_t e0 = hnref ? B.bt_e0[hsb + b] : hel;
                 for (uint32_t j = lane; j < n; j += 32) {
-                    B.cc_pos[o + j] = B.cand_ub[e0 + j];
-                    B.cc_item[o + j] = item0 + src;
+                    const uint32_t p = B.cand_ub[e0 + j];
+                    B.cc_pos[o + j] = p;
+                    B.cc_item[o + j] = hit;
+                    put_window(B, o + j, p, hL, he, ref_length);
                 }
                 o += n;
             }
@@ -2164,8 +2187,6 @@ __device__ __forceinline__ int band_scan_min(int err, uint32_t vp, uint32_t vn, 
 
 // HB: 32-base blocks the head pass runs (1 or 2; the autotuner picks it per
 // read-length bucket). Any HB gives the same results: the stop is exact.
-// The tail with HB = 0 is the finishing pass of the streaming form
-// (k_verify_stream): it runs its candidates from the first base.
 template <bool HEAD, int HB>
 __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *__restrict__ b2,
                                                 uint64_t b2_words, uint64_t ref_length, MapBufs B,
@@ -2192,8 +2213,6 @@ __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *_
         cp[0] = cp[1] = 0;
         if (HEAD) {
             c = j;
-        } else if (HB == 0) { // finishing pass: run from the first base
-            c = B.vt_x[j].x;
         } else {
             const uint2 x = B.vt_x[j];
             const uint4 st = B.vt_st[j], st2 = HB >= 2 ? B.vt_cp[j] : make_uint4(0u, 0u, 0u, 0u);
@@ -2306,10 +2325,8 @@ __global__ void __launch_bounds__(128, HEAD ? 10 : 0) k_verify(const uint32_t *_
 // that at once. A lane whose candidate stopped or reached its last base takes
 // the next one from the warp's share of the queue (ranges of 32 taken with one
 // atomic), so lanes are not held by the slowest candidate of a group. The
-// candidates that reach their last base (about 2% on the human-scale genome)
-// are queued for the finishing pass k_verify<false, 0>, which runs them again
-// from the first base with checkpoints, the final scan (634-650), the Hamming
-// check and the traceback queue.
+// candidates with fewer than CH bases left (about 2% on the human-scale
+// genome) are queued with their state for the finishing pass k_verify_finish.
 //
 // Each lane keeps a sliding window of the packed genome in registers: the
 // (lo, hi) word pairs k .. k + 2 that hold window bases i .. i + 95, where k
@@ -2323,7 +2340,6 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
                                                            uint64_t cap_elems, uint64_t cap_cands) {
     static_assert(CH == 8 || CH == 16, "a chunk moves the window by at most one word pair");
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
-    const uint32_t *__restrict__ lens = B.par->lens;
     const uint2 *__restrict__ b2p = reinterpret_cast<const uint2 *>(b2); // (lo, hi) word pairs
     const uint64_t npairs = b2_words / 2;
     auto pair_at = [&](uint64_t q) { return q < npairs ? b2p[q] : make_uint2(0u, 0u); };
@@ -2338,6 +2354,7 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
     bool act = false;
     // meta: read length | e << 8 | (last_high + 1, 0 when last_high < 0) << 16
     uint32_t c = 0, meta = 0, i = 0, vp = 0, vn = 0, ones = 0, ws = 0;
+    bool fin0 = false; // the candidate just taken goes to the finishing pass as it is
     uint2 a0 = {0, 0}, a1 = {0, 0}, a2 = {0, 0}, nx = {0, 0}, rr = {0, 0}, nrr = {0, 0};
     const uint2 *rwp = nullptr; // the item's read word pairs (lo, hi) per 32-base block
     for (;;) {
@@ -2365,19 +2382,19 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
             }
             if (!act && j != 0xffffffffu) {
                 c = j;
-                const uint32_t item = B.cc_item[c], p = B.cc_pos[c];
-                const uint32_t L = lens[item >> 1], e = B.it_e[item];
-                uint32_t rl;
-                ws = window_start(p, L, e, ref_length, &rl);
+                ws = B.cc_ws[c];
+                meta = B.cc_meta[c];
+                const uint32_t item = B.cc_item[c];
                 if (ws == 0xffffffffu) {
                     B.vr_flag[c] = VR_INVALID;
                     B.vr_err[c] = SWM_MAXERROR;
                     B.vr_mloc[c] = -1;
+                } else if ((meta & 0xffu) < CH) { // shorter than a chunk: straight to the finishing pass
+                    fin0 = true;
+                    i = vp = vn = ones = 0;
                 } else {
                     act = true;
                     i = vp = vn = ones = 0;
-                    const int lh = (int)rl - (int)L; // last_high: cells 0 .. lh of the final scan
-                    meta = L | e << 8 | (uint32_t)(lh > 0 ? lh : 0) << 16;
                     const uint64_t q = ws >> 5;
                     a0 = pair_at(q);
                     a1 = pair_at(q + 1);
@@ -2385,15 +2402,12 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
                     nx = pair_at(q + 3);
                     rwp = reinterpret_cast<const uint2 *>(B.it_w + (uint64_t)item * 32);
                     rr = rwp[0];
-                    nrr = L > 32 ? rwp[1] : make_uint2(0u, 0u);
+                    nrr = (meta & 0xffu) > 32 ? rwp[1] : make_uint2(0u, 0u);
                 }
             }
         }
-        if (!__any_sync(0xffffffffu, act)) {
-            if (drained && qn >= qe) break;
-            continue;
-        }
-        bool fin = false, dead = false;
+        bool fin = fin0, dead = false;
+        fin0 = false;
         if (act) {
             const uint32_t L = meta & 0xffu, e = (meta >> 8) & 0xffu;
             const uint32_t MASK = (1u << (2 * e + 1)) - 1u, lhm = (1u << (meta >> 16)) - 1u;
@@ -2401,7 +2415,6 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
             const uint32_t xl0 = __funnelshift_r(a0.x, a1.x, sh), xl1 = __funnelshift_r(a1.x, a2.x, sh);
             const uint32_t xh0 = __funnelshift_r(a0.y, a1.y, sh), xh1 = __funnelshift_r(a1.y, a2.y, sh);
             const uint32_t rlw = rr.x >> (i & 31), rhw = rr.y >> (i & 31);
-            const uint32_t nst = min((uint32_t)CH, L - i);
             uint32_t acc = 0;
 #define SWM_STREAM_STEP(t)                                                                                        \
     {                                                                                                             \
@@ -2418,17 +2431,15 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
         vp = hn | ~(x | hp);                                                                                      \
         acc = __funnelshift_r(acc, d0, 1);                                                                        \
     }
-            if (nst == CH) {
 #pragma unroll
-                for (uint32_t t = 0; t < CH; t++) SWM_STREAM_STEP(t)
-            } else {
-                for (uint32_t t = 0; t < nst; t++) SWM_STREAM_STEP(t)
-            }
+            for (uint32_t t = 0; t < CH; t++) SWM_STREAM_STEP(t)
 #undef SWM_STREAM_STEP
             ones += __popc(acc);
-            i += nst;
-            nsteps += nst;
-            if (i >= L) {
+            i += CH;
+            nsteps += CH;
+            // a candidate with fewer than CH bases left goes to the finishing
+            // pass, which runs it from the first base: every chunk is whole
+            if (i + CH > L) {
                 fin = true;
             } else if ((int)(i - ones) - (int)__popc(vn & lhm) > (int)e) {
                 dead = true;
@@ -2451,8 +2462,10 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
             uint32_t at = 0;
             if (lane == leader) at = atomicAdd(&B.tot[TOT_VT], (uint32_t)__popc(fm));
             at = __shfl_sync(0xffffffffu, at, leader);
-            if (fin) {
-                B.vt_x[at + __popc(fm & lanemask_lt())] = make_uint2(c, 0u);
+            if (fin) { // the finishing pass resumes from this state
+                const uint32_t q = at + __popc(fm & lanemask_lt());
+                B.vt_x[q] = make_uint2(c, ones);
+                B.vt_st[q] = make_uint4(vp, vn, i, 0u);
                 act = false;
             }
         }
@@ -2463,9 +2476,122 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
             B.vr_flag[c] = VR_FAIL;
             act = false;
         }
+        if (drained && qn >= qe && !__any_sync(0xffffffffu, act)) break;
     }
     warp_add_u64(&B.stat[ST_CELLS], (unsigned long long)cells);
     warp_add_u64(&B.stat[ST_STEPS], (unsigned long long)nsteps);
+}
+
+// Finishing pass of the streaming form. Each queued candidate resumes from
+// the state k_verify_stream left (at most CH - 1 bases to go), then the final
+// scan (634-650); a passing candidate gets the Hamming check (252-287) and,
+// when that does not resolve it, a rerun from the first base that leaves the
+// traceback its (VP, VN) checkpoints, as the two-pass tail does.
+__global__ void __launch_bounds__(128, 8) k_verify_finish(const uint32_t *__restrict__ b2, uint64_t b2_words,
+                                                       uint64_t ref_length, MapBufs B, uint64_t cap_chunks,
+                                                       uint64_t cap_elems, uint64_t cap_cands, uint64_t cap_arena) {
+    if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint2 *__restrict__ b2p = reinterpret_cast<const uint2 *>(b2);
+    const uint64_t npairs = b2_words / 2;
+    auto pair_at = [&](uint64_t q) { return q < npairs ? b2p[q] : make_uint2(0u, 0u); };
+    const uint64_t n = B.tot[TOT_VT];
+    unsigned long long cells = 0, passed = 0, steps = 0;
+    for (;;) {
+        const uint32_t jb = warp_take(&B.tot[TOT_VTQ]);
+        if (jb >= n) break;
+        const uint64_t j = jb + (threadIdx.x & 31);
+        if (j >= n) continue;
+        const uint2 x = B.vt_x[j];
+        const uint4 st = B.vt_st[j];
+        const uint32_t c = x.x, i0 = st.z;
+        uint32_t ones = x.y, vp = st.x, vn = st.y;
+        const uint32_t item = B.cc_item[c], ws = B.cc_ws[c], meta = B.cc_meta[c];
+        const uint32_t L = meta & 0xffu, e = (meta >> 8) & 0xffu, rl = L + (meta >> 16);
+        const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
+        const uint32_t *RW = B.it_w + (uint64_t)item * 32;
+        {   // the last L - i0 < 32 bases
+            const uint32_t pos = ws + i0, sh = pos & 31;
+            const uint64_t q = pos >> 5;
+            const uint2 a0 = pair_at(q), a1 = pair_at(q + 1), a2 = pair_at(q + 2);
+            const uint32_t xl0 = __funnelshift_r(a0.x, a1.x, sh), xl1 = __funnelshift_r(a1.x, a2.x, sh);
+            const uint32_t xh0 = __funnelshift_r(a0.y, a1.y, sh), xh1 = __funnelshift_r(a1.y, a2.y, sh);
+            const uint32_t rb = i0 >> 5, rs = i0 & 31;
+            const uint32_t rlw = __funnelshift_r(RW[2 * rb], rb + 1 < 8 ? RW[2 * rb + 2] : 0u, rs);
+            const uint32_t rhw = __funnelshift_r(RW[2 * rb + 1], rb + 1 < 8 ? RW[2 * rb + 3] : 0u, rs);
+            uint32_t acc = 0;
+            for (uint32_t t = 0; t < L - i0; t++) {
+                const uint32_t wls = __funnelshift_r(xl0, xl1, t), whs = __funnelshift_r(xh0, xh1, t);
+                const uint32_t mL = 0u - ((rlw >> t) & 1u), mH = 0u - ((rhw >> t) & 1u);
+                const uint32_t eq = ~((wls ^ mL) | (whs ^ mH)) & MASK;
+                uint32_t xx = eq | vn;
+                const uint32_t d0 = ((vp + (xx & vp)) ^ vp) | xx;
+                const uint32_t hn = vp & d0;
+                const uint32_t hp = vn | ~(vp | d0);
+                xx = d0 >> 1;
+                vn = xx & hp;
+                vp = hn | ~(xx | hp);
+                acc = __funnelshift_r(acc, d0, 1);
+            }
+            ones += __popc(acc);
+            steps += L - i0;
+        }
+        int loc;
+        const int err = myers_final(vp, vn, ones, L, e, rl, &loc);
+        cells += (unsigned long long)L * (2 * e + 1);
+        B.vr_err[c] = err;
+        B.vr_mloc[c] = loc;
+        if (err > (int)e) {
+            B.vr_flag[c] = VR_FAIL;
+            continue;
+        }
+        passed++;
+        uint32_t WL[SWM_WIN_WORDS], WH[SWM_WIN_WORDS];
+        load_window(b2, b2_words, ws, L, e, WL, WH);
+        // Hamming shortcut (align_reads, 252-287)
+        const int start = loc - (int)L + 1;
+        int ham = 0;
+        for (uint32_t ii = 0; ii * 32 < L; ii++) {
+            uint32_t mask = 0xffffffffu;
+            if ((ii + 1) * 32 > L) mask >>= (32 - (L - ii * 32));
+            const uint32_t lref = swm_fsr(WL[ii], WL[ii + 1], (uint32_t)start);
+            const uint32_t href = swm_fsr(WH[ii], WH[ii + 1], (uint32_t)start);
+            const uint32_t xm = ((RW[16 + 2 * ii + 1] ^ href) | (RW[16 + 2 * ii] ^ lref)) & mask;
+            ham += __popc(xm);
+        }
+        uint8_t *slot = B.vr_cig + c * SWM_CIGAR_SLOT;
+        if (ham == err) {
+            uint8_t txt[8];
+            int nt = put_len(txt, L);
+            txt[nt++] = 'M';
+            slot[0] = (uint8_t)ham;
+            slot[1] = (uint8_t)nt;
+            for (int t = 0; t < nt; t++) slot[2 + t] = txt[t];
+            B.vr_tlen[c] = (uint16_t)nt;
+            B.vr_loc[c] = ws + (uint32_t)start + 1;
+            B.vr_flag[c] = VR_HAM;
+            continue;
+        }
+        // checkpoints for the traceback: the recurrence again from the first base
+        uint32_t rw[16];
+#pragma unroll
+        for (int t = 0; t < 16; t++) rw[t] = RW[t];
+        uint32_t cp[32];
+        uint32_t vp2 = 0, vn2 = 0, ones2 = 0;
+        const uint32_t nblk = (L + 31) >> 5;
+        myers_blocks(WL, WH, rw, L, MASK, 0, nblk, vp2, vn2, ones2, cp);
+        steps += L;
+        B.vr_loc[c] = ws; // window start, used by the traceback
+        B.vr_flag[c] = VR_NEEDTB;
+        const uint32_t at = atomicAdd(&B.tot[TOT_TB], 1u);
+        B.tb_list[at] = c;
+        uint4 *cpo = reinterpret_cast<uint4 *>(B.tb_cp + (uint64_t)at * 32);
+#pragma unroll
+        for (uint32_t kq = 0; kq < 8; kq++)
+            if (kq < nblk) cpo[kq] = make_uint4(cp[4 * kq], cp[4 * kq + 1], cp[4 * kq + 2], cp[4 * kq + 3]);
+    }
+    warp_add_u64(&B.stat[ST_CELLS], cells);
+    warp_add_u64(&B.stat[ST_PASSED], passed);
+    warp_add_u64(&B.stat[ST_STEPS], steps);
 }
 
 // Traceback of the passing candidates that the Hamming check did not resolve
@@ -3027,7 +3153,7 @@ static void free_bufs(MapBufs &B) {
     void *ps[] = {B.par, B.it_w, B.sel, B.sel_fl, B.sel_key, B.it_perm, B.unm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand, B.plan_list,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
-                  B.cc_item, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
+                  B.cc_item, B.cc_ws, B.cc_meta, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
                   B.tb_cp, B.slow_list, B.vt_x, B.vt_st, B.vt_cp,
                   B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
     for (void *p : ps) cudaFree(p);
@@ -3077,7 +3203,7 @@ static int alloc_work(swm_mapper *m) {
     m->gen++; // the captured graph holds the old buffers
     cudaFree(B.ch_g); cudaFree(B.ch_meta); cudaFree(B.plan_keys); cudaFree(B.bt_c0); cudaFree(B.bt_c1); cudaFree(B.bt_e0);
     cudaFree(B.bt_cnt); cudaFree(B.sort_scratch); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
-    cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
+    cudaFree(B.cc_item); cudaFree(B.cc_ws); cudaFree(B.cc_meta); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
     cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
     cudaFree(B.tb_list); cudaFree(B.tb_cp); cudaFree(B.slow_list); cudaFree(B.vt_x); cudaFree(B.vt_st); cudaFree(B.vt_cp);
     cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
@@ -3092,6 +3218,8 @@ static int alloc_work(swm_mapper *m) {
     rc |= dmalloc(&B.cand_ub, m->cap_elems);
     rc |= dmalloc(&B.cc_pos, m->cap_cands);
     rc |= dmalloc(&B.cc_item, m->cap_cands);
+    rc |= dmalloc(&B.cc_ws, m->cap_cands);
+    rc |= dmalloc(&B.cc_meta, m->cap_cands);
     rc |= dmalloc(&B.vr_flag, m->cap_cands);
     rc |= dmalloc(&B.vr_loc, m->cap_cands);
     rc |= dmalloc(&B.vr_err, m->cap_cands);
@@ -3229,7 +3357,8 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     rc = swm_exclusive_scan(B.it_nel, B.it_eloff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_ELEMS, st);
     if (rc) return rc;
     m->launches += 6;
-    k_plan_list<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks);
+    const bool table = ix->d_ctab_off && ix->k == K12;
+    k_plan_list<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks, !table);
     k_plan_lanes<<<grid_cap(ci, PLAN_LANE_WARPS * 32, 6), PLAN_LANE_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
                                                                                          m->cap_elems);
     k_plan<<<grid_cap(ci, PLAN_WARPS * 32, 16), PLAN_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
@@ -3237,7 +3366,7 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     m->launches += 3;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[2], st, cudaEventRecordExternal));
-    if (ix->d_ctab_off && ix->k == K12)
+    if (table)
         k_cand_table<<<cand_grid(m), CAND_WARPS * 32, 0, st>>>(ix->d_pos, ix->d_ls, ix->d_ctab_off, ix->d_ctab_pos, B,
                                                                m->cap_chunks, m->cap_elems, ix->k + SWM_SEED_STEP - 1);
     else
@@ -3249,7 +3378,7 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     rc = swm_exclusive_scan(B.it_ncand, B.it_coff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_CANDS, st);
     if (rc) return rc;
     m->launches += 3;
-    k_compact<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands);
+    k_compact<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands, ix->ref_length);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[4], st, cudaEventRecordExternal));
@@ -3260,8 +3389,8 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
             auto stream = m->vmode == VMODE_STREAM8 ? k_verify_stream<8> : k_verify_stream<16>;
             stream<<<grid_cap(m->cap_cands, 128, 10), 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks,
                                                                      m->cap_elems, m->cap_cands);
-            k_verify<false, 0><<<vg, 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks, m->cap_elems,
-                                                   m->cap_cands, m->cap_arena);
+            k_verify_finish<<<vg, 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks, m->cap_elems,
+                                                m->cap_cands, m->cap_arena);
         } else {
             auto head = m->vmode == VMODE_HEAD32 ? k_verify<true, 1> : k_verify<true, 2>;
             auto tail = m->vmode == VMODE_HEAD32 ? k_verify<false, 1> : k_verify<false, 2>;

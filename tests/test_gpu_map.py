@@ -56,9 +56,18 @@ def test_gpu_plain_1mbp(cuda_lib):
     assert st["candidates"] == ref.stats["candidates"]
     assert st["mapped_reads"] == ref.stats["mapped_reads"]
     # every passing candidate runs all 100 read bases through the recurrence;
-    # no candidate runs more
-    assert 100 * st["passed"] <= st["myers_steps"] <= 100 * st["candidates"]
-    assert st["myers_steps"] >= 64 * st["candidates"] // 2
+    # a candidate runs at most all of them, and (streaming form, the default)
+    # all of them once more when its traceback needs checkpoints
+    assert m.verify() == "stream16"
+    assert 100 * st["passed"] <= st["myers_steps"] <= 100 * (st["candidates"] + st["passed"])
+    assert st["myers_steps"] >= 16 * st["candidates"] // 2
+    # the two-pass form runs no candidate past its last base
+    m.set_verify("head64")
+    out2 = m.map(reads, lens, 5)
+    _check(out2, ref.records(), ref.unmapped)
+    st2 = m.stats()
+    assert 100 * st2["passed"] <= st2["myers_steps"] <= 100 * st2["candidates"]
+    assert st2["myers_steps"] >= 64 * st2["candidates"] // 2
 
 
 @pytest.mark.parametrize("table", [True, False])
