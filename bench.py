@@ -620,9 +620,13 @@ def run_gpu(args):
                              "gbs": round(byts / (t_ms / 1e3) / 1e9, 1) if t_ms > 0 else None,
                              "bytes_per_step": int(byts)}
     dom = max(STAGES, key=lambda s: per_step["ms_" + s])
+    # the verification kernels the blocks ran: streaming (k_verify_stream, then
+    # k_verify_finish) or the two passes of k_verify
+    streaming = all(hd.startswith("stream") for _, _, hd in blocks)
+    vkern = "k_verify_stream" if streaming else "k_verify"
     kern = {"seed": "k_seed12" if w["k"] == 12 else "k_seed", "plan": "k_plan",
             "candidates": "k_cand_table" if table else "k_cand", "compact": "k_compact",
-            "verify": "k_verify", "traceback": "k_traceback", "records": "k_records"}[dom]
+            "verify": vkern, "traceback": "k_traceback", "records": "k_records"}[dom]
     launches_per_step = per_step["blocks"]
     avg_launch_s = per_step["ms_" + dom] / 1e3 / launches_per_step
     alg_bytes_launch = stage_bytes(dom, per_step, L, e, table) / launches_per_step
@@ -630,7 +634,7 @@ def run_gpu(args):
     tr = profile_traffic(kern)
     traffic = None
     if tr:
-        unit_key = {"k_verify": "candidates", "k_cand": "fetched", "k_cand_table": "items", "k_seed": "items",
+        unit_key = {"k_verify": "candidates", "k_verify_stream": "candidates", "k_cand": "fetched", "k_cand_table": "items", "k_seed": "items",
                     "k_seed12": "items",
                     "k_plan": "chunks", "k_traceback": "passed"}.get(kern)
         for key, val in tr.items():
@@ -676,11 +680,15 @@ def run_gpu(args):
     int_peak = 152 * 64 * sm_mhz * 1e6 / 1e12
     myers_ops = per_step["myers_steps"] * 21
     t_verify = per_step["ms_verify"] / 1e3
-    int_pipe = {"kernel": "k_verify", "ops_per_step": int(myers_ops), "achieved_tops": round(myers_ops / t_verify / 1e12, 2)
+    int_pipe = {"kernel": vkern, "ops_per_step": int(myers_ops), "achieved_tops": round(myers_ops / t_verify / 1e12, 2)
                 if t_verify > 0 else None, "peak_tops": round(int_peak, 2),
                 "frac": round(myers_ops / t_verify / 1e12 / int_peak, 4) if t_verify > 0 else None,
                 "ops_model": "21 int ops per executed Myers step (17 recurrence + 4 pattern word), steps counted "
-                             "on the device over both passes (the head stops hopeless candidates after 64 bases)",
+                             "on the device over all verification kernels ("
+                             + ("streaming: each lane stops its candidate at the first 16-base chunk whose band bound "
+                                "exceeds e; the finishing kernel runs the last bases and reruns tracebacks"
+                                if streaming else
+                                "two passes: the head stops hopeless candidates after 64 bases") + ")",
                 "peak_model": "152 SMs x 64 ALU-pipe lanes (16 per sub-partition) x median SM clock under load"}
 
     line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,

@@ -125,7 +125,6 @@ struct MapBufs {
     uint32_t *cand_ub;
     // dense candidates (cap_cands)
     uint32_t *cc_pos, *cc_item;
-    uint32_t *cc_ws, *cc_meta; // window start (0xffffffff: invalid) and L | e << 8 | max(last_high, 0) << 16
     uint8_t *vr_flag;
     uint32_t *vr_loc;
     int32_t *vr_err, *vr_mloc;
@@ -1903,21 +1902,8 @@ __global__ void __launch_bounds__(CAND_WARPS * 32, CAND_MIN_BLOCKS)
 // Dense candidate list: item by item, batch by batch, in verification order.
 #define COMPACT_HEAVY 16 // candidates above which an item is copied by its whole warp
 
-// Each candidate also gets its window start and (L, e, last_high) for the
-// streaming verification (window_start, adjust_ref_len 1403-1435).
-__device__ __forceinline__ uint32_t window_start(uint32_t base_pos, uint32_t L, uint32_t e, uint64_t ref_length,
-                                                 uint32_t *rl_out);
-__device__ __forceinline__ void put_window(MapBufs &B, uint64_t o, uint32_t p, uint32_t L, uint32_t e,
-                                           uint64_t ref_length) {
-    uint32_t rl;
-    const uint32_t ws = window_start(p, L, e, ref_length, &rl);
-    const int lh = (int)rl - (int)L;
-    B.cc_ws[o] = ws;
-    B.cc_meta[o] = L | e << 8 | (uint32_t)(lh > 0 ? lh : 0) << 16;
-}
-
 __global__ void __launch_bounds__(256) k_compact(MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
-                                                 uint64_t cap_cands, uint64_t ref_length) {
+                                                 uint64_t cap_cands) {
     const uint32_t nitems = B.par->nitems;
     if (B.tot[TOT_FLAGS] != 0 || B.tot[TOT_CHUNKS] > cap_chunks || B.tot[TOT_ELEMS] > cap_elems) return;
     const uint32_t lane = lane_id();
@@ -1943,16 +1929,13 @@ __global__ void __launch_bounds__(256) k_compact(MapBufs B, uint64_t cap_chunks,
             }
             heavy = nb && nc > COMPACT_HEAVY;
             if (nb && !heavy) {
-                const uint32_t L = B.par->lens[item >> 1], e = B.it_e[item];
                 uint32_t o = o0;
                 for (uint32_t b = 0; b < nb; b++) {
                     const uint32_t n = nref ? B.bt_cnt[sbase + b] : nc; // one batch when there are no refills
                     const uint32_t e0 = nref ? B.bt_e0[sbase + b] : eloff;
                     for (uint32_t j = 0; j < n; j++) {
-                        const uint32_t p = B.cand_ub[e0 + j];
-                        B.cc_pos[o + j] = p;
+                        B.cc_pos[o + j] = B.cand_ub[e0 + j];
                         B.cc_item[o + j] = item;
-                        put_window(B, o + j, p, L, e, ref_length);
                     }
                     o += n;
                 }
@@ -1966,15 +1949,12 @@ __global__ void __launch_bounds__(256) k_compact(MapBufs B, uint64_t cap_chunks,
             const uint32_t hnc = __shfl_sync(0xffffffffu, nc, src), hsb = __shfl_sync(0xffffffffu, sbase, src);
             const uint32_t hel = __shfl_sync(0xffffffffu, eloff, src);
             uint32_t o = __shfl_sync(0xffffffffu, o0, src);
-            const uint32_t hit = item0 + src, hL = B.par->lens[hit >> 1], he = B.it_e[hit];
             for (uint32_t b = 0; b < hnb; b++) {
                 const uint32_t n = hnref ? B.bt_cnt[hsb + b] : hnc;
                 const uint32_t e0 = hnref ? B.bt_e0[hsb + b] : hel;
                 for (uint32_t j = lane; j < n; j += 32) {
-                    const uint32_t p = B.cand_ub[e0 + j];
-                    B.cc_pos[o + j] = p;
-                    B.cc_item[o + j] = hit;
-                    put_window(B, o + j, p, hL, he, ref_length);
+                    B.cc_pos[o + j] = B.cand_ub[e0 + j];
+                    B.cc_item[o + j] = item0 + src;
                 }
                 o += n;
             }
@@ -2382,9 +2362,12 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
             }
             if (!act && j != 0xffffffffu) {
                 c = j;
-                ws = B.cc_ws[c];
-                meta = B.cc_meta[c];
-                const uint32_t item = B.cc_item[c];
+                const uint32_t item = B.cc_item[c], p = B.cc_pos[c];
+                const uint32_t L = B.par->lens[item >> 1], e = B.it_e[item];
+                uint32_t rl;
+                ws = window_start(p, L, e, ref_length, &rl);
+                const int lh = (int)rl - (int)L; // last_high: cells 0 .. lh of the final scan
+                meta = L | e << 8 | (uint32_t)(lh > 0 ? lh : 0) << 16;
                 if (ws == 0xffffffffu) {
                     B.vr_flag[c] = VR_INVALID;
                     B.vr_err[c] = SWM_MAXERROR;
@@ -2505,8 +2488,9 @@ __global__ void __launch_bounds__(128, 8) k_verify_finish(const uint32_t *__rest
         const uint4 st = B.vt_st[j];
         const uint32_t c = x.x, i0 = st.z;
         uint32_t ones = x.y, vp = st.x, vn = st.y;
-        const uint32_t item = B.cc_item[c], ws = B.cc_ws[c], meta = B.cc_meta[c];
-        const uint32_t L = meta & 0xffu, e = (meta >> 8) & 0xffu, rl = L + (meta >> 16);
+        const uint32_t item = B.cc_item[c], L = B.par->lens[item >> 1], e = B.it_e[item];
+        uint32_t rl;
+        const uint32_t ws = window_start(B.cc_pos[c], L, e, ref_length, &rl);
         const uint32_t MASK = (1u << (2 * e + 1)) - 1u;
         const uint32_t *RW = B.it_w + (uint64_t)item * 32;
         {   // the last L - i0 < 32 bases
@@ -3153,7 +3137,7 @@ static void free_bufs(MapBufs &B) {
     void *ps[] = {B.par, B.it_w, B.sel, B.sel_fl, B.sel_key, B.it_perm, B.unm, B.it_nsel, B.it_e, B.it_nch, B.it_nel, B.it_nbat,
                   B.it_choff, B.it_eloff, B.it_nrec, B.it_nw, B.it_nb, B.it_recoff, B.it_woff, B.it_boff, B.it_ncand, B.plan_list,
                   B.it_coff, B.ch_g, B.ch_meta, B.bt_c0, B.bt_c1, B.bt_e0, B.bt_cnt, B.sort_scratch, B.cand_ub, B.cc_pos,
-                  B.cc_item, B.cc_ws, B.cc_meta, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
+                  B.cc_item, B.plan_keys, B.vr_flag, B.vr_loc, B.vr_err, B.vr_mloc, B.vr_tlen, B.vr_cig, B.vr_aoff, B.arena, B.tb_list,
                   B.tb_cp, B.slow_list, B.vt_x, B.vt_st, B.vt_cp,
                   B.out_w, B.out_c, B.rec_woff, B.rec_boff, B.rec_blen, B.tot, B.stat, B.scan_tmp};
     for (void *p : ps) cudaFree(p);
@@ -3203,7 +3187,7 @@ static int alloc_work(swm_mapper *m) {
     m->gen++; // the captured graph holds the old buffers
     cudaFree(B.ch_g); cudaFree(B.ch_meta); cudaFree(B.plan_keys); cudaFree(B.bt_c0); cudaFree(B.bt_c1); cudaFree(B.bt_e0);
     cudaFree(B.bt_cnt); cudaFree(B.sort_scratch); cudaFree(B.cand_ub); cudaFree(B.cc_pos);
-    cudaFree(B.cc_item); cudaFree(B.cc_ws); cudaFree(B.cc_meta); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
+    cudaFree(B.cc_item); cudaFree(B.vr_flag); cudaFree(B.vr_loc); cudaFree(B.vr_err); cudaFree(B.vr_mloc);
     cudaFree(B.vr_tlen); cudaFree(B.vr_cig); cudaFree(B.vr_aoff); cudaFree(B.arena); cudaFree(B.out_w);
     cudaFree(B.tb_list); cudaFree(B.tb_cp); cudaFree(B.slow_list); cudaFree(B.vt_x); cudaFree(B.vt_st); cudaFree(B.vt_cp);
     cudaFree(B.out_c); cudaFree(B.rec_woff); cudaFree(B.rec_boff); cudaFree(B.rec_blen); cudaFree(B.scan_tmp);
@@ -3218,8 +3202,6 @@ static int alloc_work(swm_mapper *m) {
     rc |= dmalloc(&B.cand_ub, m->cap_elems);
     rc |= dmalloc(&B.cc_pos, m->cap_cands);
     rc |= dmalloc(&B.cc_item, m->cap_cands);
-    rc |= dmalloc(&B.cc_ws, m->cap_cands);
-    rc |= dmalloc(&B.cc_meta, m->cap_cands);
     rc |= dmalloc(&B.vr_flag, m->cap_cands);
     rc |= dmalloc(&B.vr_loc, m->cap_cands);
     rc |= dmalloc(&B.vr_err, m->cap_cands);
@@ -3378,7 +3360,7 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     rc = swm_exclusive_scan(B.it_ncand, B.it_coff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_CANDS, st);
     if (rc) return rc;
     m->launches += 3;
-    k_compact<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands, ix->ref_length);
+    k_compact<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks, m->cap_elems, m->cap_cands);
     m->launches++;
     LAUNCH_CHECK();
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[4], st, cudaEventRecordExternal));
