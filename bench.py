@@ -622,8 +622,9 @@ def run_gpu(args):
     dom = max(STAGES, key=lambda s: per_step["ms_" + s])
     # the verification kernels the blocks ran: streaming (k_verify_stream, then
     # k_verify_finish) or the two passes of k_verify
-    streaming = all(hd.startswith("stream") for _, _, hd in blocks)
-    vkern = "k_verify_stream" if streaming else "k_verify"
+    streaming = all(hd.startswith(("stream", "pair")) for _, _, hd in blocks)
+    vkern = ("k_verify_pair" if all(hd == "pair16" for _, _, hd in blocks) and eper is None and E <= 7
+             else "k_verify_stream") if streaming else "k_verify"
     kern = {"seed": "k_seed12" if w["k"] == 12 else "k_seed", "plan": "k_plan",
             "candidates": "k_cand_table" if table else "k_cand", "compact": "k_compact",
             "verify": vkern, "traceback": "k_traceback", "records": "k_records"}[dom]
@@ -997,7 +998,7 @@ def main():
                     help="reads of the timed workload compared with the reference's own mapper after the timing")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--requests", type=int, default=None, help="requests of the serving workload")
-    ap.add_argument("--verify", choices=["head64", "head32", "stream8", "stream16"], default="stream16",
+    ap.add_argument("--verify", choices=["head64", "head32", "stream8", "stream16", "pair16"], default="stream16",
                     help="form of the verification stage when the autotuner does not choose it per length bucket")
     ap.add_argument("--table", type=int, default=1,
                     help="keep the index's candidate table (1) or drop it before the mappers are made (0)")

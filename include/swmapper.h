@@ -237,6 +237,10 @@ typedef struct {
                                    8 / 16 bases, refilled from the queue as
                                    candidates stop (verify_head_bases is then
                                    ignored)                                       */
+    uint32_t verify_pairs;      /* 1 (with verify_chunk 16): two candidates per lane
+                                   in 15-bit halves of each word, for blocks whose
+                                   thresholds are all <= 7 (others run with one per
+                                   lane); 0: one per lane                         */
 } swm_tuning;
 
 /* Apply *set (may be NULL) and report the current settings in *get (may be

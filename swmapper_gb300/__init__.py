@@ -84,11 +84,12 @@ _lib = None
 
 class Tuning(C.Structure):
     """swm_tuning (include/swmapper.h)."""
-    _fields_ = [("verify_head_bases", C.c_uint32), ("verify_chunk", C.c_uint32)]
+    _fields_ = [("verify_head_bases", C.c_uint32), ("verify_chunk", C.c_uint32), ("verify_pairs", C.c_uint32)]
 
 
-# verification forms: name -> (verify_head_bases, verify_chunk)
-VERIFY_MODES = {"head32": (32, 0), "head64": (64, 0), "stream8": (64, 8), "stream16": (64, 16)}
+# verification forms: name -> (verify_head_bases, verify_chunk, verify_pairs)
+VERIFY_MODES = {"head32": (32, 0, 0), "head64": (64, 0, 0), "stream8": (64, 8, 0), "stream16": (64, 16, 0),
+                "pair16": (64, 16, 1)}
 
 
 def lib():
@@ -325,19 +326,21 @@ class Mapper:
     def set_verify(self, mode: str) -> None:
         """Form of the verification stage (swm_mapper_tuning): "head32" /
         "head64" (a first pass over that many bases of every candidate, then
-        the rest), or "stream8" / "stream16" (each lane runs its own candidate
-        and tests the stop bound every 8 / 16 bases). Results never change."""
+        the rest), "stream8" / "stream16" (each lane runs its own candidate
+        and tests the stop bound every 8 / 16 bases) or "pair16" (two
+        candidates per lane when every threshold is <= 7). Results never
+        change."""
         if mode not in VERIFY_MODES:
             raise SwmError(f"unknown verification form {mode!r} (one of {', '.join(VERIFY_MODES)})", -1)
-        head, chunk = VERIFY_MODES[mode]
-        t = Tuning(verify_head_bases=head, verify_chunk=chunk)
+        head, chunk, pairs = VERIFY_MODES[mode]
+        t = Tuning(verify_head_bases=head, verify_chunk=chunk, verify_pairs=pairs)
         _check(lib().swm_mapper_tuning(self._h, C.byref(t), None), "swm_mapper_tuning")
 
     def verify(self) -> str:
         t = Tuning()
         _check(lib().swm_mapper_tuning(self._h, None, C.byref(t)), "swm_mapper_tuning")
-        for name, (head, chunk) in VERIFY_MODES.items():
-            if chunk == t.verify_chunk and (chunk or head == t.verify_head_bases):
+        for name, (head, chunk, pairs) in VERIFY_MODES.items():
+            if chunk == t.verify_chunk and pairs == t.verify_pairs and (chunk or head == t.verify_head_bases):
                 return name
         raise SwmError(f"unexpected tuning {t.verify_head_bases}/{t.verify_chunk}", -1)
 

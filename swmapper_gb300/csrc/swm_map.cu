@@ -154,8 +154,10 @@ struct MapBufs {
 // results. HEAD32 / HEAD64: a head pass over the first 32 / 64 bases of every
 // candidate, then a tail pass over the ones still alive. STREAM8 / STREAM16:
 // k_verify_stream with its stop test every 8 / 16 bases, then the finishing
-// pass.
-enum { VMODE_HEAD32 = 0, VMODE_HEAD64, VMODE_STREAM8, VMODE_STREAM16, VMODE_N };
+// pass. PAIR16: k_verify_pair (two candidates per lane, stop test every 16
+// bases), then the finishing pass; a block that may hold a threshold above 7
+// (per-read thresholds, or e > 7) runs STREAM16 instead.
+enum { VMODE_HEAD32 = 0, VMODE_HEAD64, VMODE_STREAM8, VMODE_STREAM16, VMODE_PAIR16, VMODE_N };
 
 struct swm_mapper {
     swm_index *ix;
@@ -2465,6 +2467,191 @@ __global__ void __launch_bounds__(128, 10) k_verify_stream(const uint32_t *__res
     warp_add_u64(&B.stat[ST_STEPS], (unsigned long long)nsteps);
 }
 
+// Streaming verification with two candidates per lane (every e <= 7). The
+// band of e <= 7 is at most 15 bits, and the recurrence run in a 15-bit lane
+// gives the same band, D0 bit 0 and state as in a 32-bit one, so a lane packs
+// candidate A in bits 0..14 and B in bits 16..30 of one word. Bits 15 and 31
+// are guards kept at 0 in VP, VN and X & VP, so the carry of VP + (X & VP)
+// out of a half stops in its guard; D0 is masked to the halves (the carry
+// would otherwise enter the top bit of X through D0 >> 1) and VN after the
+// shift (bit 15 gets B's bit 0); VP's guards then stay 0 by themselves. The
+// step costs 10 logic ops for both candidates plus their pattern words: each
+// half's window bits by funnel shift and one byte permute, the read bases as
+// all-ones / all-zeros per half by the permute's sign replication. Each half
+// stops, finishes and refills on its own exactly as in k_verify_stream, and
+// its state goes to k_verify_finish as a 32-bit lane (the same continuation).
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
+    return d;
+}
+
+// Next n work units of a warp from a device work queue (head *q).
+__device__ __forceinline__ uint32_t warp_take_n(uint32_t *q, uint32_t n) {
+    uint32_t b = 0;
+    if ((threadIdx.x & 31) == 0) b = atomicAdd(q, n);
+    return __shfl_sync(0xffffffffu, b, 0);
+}
+
+template <int CH>
+__global__ void __launch_bounds__(128, 10) k_verify_pair(const uint32_t *__restrict__ b2, uint64_t b2_words,
+                                                         uint64_t ref_length, MapBufs B, uint64_t cap_chunks,
+                                                         uint64_t cap_elems, uint64_t cap_cands) {
+    static_assert(CH == 16, "a chunk is 16 read bases: one halfword of read bits per half");
+    if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
+    const uint2 *__restrict__ b2p = reinterpret_cast<const uint2 *>(b2);
+    const uint64_t npairs = b2_words / 2;
+    auto pair_at = [&](uint64_t q) { return q < npairs ? b2p[q] : make_uint2(0u, 0u); };
+    const uint64_t nc_all = B.tot[TOT_CANDS];
+    const uint32_t n = (uint32_t)(nc_all < cap_cands ? nc_all : cap_cands);
+    const uint32_t lane = lane_id();
+    uint32_t cells = 0, nsteps = 0; // per lane, both halves
+    uint32_t qn = 0, qe = 0;        // the warp's queue entries not handed out yet
+    bool drained = false;
+    bool act[2] = {false, false};
+    // per half: candidate, L | e << 8 | max(last_high, 0) << 16, bases done, window start, item, D0 bit-0 count
+    uint32_t c[2] = {0, 0}, meta[2] = {0, 0}, i[2] = {0, 0}, ws[2] = {0, 0}, item[2] = {0, 0}, ones[2] = {0, 0};
+    uint32_t vp = 0, vn = 0, PM = 0; // packed state and band masks
+    for (;;) {
+        const unsigned needA = __ballot_sync(0xffffffffu, !act[0]), needB = __ballot_sync(0xffffffffu, !act[1]);
+        bool fin[2] = {false, false}, dead[2] = {false, false};
+        if (needA | needB) {
+            const uint32_t na = __popc(needA), k = na + __popc(needB), avail = qe - qn;
+            uint32_t jb = qe, je = qe;
+            if (k > avail && !drained) {
+                const uint32_t t = warp_take_n(&B.tot[TOT_VQ], 64u);
+                if (t >= n) {
+                    drained = true;
+                } else {
+                    jb = t;
+                    je = min(t + 64u, n);
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (act[h]) continue;
+                const uint32_t r = h == 0 ? __popc(needA & lanemask_lt()) : na + __popc(needB & lanemask_lt());
+                uint32_t j = 0xffffffffu;
+                if (r < avail) j = qn + r;
+                else if (jb + (r - avail) < je) j = jb + (r - avail);
+                if (j == 0xffffffffu) continue;
+                c[h] = j;
+                const uint32_t it = B.cc_item[j], p = B.cc_pos[j];
+                const uint32_t L = B.par->lens[it >> 1], e = B.it_e[it];
+                uint32_t rl;
+                const uint32_t w = window_start(p, L, e, ref_length, &rl);
+                const uint32_t hm = h ? 0xffff0000u : 0x0000ffffu;
+                vp &= ~hm;
+                vn &= ~hm;
+                PM &= ~hm;
+                ones[h] = 0;
+                i[h] = 0;
+                if (w == 0xffffffffu) {
+                    B.vr_flag[j] = VR_INVALID;
+                    B.vr_err[j] = SWM_MAXERROR;
+                    B.vr_mloc[j] = -1;
+                    continue;
+                }
+                const int lh = (int)rl - (int)L;
+                meta[h] = L | e << 8 | (uint32_t)(lh > 0 ? lh : 0) << 16;
+                ws[h] = w;
+                item[h] = it;
+                if (L < CH) { // shorter than a chunk: straight to the finishing pass
+                    fin[h] = true;
+                } else {
+                    act[h] = true;
+                    PM |= ((1u << (2 * e + 1)) - 1u) << (16 * h);
+                }
+            }
+            if (k <= avail) {
+                qn += k;
+            } else {
+                qn = min(jb + (k - avail), je);
+                qe = je;
+            }
+        }
+        if (act[0] || act[1]) {
+            uint32_t xl0[2], xl1[2], xh0[2], xh1[2], rb[2][2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) { // window bits and read bits of the chunk (inactive half: zeros)
+                const uint32_t pos = ws[h] + i[h], sh = pos & 31;
+                uint2 a0 = make_uint2(0u, 0u), a1 = a0, a2 = a0, rr = a0;
+                if (act[h]) {
+                    const uint64_t q = pos >> 5;
+                    a0 = pair_at(q);
+                    a1 = pair_at(q + 1);
+                    a2 = pair_at(q + 2);
+                    rr = reinterpret_cast<const uint2 *>(B.it_w + (uint64_t)item[h] * 32)[i[h] >> 5];
+                }
+                xl0[h] = __funnelshift_r(a0.x, a1.x, sh);
+                xl1[h] = __funnelshift_r(a1.x, a2.x, sh);
+                xh0[h] = __funnelshift_r(a0.y, a1.y, sh);
+                xh1[h] = __funnelshift_r(a1.y, a2.y, sh);
+                // read base t of the chunk at bit 15 - t of the half (bit reverse of the low halfword)
+                rb[h][0] = __brev((rr.x >> (i[h] & 31)) & 0xffffu);
+                rb[h][1] = __brev((rr.y >> (i[h] & 31)) & 0xffffu);
+            }
+            // A's reversed bits in 15..0, B's in 31..16
+            const uint32_t RL = prmt(rb[0][0], rb[1][0], 0x7632u), RH = prmt(rb[0][1], rb[1][1], 0x7632u);
+            uint32_t acc = 0;
+#pragma unroll
+            for (uint32_t t = 0; t < CH; t++) {
+                const uint32_t wl = prmt(__funnelshift_r(xl0[0], xl1[0], t), __funnelshift_r(xl0[1], xl1[1], t), 0x5410u);
+                const uint32_t wh = prmt(__funnelshift_r(xh0[0], xh1[0], t), __funnelshift_r(xh0[1], xh1[1], t), 0x5410u);
+                // read base t of each half as all-ones / all-zeros: the sign of bytes 1 and 3
+                const uint32_t mL = prmt(RL << t, 0u, 0xbb99u), mH = prmt(RH << t, 0u, 0xbb99u);
+                const uint32_t eq = ~((wl ^ mL) | (wh ^ mH)) & PM;
+                uint32_t x = eq | vn;
+                const uint32_t d0 = (((vp + (x & vp)) ^ vp) | x) & 0x7fff7fffu;
+                const uint32_t hn = vp & d0;
+                const uint32_t hp = vn | ~(vp | d0);
+                x = d0 >> 1;
+                vn = x & hp & 0x7fff7fffu;
+                vp = hn | ~(x | hp);
+                acc += d0 & 0x00010001u;
+            }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (!act[h]) continue;
+                ones[h] += h ? acc >> 16 : acc & 0xffffu;
+                i[h] += CH;
+                nsteps += CH;
+                const uint32_t L = meta[h] & 0xffu, e = (meta[h] >> 8) & 0xffu;
+                const uint32_t vnh = (vn >> (16 * h)) & 0x7fffu, lhm = (1u << (meta[h] >> 16)) - 1u;
+                if (i[h] + CH > L) fin[h] = true;
+                else if ((int)(i[h] - ones[h]) - (int)__popc(vnh & lhm) > (int)e) dead[h] = true;
+            }
+        }
+        const unsigned fA = __ballot_sync(0xffffffffu, fin[0]), fB = __ballot_sync(0xffffffffu, fin[1]);
+        if (fA | fB) {
+            const uint32_t leader = __ffs(fA | fB) - 1;
+            uint32_t at = 0;
+            if (lane == leader) at = atomicAdd(&B.tot[TOT_VT], (uint32_t)(__popc(fA) + __popc(fB)));
+            at = __shfl_sync(0xffffffffu, at, leader);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (!fin[h]) continue;
+                const uint32_t q = at + (h == 0 ? __popc(fA & lanemask_lt()) : __popc(fA) + __popc(fB & lanemask_lt()));
+                B.vt_x[q] = make_uint2(c[h], ones[h]);
+                B.vt_st[q] = make_uint4((vp >> (16 * h)) & 0x7fffu, (vn >> (16 * h)) & 0x7fffu, i[h], 0u);
+                act[h] = false;
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (!dead[h]) continue;
+            cells += (meta[h] & 0xffu) * (2 * ((meta[h] >> 8) & 0xffu) + 1);
+            B.vr_err[c[h]] = SWM_MAXERROR;
+            B.vr_mloc[c[h]] = -1;
+            B.vr_flag[c[h]] = VR_FAIL;
+            act[h] = false;
+        }
+        if (drained && qn >= qe && !__any_sync(0xffffffffu, act[0] || act[1])) break;
+    }
+    warp_add_u64(&B.stat[ST_CELLS], (unsigned long long)cells);
+    warp_add_u64(&B.stat[ST_STEPS], (unsigned long long)nsteps);
+}
+
 // Finishing pass of the streaming form. Each queued candidate resumes from
 // the state k_verify_stream left (at most CH - 1 bases to go), then the final
 // scan (634-650); a passing candidate gets the Hamming check (252-287) and,
@@ -3310,7 +3497,7 @@ extern "C" void swm_mapper_free(swm_mapper *m) {
 // The whole pipeline of one block on st, every size read on the device (the
 // grids cover the buffers' capacity; kernels loop over what the block has).
 // Captured into the mapper's graph; gclass picks the seed kernel.
-static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
+static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass, int vmode) {
     MapBufs &B = m->b;
     const uint32_t *d_n = &B.par->nitems;
     const uint64_t ci = m->cap_items;
@@ -3367,15 +3554,16 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass) {
     {
         const unsigned vg = grid_cap(m->cap_cands, 128, 16);
         const uint64_t nw = ix->n_words2 + SWM_PAD_WORDS;
-        if (m->vmode == VMODE_STREAM8 || m->vmode == VMODE_STREAM16) {
-            auto stream = m->vmode == VMODE_STREAM8 ? k_verify_stream<8> : k_verify_stream<16>;
+        if (vmode == VMODE_STREAM8 || vmode == VMODE_STREAM16 || vmode == VMODE_PAIR16) {
+            auto stream = vmode == VMODE_STREAM8 ? k_verify_stream<8>
+                          : vmode == VMODE_STREAM16 ? k_verify_stream<16> : k_verify_pair<16>;
             stream<<<grid_cap(m->cap_cands, 128, 10), 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks,
                                                                      m->cap_elems, m->cap_cands);
             k_verify_finish<<<vg, 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks, m->cap_elems,
                                                 m->cap_cands, m->cap_arena);
         } else {
-            auto head = m->vmode == VMODE_HEAD32 ? k_verify<true, 1> : k_verify<true, 2>;
-            auto tail = m->vmode == VMODE_HEAD32 ? k_verify<false, 1> : k_verify<false, 2>;
+            auto head = vmode == VMODE_HEAD32 ? k_verify<true, 1> : k_verify<true, 2>;
+            auto tail = vmode == VMODE_HEAD32 ? k_verify<false, 1> : k_verify<false, 2>;
             head<<<vg, 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
                                      m->cap_arena);
             tail<<<vg, 128, 0, st>>>(ix->d_b2, nw, ix->ref_length, B, m->cap_chunks, m->cap_elems, m->cap_cands,
@@ -3433,12 +3621,12 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
     P->nitems = 2 * nreads;
     P->errors = errors;
     P->pad = 0;
-    const int h = m->vmode;
+    const int h = m->vmode == VMODE_PAIR16 && (d_e || errors > 7) ? VMODE_STREAM16 : m->vmode;
     if (!m->gx[gclass][h] || m->gx_gen[gclass][h] != m->gen || m->gx_tab[gclass][h] != m->ix->ctab_gen) {
         drop_graph(m, gclass, h);
         cudaGraph_t g = nullptr;
         SWM_CUDA(cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal));
-        const int rc = enqueue_ops(m, m->st, gclass);
+        const int rc = enqueue_ops(m, m->st, gclass, h);
         const cudaError_t ce = cudaStreamEndCapture(m->st, &g);
         if (rc != SWM_OK || ce != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -3923,7 +4111,13 @@ extern "C" int swm_mapper_tuning(swm_mapper *m, const swm_tuning *set, swm_tunin
     if (!m) return SWM_ERR_ARG;
     if (set) {
         int mode;
-        if (set->verify_chunk == 8) mode = VMODE_STREAM8;
+        if (set->verify_pairs > 1 || (set->verify_pairs && set->verify_chunk != 16)) {
+            swm_set_error("swm_mapper_tuning: verify_pairs must be 0, or 1 with verify_chunk 16 (got %u, %u)",
+                          set->verify_pairs, set->verify_chunk);
+            return SWM_ERR_ARG;
+        }
+        if (set->verify_pairs) mode = VMODE_PAIR16;
+        else if (set->verify_chunk == 8) mode = VMODE_STREAM8;
         else if (set->verify_chunk == 16) mode = VMODE_STREAM16;
         else if (set->verify_chunk != 0) {
             swm_set_error("swm_mapper_tuning: verify_chunk must be 0, 8 or 16 (got %u)", set->verify_chunk);
@@ -3939,7 +4133,8 @@ extern "C" int swm_mapper_tuning(swm_mapper *m, const swm_tuning *set, swm_tunin
     }
     if (get) {
         get->verify_head_bases = m->vmode == VMODE_HEAD32 ? 32u : 64u;
-        get->verify_chunk = m->vmode == VMODE_STREAM8 ? 8u : m->vmode == VMODE_STREAM16 ? 16u : 0u;
+        get->verify_chunk = m->vmode == VMODE_STREAM8 ? 8u : m->vmode >= VMODE_STREAM16 ? 16u : 0u;
+        get->verify_pairs = m->vmode == VMODE_PAIR16 ? 1u : 0u;
     }
     return SWM_OK;
 }

@@ -16,7 +16,8 @@ so reads of very different lengths side by side waste lanes. The autotuner
   candidate with an exact stop test, then the rest ("head64", "head32"), or
   lanes that each run their own candidate and test a stop bound every 8 or
   16 bases, taking the next candidate as soon as theirs stops ("stream8",
-  "stream16"). Which is faster depends on how early the candidates of that
+  "stream16"), or two such candidates per lane when every threshold is <= 7
+  ("pair16"). Which is faster depends on how early the candidates of that
   read length can be ruled out, against the per-chunk cost of the test.
 
 Results do not depend on any choice: every read maps the same in any block
@@ -32,7 +33,7 @@ import numpy as np
 BUCKET_BP = 32
 BLOCKS = (65536, 131072, 262144, 524288)
 MAPPERS = (1, 2, 3)
-VERIFY = ("head64", "head32", "stream8", "stream16")  # forms of the verification stage
+VERIFY = ("head64", "head32", "stream8", "stream16", "pair16")  # forms of the verification stage
 BUCKET_BLOCKS = (131072, 524288)  # reads per block tried for each length bucket
 
 _cache: dict = {}

@@ -393,10 +393,11 @@ def test_gpu_mapping_other_seed_lengths(cuda_lib, k, e):
     assert m.stats()["candidates"] == ref.stats["candidates"]
 
 
-@pytest.mark.parametrize("mode", ["head32", "head64", "stream8", "stream16"])
+@pytest.mark.parametrize("mode", ["head32", "head64", "stream8", "stream16", "pair16"])
 def test_gpu_verify_forms(cuda_lib, mode):
     """The form of the verification stage (an autotuner knob) changes no
-    result: reads of 50-250 bp, per-read e up to 13, against the oracle."""
+    result: reads of 50-250 bp, per-read e up to 13 (the two-per-lane form
+    runs these blocks one per lane), against the oracle."""
     g = genome(2_000_000, 90, "human", nrun_min=2000, nrun_max=20000, copies_per_family=200)
     reads, lens, _, _ = synth.reads(g, 3000, 50, 250, 0.04, seed=91, stride=250)
     eper = np.array([math.ceil(0.05 * int(L)) for L in lens], np.uint8)
@@ -413,7 +414,7 @@ def test_gpu_verify_forms(cuda_lib, mode):
     assert m.verify() == mode
 
 
-@pytest.mark.parametrize("mode", ["stream8", "stream16"])
+@pytest.mark.parametrize("mode", ["stream8", "stream16", "pair16"])
 def test_gpu_streaming_verify_uniform_e(cuda_lib, mode):
     """Streaming verification at one e for every read (150 bp, e = 7) on a
     repeat-rich genome: records, candidate counts and passing counts equal the
@@ -436,3 +437,33 @@ def test_gpu_streaming_verify_uniform_e(cuda_lib, mode):
     assert st["passed"] == st64["passed"]
     assert st["cells"] == st64["cells"]
     assert st["myers_steps"] < st64["myers_steps"]
+
+
+@pytest.mark.parametrize("e", [0, 2, 5, 7])
+def test_gpu_pair_verify_every_length(cuda_lib, e):
+    """Two candidates per lane (15-bit halves of one word) at every e the form
+    takes, reads of 15-254 bp (shorter than one 16-base chunk too) on a
+    repeat-rich genome, and reads placed at both genome ends: records equal
+    the oracle's and the one-per-lane streaming form's, step for step."""
+    g = genome(1_500_000, 95 + e, "human", nrun_min=2000, nrun_max=20000, copies_per_family=200)
+    reads, lens, _, _ = synth.reads(g, 3000, 15, 254, 0.03, seed=96 + e, stride=256)
+    ends = np.zeros((4, 256), np.uint8)
+    for r, (st, L) in enumerate([(0, 150), (3, 100), (g.size - 150, 150), (g.size - 40, 40)]):
+        ends[r, :L] = g[st:st + L]
+    reads = np.concatenate([reads, ends])
+    lens = np.concatenate([lens, np.array([150, 100, 150, 40], np.uint32)])
+    _, mix = oracle_index(g)
+    want = po.map_reads(mix, reads, lens, e, nthreads=8)
+    ix = cuda_lib.Index.build(g)
+    m = cuda_lib.Mapper(ix, max_reads=reads.shape[0])
+    m.set_verify("stream16")
+    one = m.map(reads, lens, e)
+    st1 = m.stats()
+    m.set_verify("pair16")
+    assert m.verify() == "pair16"
+    two = m.map(reads, lens, e)
+    st2 = m.stats()
+    _check(two, want.records(), want.unmapped)
+    _check(two, one.records(), one.unmapped)
+    for k in ("candidates", "passed", "cells", "myers_steps"):
+        assert st2[k] == st1[k], k
