@@ -1972,6 +1972,13 @@ __global__ void __launch_bounds__(256) k_compact(MapBufs B, uint64_t cap_chunks,
 // integer types; returns 0xffffffff when the window is rejected.
 __device__ __forceinline__ uint32_t window_start(uint32_t base_pos, uint32_t L, uint32_t e, uint64_t ref_length,
                                                  uint32_t *rl_out) {
+    // the window base_pos - e .. base_pos + L + e - 1 inside the genome (and
+    // base_pos + L inside 32 bits): front > 0 > back below, so ref_len stays
+    // L + 2e and the shift e
+    if (base_pos > e && (uint64_t)base_pos + L + e < ref_length && (uint64_t)base_pos + L <= 0xffffffffull) {
+        *rl_out = L + 2 * e;
+        return base_pos - e;
+    }
     const uint64_t dist_error = e;
     uint64_t shift_tmp = e;
     uint64_t ref_len = (uint64_t)L + 2 * shift_tmp;
@@ -2527,19 +2534,37 @@ __global__ void __launch_bounds__(128, 10) k_verify_pair(const uint32_t *__restr
                     je = min(t + 64u, n);
                 }
             }
+            // the two halves' refills issue their loads level by level together
+            uint32_t j2[2], it2[2] = {0, 0}, p2[2] = {0, 0}, L2[2] = {0, 0}, e2[2] = {0, 0};
 #pragma unroll
             for (int h = 0; h < 2; h++) {
-                if (act[h]) continue;
                 const uint32_t r = h == 0 ? __popc(needA & lanemask_lt()) : na + __popc(needB & lanemask_lt());
-                uint32_t j = 0xffffffffu;
-                if (r < avail) j = qn + r;
-                else if (jb + (r - avail) < je) j = jb + (r - avail);
+                j2[h] = 0xffffffffu;
+                if (!act[h]) {
+                    if (r < avail) j2[h] = qn + r;
+                    else if (jb + (r - avail) < je) j2[h] = jb + (r - avail);
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+                if (j2[h] != 0xffffffffu) {
+                    it2[h] = B.cc_item[j2[h]];
+                    p2[h] = B.cc_pos[j2[h]];
+                }
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+                if (j2[h] != 0xffffffffu) {
+                    L2[h] = B.par->lens[it2[h] >> 1];
+                    e2[h] = B.it_e[it2[h]];
+                }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const uint32_t j = j2[h];
                 if (j == 0xffffffffu) continue;
                 c[h] = j;
-                const uint32_t it = B.cc_item[j], p = B.cc_pos[j];
-                const uint32_t L = B.par->lens[it >> 1], e = B.it_e[it];
+                const uint32_t L = L2[h], e = e2[h];
                 uint32_t rl;
-                const uint32_t w = window_start(p, L, e, ref_length, &rl);
+                const uint32_t w = window_start(p2[h], L, e, ref_length, &rl);
                 const uint32_t hm = h ? 0xffff0000u : 0x0000ffffu;
                 vp &= ~hm;
                 vn &= ~hm;
@@ -2555,7 +2580,7 @@ __global__ void __launch_bounds__(128, 10) k_verify_pair(const uint32_t *__restr
                 const int lh = (int)rl - (int)L;
                 meta[h] = L | e << 8 | (uint32_t)(lh > 0 ? lh : 0) << 16;
                 ws[h] = w;
-                item[h] = it;
+                item[h] = it2[h];
                 if (L < CH) { // shorter than a chunk: straight to the finishing pass
                     fin[h] = true;
                 } else {
