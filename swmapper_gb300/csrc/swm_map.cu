@@ -1493,30 +1493,30 @@ __device__ __forceinline__ uint32_t batch_sort_unique(uint32_t *sc, uint32_t *gs
                                                       uint32_t *dst) {
     const uint32_t lane = lane_id();
     uint32_t u = 0;
-    if (kept <= 32) {
-        // survivors are mostly copies of a few positions: take the
-        // distinct values smallest first (up to 8), sort what is left
+    if (kept <= 8) {
+        // at most 8 values: take the distinct ones smallest first
         uint32_t v = lane < kept ? sc[lane] : 0xffffffffu, res = 0;
         for (;;) {
             const uint32_t m = __reduce_min_sync(0xffffffffu, v);
-            if (m == 0xffffffffu || u == 8) break;
+            if (m == 0xffffffffu) break;
             res = lane == u ? m : res;
             v = v == m ? 0xffffffffu : v;
             u++;
         }
         if (lane < u) dst[lane] = res;
-        if (__any_sync(0xffffffffu, v != 0xffffffffu)) {
-            warp_sort_k<32>(v);
-            const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
-            const bool keep = v != 0xffffffffu && (lane == 0 || prev != v);
-            const uint32_t m = __ballot_sync(0xffffffffu, keep);
-            if (keep) dst[u + __popc(m & lanemask_lt())] = v;
-            u += __popc(m);
-        }
+    } else if (kept <= 32) {
+        uint32_t v = lane < kept ? sc[lane] : 0xffffffffu;
+        if (kept <= 16) warp_sort_k<16>(v); // lanes 16.. hold the pad, already in order
+        else warp_sort_k<32>(v);
+        const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 1);
+        const bool keep = v != 0xffffffffu && (lane == 0 || prev != v);
+        const uint32_t m = __ballot_sync(0xffffffffu, keep);
+        if (keep) dst[__popc(m & lanemask_lt())] = v;
+        u = __popc(m);
     } else if (kept <= 64) {
         u = warp_sort_unique<2>(sc, kept, dst);
     } else if (kept <= 128) {
-        u = warp_sort_unique<4>(gs, kept, dst);
+        u = warp_sort_unique<4>(spilled ? gs : sc, kept, dst);
     } else if (kept <= 256) {
         u = warp_sort_unique<8>(gs, kept, dst);
     } else { // bitonic sort in the warp's global scratch
@@ -1552,7 +1552,7 @@ __device__ __forceinline__ uint32_t batch_sort_unique(uint32_t *sc, uint32_t *gs
 
 #define CAND_MAXCH 128 // chunks (runs) per batch: block_size < 256 allows at most 128
 
-#define CAND_SMEM_KEEP 64 // survivors of a batch held in shared memory (more go to global scratch)
+#define CAND_SMEM_KEEP 128 // survivors of a batch held in shared memory (more go to global scratch)
 
 struct CandSmem {
     uint32_t gs[CAND_MAXCH];     // first global index of each chunk minus its start in the batch
