@@ -1,10 +1,12 @@
 #!/usr/bin/env python3
 """Mapped reads/s of SWMapper's hot path on GB300.
 
-Workload (the batched configuration): a 100 Mbp synthetic genome (41% GC, 10%
-of it repeat copies of 300 bp-6 kb families at 1% divergence), k=12 index built
-on the GPU, 1,000,000 reads of 150 bp at 3% error (70% substitutions, 15% 1-bp
-insertions, 15% 1-bp deletions) from both strands, error threshold e=7.
+Workload (default, the human-scale configuration): a 3.1 Gbp synthetic genome
+(41% GC, 5% N in runs of 10 kb-1 Mb, 50% of it repeat families at 2-15%
+divergence), k=12 index built on the GPU, 10,000,000 reads of 150 bp at 3%
+error (70% substitutions, 15% 1-bp insertions, 15% 1-bp deletions) from both
+strands, error threshold e=7. `--workload batched | plain | uneven | serving`
+selects the other configurations.
 
 A step maps every read of the workload (both strands, in blocks) with the
 index and the reads resident in HBM; several mappers take the blocks in turn
@@ -14,9 +16,10 @@ mappers come from the autotuner (swmapper_gb300/tune.py), run before the timed
 region. `value` is mapped reads per second over the K timed steps (CUDA events
 spanning the mappers' streams). `e2e` runs the same reads through the public
 host API (H2D from page-locked memory, mapping, D2H of the packed records)
-with four mappers in turn over a continuous stream of blocks, timed on the host
-clock. The stage breakdown and the roofline views come from one extra untimed
-pass with one mapper, so each kernel runs alone: `roofline` (the dominant
+with two mappers in turn over a continuous stream of blocks (the reference's
+double buffering), timed on the host clock. The stage breakdown and the
+roofline views come from one extra untimed pass with one mapper, so each
+kernel runs alone: `roofline` (the dominant
 kernel's algorithmic bytes against the measured HBM copy bandwidth),
 `gather_roofline` (the seed and candidate kernels' 32-byte sector requests
 against the random-read rate a probe kernel measures at their footprint) and
@@ -725,9 +728,48 @@ def run_gpu(args):
                                     "sample": f"first {n} reads of the workload, {dt:.1f} s, {threads} threads"}
     if rank == 0 and ws == 1 and args.serving and w["genome_kind"] == "human":
         line["serving"] = serving_loads(swm, ix, g, args)
+    if rank == 0 and ws == 1 and args.index_load:
+        line["index_load"] = index_load(swm, rt, ix, w["k"], local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
+
+
+def index_load(swm, rt, ix, k, device):
+    """After the timing: the resident index written as the reference's seven
+    files (swm_index_save) and read back by swm_index_open (sizes checked,
+    one thread per file streaming chunks through page-locked buffers to the
+    device), host clock around each call. The files were just written, so the
+    load reads them from the page cache: it measures the loader and the H2D
+    copies, not the disk. Skipped when the temporary directory lacks room."""
+    import shutil
+    inf = ix.info()
+    nb = 1 << (2 * k)  # .hash_count and .hash_offset, then the entries and the bit planes
+    need = 4 * nb + 4 * (nb + 1) + 6 * inf.n_seeds + 4 * (inf.n_words2 + inf.n_words3)
+    tmp = tempfile.gettempdir()
+    free = shutil.disk_usage(tmp).free
+    if free < 2 * need:
+        return {"skipped": f"{free / 1e9:.1f} GB free in {tmp}, {need / 1e9:.1f} GB of files"}
+    d = tempfile.mkdtemp(prefix="swm_index_", dir=tmp)
+    try:
+        prefix = os.path.join(d, "genome")
+        t0 = time.perf_counter()
+        ix.save(prefix)
+        t_save = time.perf_counter() - t0
+        nbytes = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
+        rt.cudaDeviceSynchronize()
+        t0 = time.perf_counter()
+        ix2 = swm.Index.open(prefix, k=k, device=device)
+        rt.cudaDeviceSynchronize()
+        t_load = time.perf_counter() - t0
+        same = ix2.info().n_seeds == inf.n_seeds
+        ix2.close()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return {"load_s": round(t_load, 3), "save_s": round(t_save, 3), "file_bytes": int(nbytes),
+            "load_gbs": round(nbytes / t_load / 1e9, 2), "entries_equal": bool(same),
+            "path": "swm_index_open on the files swm_index_save just wrote (page cache warm): size checks, "
+                    "one thread per file, 32 MiB chunks through two page-locked buffers, async H2D"}
 
 
 def parity_sample(m, mix, reads, lens, E, eper, nsample, threads):
@@ -991,7 +1033,7 @@ def main():
                     help="group reads of different lengths into 32-bp length buckets (1) or not (0)")
     ap.add_argument("--e2e-steps", type=int, default=10,
                     help="passes over the reads in the end-to-end stream (pipeline fill and drain amortised over them)")
-    ap.add_argument("--e2e-mappers", type=int, default=4, help="mappers in the end-to-end pipeline (>= 2)")
+    ap.add_argument("--e2e-mappers", type=int, default=2, help="mappers in the end-to-end pipeline (>= 2)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=2.0)
     ap.add_argument("--parity-reads", type=int, default=20000,
@@ -1004,6 +1046,8 @@ def main():
                     help="keep the index's candidate table (1) or drop it before the mappers are made (0)")
     ap.add_argument("--serving", type=int, default=1,
                     help="with the human-scale workload, also run the serving loads on its index (1) or not (0)")
+    ap.add_argument("--index-load", type=int, default=1,
+                    help="after the timing, save the index as files and time swm_index_open (1) or not (0)")
     ap.add_argument("--plain", type=int, default=1, help="also time the plain per-batch launch (1) or not (0)")
     ap.add_argument("--genome-bp", type=int, default=None, help="smaller genome for quick checks")
     ap.add_argument("--nreads", type=int, default=None, help="fewer reads for quick checks")
