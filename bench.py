@@ -433,6 +433,8 @@ def run_gpu(args):
     blocks = block_plan(nreads, block, tuned, args.verify)
     block = max(nb for _, nb, _ in blocks)
     mappers = [swm.Mapper(ix, max_reads=block) for _ in range(args.mappers)]
+    if args.serialize:  # the mappers' blocks take the GPU one at a time
+        ix.serialize_mappers(True)
     m = mappers[0]
     streams = [C.c_void_p(mm.stream()) for mm in mappers]
     ev0, ev1, evq = C.c_void_p(), C.c_void_p(), C.c_void_p()
@@ -549,7 +551,10 @@ def run_gpu(args):
         else None
 
     # end to end through the host API: two mappers in ping-pong, packed
-    # results; the reads and the result buffers are page-locked host memory
+    # results; the reads and the result buffers are page-locked host memory;
+    # the blocks' kernels run one block at a time while the other mapper's
+    # copies overlap them (swm_index_serialize_mappers)
+    ix.serialize_mappers(bool(args.e2e_serialize))
     ne = max(2, args.e2e_mappers)
     mappers = (mappers + [swm.Mapper(ix, max_reads=block) for _ in range(ne)])[:ne]
     bufs = [swm.PackedBuffers(block) for _ in range(ne)]
@@ -590,11 +595,13 @@ def run_gpu(args):
     e2e_run(e2e_steps, acc2)
     e2e_t = time.perf_counter() - t0
     e2e_t, e2e_mapped = aggregate(dist, e2e_t, [acc2["mapped"]])
+    ix.serialize_mappers(bool(args.serialize))
     rt.cudaHostUnregister.argtypes = [C.c_void_p]
     for a in pinned:
         rt.cudaHostUnregister(a.ctypes.data)
     e2e = {"value": e2e_mapped / e2e_t, "unit": UNIT,
            "h2d_bytes_per_step": int(acc2["h2d"] / e2e_steps), "d2h_bytes_per_step": int(acc2["d2h"] / e2e_steps),
+           "serialized": bool(args.e2e_serialize),
            "steps": e2e_steps, "path": f"swm_map_submit + swm_map_wait_packed, {ne} mappers in turn over a continuous stream of "
                    "blocks, page-locked host buffers"}
 
@@ -700,6 +707,7 @@ def run_gpu(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded genome and reads of the workload's shapes; no public dataset)",
             "config": {**WORKLOAD, "block_reads": block, "mappers": args.mappers,
+                       "serialized_mappers": bool(args.serialize),
                        "autotune": tuned, "length_buckets": bucketed,
                        "parallelism": f"replicas x{ws} (reads sharded by rank)",
                        "l2": (f"inputs {input_bytes / 1e6:.0f} MB (under {L2_FLUSH_BYTES >> 20} MiB, so treated as "
@@ -1046,6 +1054,10 @@ def main():
                     help="keep the index's candidate table (1) or drop it before the mappers are made (0)")
     ap.add_argument("--serving", type=int, default=1,
                     help="with the human-scale workload, also run the serving loads on its index (1) or not (0)")
+    ap.add_argument("--serialize", type=int, default=0,
+                    help="resident passes: the mappers' blocks run their kernels one block at a time (1) or side by side (0)")
+    ap.add_argument("--e2e-serialize", type=int, default=1,
+                    help="end-to-end pass: kernels one block at a time, copies overlapping (1), or side by side (0)")
     ap.add_argument("--index-load", type=int, default=1,
                     help="after the timing, save the index as files and time swm_index_open (1) or not (0)")
     ap.add_argument("--plain", type=int, default=1, help="also time the plain per-batch launch (1) or not (0)")

@@ -111,6 +111,16 @@ int swm_hash_offset_noalloc(const uint32_t *d_hash_count, uint32_t *d_hash_offse
  * there is none. */
 int swm_index_candidate_table(swm_index *ix, int enable, uint64_t *bytes);
 
+/* No counterpart in the reference, whose host loop keeps one block running on
+ * the CPEs while it reads the next block and writes the previous one
+ * (mapper_mpe.c:972-1106). on = 1: the mappers of this index run their
+ * blocks' kernels one block at a time, in the order the blocks were queued,
+ * while each mapper's input and result copies overlap the kernels of the
+ * others -- that double buffering with two mappers. on = 0 (the default):
+ * the kernels of different mappers' blocks share the GPU. Results are the
+ * same either way. Call it with no block in flight. */
+int swm_index_serialize_mappers(swm_index *ix, int on);
+
 /* Copy the index arrays to host memory in file layout (any pointer may be
  * NULL). hash_offset_end gets the END offsets serial_index writes. */
 int swm_index_download(const swm_index *ix, uint32_t *hash_count, uint32_t *hash_offset_end, uint32_t *positions,

@@ -109,6 +109,7 @@ def lib():
         L.swm_index_get_info.argtypes = [vp, C.POINTER(IndexInfo)]
         L.swm_index_download.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.swm_index_candidate_table.argtypes = [vp, C.c_int, C.POINTER(u64)]
+        L.swm_index_serialize_mappers.argtypes = [vp, C.c_int]
         L.swm_index_free.argtypes = [vp]
         L.swm_index_free.restype = None
         L.swm_mapper_create.argtypes = [vp, u64, C.POINTER(vp)]
@@ -213,6 +214,11 @@ class Index:
         mode = -1 if enable is None else (1 if enable else 0)
         _check(lib().swm_index_candidate_table(self._h, mode, C.byref(nbytes)), "swm_index_candidate_table")
         return int(nbytes.value)
+
+    def serialize_mappers(self, on: bool = True) -> None:
+        """Run the mappers' blocks one at a time on the GPU, their copies
+        overlapping the other mappers' kernels (swm_index_serialize_mappers)."""
+        _check(lib().swm_index_serialize_mappers(self._h, 1 if on else 0), "swm_index_serialize_mappers")
 
     def close(self) -> None:
         if self._h:

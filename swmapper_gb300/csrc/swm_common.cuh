@@ -46,6 +46,11 @@ struct swm_index {
     uint32_t *d_ctab_pos;  // 4 * n_seeds (+8) positions
     uint32_t ctab_gen;     // bumped whenever the table is built or dropped
     int ctab_off;          // the caller dropped the table: no automatic build
+    // swm_index_serialize_mappers: when chain is set, every mapper of this
+    // index queues its block's kernels behind chain_ev (the completion of the
+    // block queued before it, by any mapper) and records chain_ev after them
+    int chain;
+    cudaEvent_t chain_ev;
 };
 
 // Key of the candidate table: seed code << 8 | shift << 6 | flank, where

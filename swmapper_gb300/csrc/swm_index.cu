@@ -491,6 +491,7 @@ static unsigned grid_for(uint64_t work, unsigned threads, int device, int per_sm
 
 static void index_release(swm_index *ix) {
     if (!ix) return;
+    if (ix->chain_ev) cudaEventDestroy(ix->chain_ev);
     cudaFree(ix->d_ctab_off);
     cudaFree(ix->d_ctab_pos);
     cudaFree(ix->d_count);

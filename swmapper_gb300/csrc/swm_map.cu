@@ -20,7 +20,7 @@
 //   k_verify   thread / cand   window, banded Myers, Hamming check or
 //                              traceback + CIGAR      (mapper_cpe.c:229-660,
 //                                                      1403-1435,1509-1586)
-//   k_records  thread / item   groups of 8, record flushes, dedup, primary
+//   k_records  warp / item     groups of 8, record flushes, dedup, primary
 //                              flag (count pass, scan, write pass)
 //                                                     (mapper_cpe.c:1437-1507,
 //                                                      1753-1860)
@@ -28,6 +28,7 @@
 // All sizes flow through device memory, so the host queues the whole block
 // without synchronising; capacities are checked on the device and a block
 // whose work outgrew a buffer is re-run with larger buffers.
+#include <mutex>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -56,6 +57,7 @@ enum {
     TOT_PLN, TOT_PLQ,  // items with refills and at most 32 selected seeds, queue head of k_plan_lanes
     TOT_PLW, TOT_PLWQ, // items with refills and more selected seeds, queue head of k_plan
     TOT_CQ,            // queue head of the candidate stage (items)
+    TOT_RQC, TOT_RQW,  // queue heads of the records count and write passes (groups of 32 items)
     TOT_N
 };
 
@@ -2525,13 +2527,6 @@ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
     return d;
 }
 
-// Next n work units of a warp from a device work queue (head *q).
-__device__ __forceinline__ uint32_t warp_take_n(uint32_t *q, uint32_t n) {
-    uint32_t b = 0;
-    if ((threadIdx.x & 31) == 0) b = atomicAdd(q, n);
-    return __shfl_sync(0xffffffffu, b, 0);
-}
-
 template <int CH>
 __global__ void __launch_bounds__(128, VERIFY_BLOCKS_PER_SM)
     k_verify_pair(const uint32_t *__restrict__ b2, uint64_t b2_words, uint64_t ref_length, MapBufs B,
@@ -2545,105 +2540,102 @@ __global__ void __launch_bounds__(128, VERIFY_BLOCKS_PER_SM)
     const uint32_t n = (uint32_t)(nc_all < cap_cands ? nc_all : cap_cands);
     const uint32_t lane = lane_id();
     uint32_t cells = 0, nsteps = 0; // per lane, both halves
-    uint32_t qn = 0, qe = 0;        // the warp's queue entries not handed out yet
     bool drained = false;
     bool act[2] = {false, false};
     // per half: candidate, L | e << 8 | max(last_high, 0) << 16, bases done, window start, item, D0 bit-0 count
     uint32_t c[2] = {0, 0}, meta[2] = {0, 0}, i[2] = {0, 0}, ws[2] = {0, 0}, item[2] = {0, 0}, ones[2] = {0, 0};
     uint32_t vp = 0, vn = 0, PM = 0; // packed state and band masks
+    // Candidates are set up 32 at a time with every lane (as in
+    // k_verify_stream) into a ring of 128 slots per warp; up to 64 halves can
+    // ask at once, so fewer than 64 slots are waiting when a range is taken.
+    __shared__ uint4 ring_s[4][128]; // 128 threads: 4 warps
+    uint4 *ring = ring_s[threadIdx.x >> 5];
+    uint32_t rh = 0, rt = 0; // slots handed out / staged (counts; slot = count & 127)
     for (;;) {
         const unsigned needA = __ballot_sync(0xffffffffu, !act[0]), needB = __ballot_sync(0xffffffffu, !act[1]);
         bool fin[2] = {false, false}, dead[2] = {false, false};
         if (needA | needB) {
-            const uint32_t na = __popc(needA), k = na + __popc(needB), avail = qe - qn;
-            uint32_t jb = qe, je = qe;
-            if (k > avail && !drained) {
-                const uint32_t t = warp_take_n(&B.tot[TOT_VQ], 64u);
+            const uint32_t na = __popc(needA), k = na + __popc(needB);
+            while (rt - rh < k && !drained) {
+                const uint32_t t = warp_take(&B.tot[TOT_VQ]);
                 if (t >= n) {
                     drained = true;
-                } else {
-                    jb = t;
-                    je = min(t + 64u, n);
+                    break;
                 }
+                const uint32_t cj = t + lane;
+                bool keep = false, shortc = false;
+                uint4 rec = make_uint4(0u, 0u, 0u, 0u);
+                if (cj < n) {
+                    const uint32_t it = B.cc_item[cj], p = B.cc_pos[cj];
+                    const uint32_t L = B.par->lens[it >> 1], e = B.it_e[it];
+                    uint32_t rl;
+                    const uint32_t w0 = window_start(p, L, e, ref_length, &rl);
+                    const int lh = (int)rl - (int)L;
+                    if (w0 == 0xffffffffu) {
+                        B.vr_flag[cj] = VR_INVALID;
+                        B.vr_err[cj] = SWM_MAXERROR;
+                        B.vr_mloc[cj] = -1;
+                    } else if (L < CH) { // shorter than a chunk: straight to the finishing pass
+                        shortc = true;
+                    } else {
+                        keep = true;
+                        rec = make_uint4(cj, L | e << 8 | (uint32_t)(lh > 0 ? lh : 0) << 16, w0, it);
+                    }
+                }
+                const unsigned sm = __ballot_sync(0xffffffffu, shortc);
+                if (sm) {
+                    const uint32_t leader = __ffs(sm) - 1;
+                    uint32_t at = 0;
+                    if (lane == leader) at = atomicAdd(&B.tot[TOT_VT], (uint32_t)__popc(sm));
+                    at = __shfl_sync(0xffffffffu, at, leader);
+                    if (shortc) {
+                        const uint32_t q = at + __popc(sm & lanemask_lt());
+                        B.vt_x[q] = make_uint2(cj, 0u);
+                        B.vt_st[q] = make_uint4(0u, 0u, 0u, 0u);
+                    }
+                }
+                const unsigned km = __ballot_sync(0xffffffffu, keep);
+                if (keep) ring[(rt + __popc(km & lanemask_lt())) & 127u] = rec;
+                rt += __popc(km);
+                __syncwarp();
             }
-            // the two halves' refills issue their loads level by level together
-            uint32_t j2[2], it2[2] = {0, 0}, p2[2] = {0, 0}, L2[2] = {0, 0}, e2[2] = {0, 0};
+            const uint32_t got = min(k, rt - rh);
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 const uint32_t r = h == 0 ? __popc(needA & lanemask_lt()) : na + __popc(needB & lanemask_lt());
-                j2[h] = 0xffffffffu;
-                if (!act[h]) {
-                    if (r < avail) j2[h] = qn + r;
-                    else if (jb + (r - avail) < je) j2[h] = jb + (r - avail);
-                }
-            }
-#pragma unroll
-            for (int h = 0; h < 2; h++)
-                if (j2[h] != 0xffffffffu) {
-                    it2[h] = B.cc_item[j2[h]];
-                    p2[h] = B.cc_pos[j2[h]];
-                }
-#pragma unroll
-            for (int h = 0; h < 2; h++)
-                if (j2[h] != 0xffffffffu) {
-                    L2[h] = B.par->lens[it2[h] >> 1];
-                    e2[h] = B.it_e[it2[h]];
-                }
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const uint32_t j = j2[h];
-                if (j == 0xffffffffu) continue;
-                c[h] = j;
-                const uint32_t L = L2[h], e = e2[h];
-                uint32_t rl;
-                const uint32_t w = window_start(p2[h], L, e, ref_length, &rl);
-                const uint32_t hm = h ? 0xffff0000u : 0x0000ffffu;
+                if (act[h] || r >= got) continue;
+                const uint4 sl = ring[(rh + r) & 127u];
+                const uint32_t hm = h ? 0xffff0000u : 0x0000ffffu, e = (sl.y >> 8) & 0xffu;
+                c[h] = sl.x;
+                meta[h] = sl.y;
+                ws[h] = sl.z;
+                item[h] = sl.w;
                 vp &= ~hm;
                 vn &= ~hm;
-                PM &= ~hm;
+                PM = (PM & ~hm) | (((1u << (2 * e + 1)) - 1u) << (16 * h));
                 ones[h] = 0;
                 i[h] = 0;
-                if (w == 0xffffffffu) {
-                    B.vr_flag[j] = VR_INVALID;
-                    B.vr_err[j] = SWM_MAXERROR;
-                    B.vr_mloc[j] = -1;
-                    continue;
-                }
-                const int lh = (int)rl - (int)L;
-                meta[h] = L | e << 8 | (uint32_t)(lh > 0 ? lh : 0) << 16;
-                ws[h] = w;
-                item[h] = it2[h];
-                if (L < CH) { // shorter than a chunk: straight to the finishing pass
-                    fin[h] = true;
-                } else {
-                    act[h] = true;
-                    PM |= ((1u << (2 * e + 1)) - 1u) << (16 * h);
-                }
+                act[h] = true;
             }
-            if (k <= avail) {
-                qn += k;
-            } else {
-                qn = min(jb + (k - avail), je);
-                qe = je;
-            }
+            rh += got;
+            __syncwarp(); // slots read before a later range overwrites them
         }
         if (act[0] || act[1]) {
-            uint32_t xl0[2], xl1[2], xh0[2], xh1[2], rb[2][2];
+            uint32_t xl0[2], xh0[2], rb[2][2];
 #pragma unroll
             for (int h = 0; h < 2; h++) { // window bits and read bits of the chunk (inactive half: zeros)
                 const uint32_t pos = ws[h] + i[h], sh = pos & 31;
-                uint2 a0 = make_uint2(0u, 0u), a1 = a0, a2 = a0, rr = a0;
+                uint2 a0 = make_uint2(0u, 0u), a1 = a0, rr = a0;
                 if (act[h]) {
                     const uint64_t q = pos >> 5;
                     a0 = pair_at(q);
                     a1 = pair_at(q + 1);
-                    a2 = pair_at(q + 2);
                     rr = reinterpret_cast<const uint2 *>(B.it_w + (uint64_t)item[h] * 32)[i[h] >> 5];
                 }
+                // window bits 0 .. 29 from the chunk's first base: a 16-base chunk and
+                // a band of <= 15 bits
                 xl0[h] = __funnelshift_r(a0.x, a1.x, sh);
-                xl1[h] = __funnelshift_r(a1.x, a2.x, sh);
                 xh0[h] = __funnelshift_r(a0.y, a1.y, sh);
-                xh1[h] = __funnelshift_r(a1.y, a2.y, sh);
                 // read base t of the chunk at bit 15 - t of the half (bit reverse of the low halfword)
                 rb[h][0] = __brev((rr.x >> (i[h] & 31)) & 0xffffu);
                 rb[h][1] = __brev((rr.y >> (i[h] & 31)) & 0xffffu);
@@ -2653,8 +2645,9 @@ __global__ void __launch_bounds__(128, VERIFY_BLOCKS_PER_SM)
             uint32_t acc = 0;
 #pragma unroll
             for (uint32_t t = 0; t < CH; t++) {
-                const uint32_t wl = prmt(__funnelshift_r(xl0[0], xl1[0], t), __funnelshift_r(xl0[1], xl1[1], t), 0x5410u);
-                const uint32_t wh = prmt(__funnelshift_r(xh0[0], xh1[0], t), __funnelshift_r(xh0[1], xh1[1], t), 0x5410u);
+                // window bits t .. t + 14 of each half (t + 14 <= 29: one word)
+                const uint32_t wl = prmt(xl0[0] >> t, xl0[1] >> t, 0x5410u);
+                const uint32_t wh = prmt(xh0[0] >> t, xh0[1] >> t, 0x5410u);
                 // read base t of each half as all-ones / all-zeros: the sign of bytes 1 and 3
                 const uint32_t mL = prmt(RL << t, 0u, 0xbb99u), mH = prmt(RH << t, 0u, 0xbb99u);
                 const uint32_t eq = ~((wl ^ mL) | (wh ^ mH)) & PM;
@@ -2703,7 +2696,7 @@ __global__ void __launch_bounds__(128, VERIFY_BLOCKS_PER_SM)
             B.vr_flag[c[h]] = VR_FAIL;
             act[h] = false;
         }
-        if (drained && qn >= qe && !__any_sync(0xffffffffu, act[0] || act[1])) break;
+        if (drained && rh >= rt && !__any_sync(0xffffffffu, act[0] || act[1])) break;
     }
     warp_add_u64(&B.stat[ST_CELLS], (unsigned long long)cells);
     warp_add_u64(&B.stat[ST_STEPS], (unsigned long long)nsteps);
@@ -3202,13 +3195,143 @@ __global__ void __launch_bounds__(128) k_traceback_slow(const uint32_t *__restri
 // k_records: groups of 8, record flushes, dedup, primary flag
 // ======================================================================
 
+// One item's records by the reference's rules, one thread: candidates in
+// batch order, groups of 8 with the flush test after each (1790) and after a
+// batch's last partial group (1858), the traceback path's dedup against the
+// previous location (475-477), the primary flag on the first record. The
+// count pass (WRITE false) stores the item's record / word / byte counts, the
+// write pass writes the records at the scanned offsets. Returns the records.
+template <bool WRITE>
+__device__ uint32_t records_seq(const MapBufs &B, uint32_t item, uint64_t cap_recs, uint64_t cap_words,
+                                uint64_t cap_bytes, unsigned long long &locs_total) {
+    const uint8_t *__restrict__ vflag = B.vr_flag;
+    const uint32_t *__restrict__ vloc = B.vr_loc;
+    const uint16_t *__restrict__ vtlen = B.vr_tlen;
+    const uint8_t *__restrict__ vcig = B.vr_cig;
+    uint8_t *__restrict__ out_c = B.out_c;
+    uint32_t *__restrict__ out_w = B.out_w;
+    const uint32_t s0 = B.it_choff[item] + item, nb = B.it_nbat[item];
+    uint32_t cnext = B.it_coff[item];
+    uint32_t num = 0, len = 0, last = 0, mainf = 1, nrec = 0, nw = 0, nby = 0;
+    uint32_t recbase = 0, wbase = 0, bbase = 0;
+    bool ok = true;
+    if (WRITE) {
+        recbase = B.it_recoff[item];
+        wbase = B.it_woff[item];
+        bbase = B.it_boff[item];
+        ok = (uint64_t)recbase + B.it_nrec[item] <= cap_recs && (uint64_t)wbase + B.it_nw[item] <= cap_words &&
+             (uint64_t)bbase + B.it_nb[item] <= cap_bytes;
+        if (!ok) atomicOr(&B.tot[TOT_FLAGS], OV_RECS);
+    }
+    uint32_t wrec = wbase, bcur = bbase;
+    auto put = [&]() { // put_cigar, 1437-1507
+        if (num > 0) {
+            if (WRITE && ok) {
+                out_w[wrec] = item;
+                out_w[wrec + 1] = num | (mainf ? (1u << 31) : 0u);
+                B.rec_woff[recbase + nrec] = wrec;
+                B.rec_boff[recbase + nrec] = bcur - len;
+                B.rec_blen[recbase + nrec] = len;
+            }
+            mainf = 0;
+            nrec++;
+            nw += 2 + num;
+            nby += len;
+            wrec += 2 + num;
+            locs_total += num;
+        }
+        num = 0;
+        len = 0;
+    };
+    for (uint32_t s = s0; s < s0 + nb; s++) {
+        const uint32_t cbeg = cnext, cn = B.bt_cnt[s];
+        cnext += cn;
+        uint32_t g = 0; // candidates of the batch's current group of 8 (failed and passing, not invalid)
+        const uint32_t cend = cbeg + cn;
+        for (uint32_t c = cbeg; c < cend; c++) {
+            // Runs of failed candidates (flag 0: no location, one group
+            // slot each) are taken 16 or 4 at a time. Between two
+            // locations the flush test at a group boundary sees the same
+            // (num, len) every time, and after a flush it is false, so a
+            // run that crosses one or more boundaries needs one test.
+            if ((c & 15) == 0 && c + 16 <= cend) {
+                const uint4 w = *reinterpret_cast<const uint4 *>(vflag + c);
+                if ((w.x | w.y | w.z | w.w) == 0) {
+                    if (g + 16 >= 8 && (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16)) put();
+                    g = (g + 16) & 7;
+                    c += 15;
+                    continue;
+                }
+            }
+            if ((c & 3) == 0 && c + 4 <= cend && *reinterpret_cast<const uint32_t *>(vflag + c) == 0) {
+                if (g + 4 >= 8 && (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16)) put();
+                g = (g + 4) & 7;
+                c += 3;
+                continue;
+            }
+            const uint8_t f = vflag[c];
+            if (f == VR_INVALID) continue;
+            if (f == VR_HAM || f == VR_TB) {
+                const uint32_t loc = vloc[c];
+                if (f == VR_HAM || !(num > 0 && last == loc)) { // 475-477
+                    const uint32_t tl = vtlen[c];
+                    if (WRITE && ok) {
+                        out_w[wrec + 2 + num] = loc;
+                        // [NM, len, text]: the slot's first 16 bytes in one load
+                        const uint4 h = *reinterpret_cast<const uint4 *>(vcig + (uint64_t)c * SWM_CIGAR_SLOT);
+                        const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
+                        if (tl + 2 <= 16) {
+#pragma unroll
+                            for (uint32_t q = 0; q < 16; q++)
+                                if (q < tl + 2) out_c[bcur + q] = (uint8_t)(hw[q >> 2] >> (8 * (q & 3)));
+                        } else {
+                            out_c[bcur] = (uint8_t)h.x;
+                            out_c[bcur + 1] = (uint8_t)(h.x >> 8);
+                            const uint8_t *tx = (tl <= SWM_CIGAR_SLOT - 2) ? vcig + (uint64_t)c * SWM_CIGAR_SLOT + 2
+                                                                          : B.arena + B.vr_aoff[c];
+                            for (uint32_t q = 0; q < tl; q++) out_c[bcur + 2 + q] = tx[q];
+                        }
+                    }
+                    bcur += 2 + tl;
+                    num++;
+                    len += 2 + tl;
+                    last = loc;
+                }
+            }
+            if (++g == 8) {
+                g = 0;
+                if (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16) put(); // 1790
+            }
+        }
+        if (g > 0 && (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16)) put(); // 1858
+    }
+    put();
+    if (!WRITE) {
+        B.it_nrec[item] = nrec;
+        B.it_nw[item] = nw;
+        B.it_nb[item] = nby;
+    }
+    return nrec;
+}
+
+// Records, one warp per item, groups of 32 consecutive items taken from a
+// queue. Most items need none of the sequential machinery: while num + 8 <=
+// SWM_MAX_CIGAR and len + 256 <= 16 SWM_MAX_CIGAR the flush tests are false,
+// so when the item's passing candidates (P of them, S bytes of [NM, len,
+// text] before dedup) keep within those bounds, or (write pass) the count
+// pass found at most one record, the item is one record of every passing
+// candidate in order except a traceback hit whose location equals the
+// previous passing candidate's (that previous one was then emitted or had
+// the same location itself). The warp reads 32 verdict flags per load, and
+// only the passing lanes read their location and CIGAR; the rest go through
+// records_seq on lane 0. Count pass: the item's record / word / byte counts;
+// write pass: the records, and the unmapped-read bits of the group.
 template <bool WRITE>
 __global__ void __launch_bounds__(128) k_records(MapBufs B, uint64_t cap_chunks, uint64_t cap_elems,
                                                  uint64_t cap_cands, uint64_t cap_recs, uint64_t cap_words,
                                                  uint64_t cap_bytes) {
     if (block_failed(B, cap_chunks, cap_elems, cap_cands)) return;
-    const uint32_t nitems = B.par->nitems;
-    // distinct arrays: loads of later candidates may pass earlier stores
+    const uint32_t nitems = B.par->nitems, lane = lane_id();
     const uint8_t *__restrict__ vflag = B.vr_flag;
     const uint32_t *__restrict__ vloc = B.vr_loc;
     const uint16_t *__restrict__ vtlen = B.vr_tlen;
@@ -3216,115 +3339,119 @@ __global__ void __launch_bounds__(128) k_records(MapBufs B, uint64_t cap_chunks,
     uint8_t *__restrict__ out_c = B.out_c;
     uint32_t *__restrict__ out_w = B.out_w;
     unsigned long long locs_total = 0, mapped = 0;
-    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < nitems; item += gridDim.x * blockDim.x) {
-        const uint32_t s0 = B.it_choff[item] + item, nb = B.it_nbat[item];
-        uint32_t cnext = B.it_coff[item];
-        uint32_t num = 0, len = 0, last = 0, mainf = 1, nrec = 0, nw = 0, nby = 0;
-        uint32_t recbase = 0, wbase = 0, bbase = 0;
-        bool ok = true;
-        if (WRITE) {
-            recbase = B.it_recoff[item];
-            wbase = B.it_woff[item];
-            bbase = B.it_boff[item];
-            ok = (uint64_t)recbase + B.it_nrec[item] <= cap_recs && (uint64_t)wbase + B.it_nw[item] <= cap_words &&
-                 (uint64_t)bbase + B.it_nb[item] <= cap_bytes;
-            if (!ok) atomicOr(&B.tot[TOT_FLAGS], OV_RECS);
-        }
-        uint32_t wrec = wbase, bcur = bbase;
-        auto put = [&]() { // put_cigar, 1437-1507
-            if (num > 0) {
-                if (WRITE && ok) {
-                    out_w[wrec] = item;
-                    out_w[wrec + 1] = num | (mainf ? (1u << 31) : 0u);
-                    B.rec_woff[recbase + nrec] = wrec;
-                    B.rec_boff[recbase + nrec] = bcur - len;
-                    B.rec_blen[recbase + nrec] = len;
-                }
-                mainf = 0;
-                nrec++;
-                nw += 2 + num;
-                nby += len;
-                wrec += 2 + num;
-                locs_total += num;
+    for (;;) {
+        const uint32_t item0 = warp_take(&B.tot[WRITE ? TOT_RQW : TOT_RQC]);
+        if (item0 >= nitems) break;
+        // the group's scalars: lane j holds item item0 + j's
+        const uint32_t mine = item0 + lane;
+        uint32_t g_cb = 0, g_nc = 0, g_nrec = 0, g_wb = 0, g_bb = 0, g_rb = 0;
+        bool g_ok = true;
+        if (mine < nitems) {
+            g_cb = B.it_coff[mine];
+            g_nc = B.it_nbat[mine] ? B.it_ncand[mine] : 0u;
+            if (WRITE) {
+                g_nrec = B.it_nrec[mine];
+                g_wb = B.it_woff[mine];
+                g_bb = B.it_boff[mine];
+                g_rb = B.it_recoff[mine];
+                g_ok = (uint64_t)g_rb + g_nrec <= cap_recs && (uint64_t)g_wb + B.it_nw[mine] <= cap_words &&
+                       (uint64_t)g_bb + B.it_nb[mine] <= cap_bytes;
             }
-            num = 0;
-            len = 0;
-        };
-        for (uint32_t s = s0; s < s0 + nb; s++) {
-            const uint32_t cbeg = cnext, cn = B.bt_cnt[s];
-            cnext += cn;
-            uint32_t g = 0; // candidates of the batch's current group of 8 (failed and passing, not invalid)
-            const uint32_t cend = cbeg + cn;
-            for (uint32_t c = cbeg; c < cend; c++) {
-                // Runs of failed candidates (flag 0: no location, one group
-                // slot each) are taken 16 or 4 at a time. Between two
-                // locations the flush test at a group boundary sees the same
-                // (num, len) every time, and after a flush it is false, so a
-                // run that crosses one or more boundaries needs one test.
-                if ((c & 15) == 0 && c + 16 <= cend) {
-                    const uint4 w = *reinterpret_cast<const uint4 *>(vflag + c);
-                    if ((w.x | w.y | w.z | w.w) == 0) {
-                        if (g + 16 >= 8 && (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16)) put();
-                        g = (g + 16) & 7;
-                        c += 15;
-                        continue;
-                    }
+        }
+        const uint32_t cnt = min(32u, nitems - item0);
+        for (uint32_t j = 0; j < cnt; j++) {
+            const uint32_t item = item0 + j;
+            const uint32_t cb = __shfl_sync(0xffffffffu, g_cb, j), nc = __shfl_sync(0xffffffffu, g_nc, j);
+            const uint32_t nrec_c = __shfl_sync(0xffffffffu, g_nrec, j);
+            if (WRITE && nrec_c == 0) continue; // nothing passed (or every location deduped)
+            if (WRITE && nrec_c > 1) {          // flushes: the sequential rules
+                if (lane == 0) records_seq<true>(B, item, cap_recs, cap_words, cap_bytes, locs_total);
+                continue;
+            }
+            const uint32_t wbase = __shfl_sync(0xffffffffu, g_wb, j), bbase = __shfl_sync(0xffffffffu, g_bb, j);
+            const bool ok = __shfl_sync(0xffffffffu, (uint32_t)g_ok, j) != 0;
+            uint32_t num = 0, len = 0, P = 0, S = 0, last = 0;
+            bool has = false;
+            for (uint32_t c0 = cb; c0 < cb + nc; c0 += 32) {
+                const uint32_t c = c0 + lane;
+                const uint8_t f = c < cb + nc ? vflag[c] : (uint8_t)VR_FAIL;
+                const bool pass = f == VR_HAM || f == VR_TB;
+                const unsigned pm = __ballot_sync(0xffffffffu, pass);
+                if (!pm) continue;
+                uint32_t loc = 0, tl = 0;
+                if (pass) {
+                    loc = vloc[c];
+                    tl = vtlen[c];
                 }
-                if ((c & 3) == 0 && c + 4 <= cend && *reinterpret_cast<const uint32_t *>(vflag + c) == 0) {
-                    if (g + 4 >= 8 && (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16)) put();
-                    g = (g + 4) & 7;
-                    c += 3;
-                    continue;
-                }
-                const uint8_t f = vflag[c];
-                if (f == VR_INVALID) continue;
-                if (f == VR_HAM || f == VR_TB) {
-                    const uint32_t loc = vloc[c];
-                    if (f == VR_HAM || !(num > 0 && last == loc)) { // 475-477
-                        const uint32_t tl = vtlen[c];
-                        if (WRITE && ok) {
-                            out_w[wrec + 2 + num] = loc;
-                            // [NM, len, text]: the slot's first 16 bytes in one load
-                            const uint4 h = *reinterpret_cast<const uint4 *>(vcig + (uint64_t)c * SWM_CIGAR_SLOT);
-                            const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
-                            if (tl + 2 <= 16) {
+                const unsigned below = pm & lanemask_lt();
+                const uint32_t ploc = __shfl_sync(0xffffffffu, loc, below ? 31 - __clz(below) : lane);
+                const bool dup = f == VR_TB && (below ? ploc == loc : (has && last == loc));
+                const bool keep = pass && !dup;
+                const unsigned km = __ballot_sync(0xffffffffu, keep);
+                const uint32_t by = keep ? 2 + tl : 0u;
+                const uint32_t incl = warp_scan_incl(by);
+                if (WRITE && keep && ok) {
+                    out_w[wbase + 2 + num + __popc(km & lanemask_lt())] = loc;
+                    const uint32_t bcur = bbase + len + incl - by;
+                    const uint4 h = *reinterpret_cast<const uint4 *>(vcig + (uint64_t)c * SWM_CIGAR_SLOT);
+                    const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
+                    if (tl + 2 <= 16) {
 #pragma unroll
-                                for (uint32_t q = 0; q < 16; q++)
-                                    if (q < tl + 2) out_c[bcur + q] = (uint8_t)(hw[q >> 2] >> (8 * (q & 3)));
-                            } else {
-                                out_c[bcur] = (uint8_t)h.x;
-                                out_c[bcur + 1] = (uint8_t)(h.x >> 8);
-                                const uint8_t *tx = (tl <= SWM_CIGAR_SLOT - 2) ? vcig + (uint64_t)c * SWM_CIGAR_SLOT + 2
-                                                                              : B.arena + B.vr_aoff[c];
-                                for (uint32_t q = 0; q < tl; q++) out_c[bcur + 2 + q] = tx[q];
-                            }
-                        }
-                        bcur += 2 + tl;
-                        num++;
-                        len += 2 + tl;
-                        last = loc;
+                        for (uint32_t q = 0; q < 16; q++)
+                            if (q < tl + 2) out_c[bcur + q] = (uint8_t)(hw[q >> 2] >> (8 * (q & 3)));
+                    } else {
+                        out_c[bcur] = (uint8_t)h.x;
+                        out_c[bcur + 1] = (uint8_t)(h.x >> 8);
+                        const uint8_t *tx = (tl <= SWM_CIGAR_SLOT - 2) ? vcig + (uint64_t)c * SWM_CIGAR_SLOT + 2
+                                                                      : B.arena + B.vr_aoff[c];
+                        for (uint32_t q = 0; q < tl; q++) out_c[bcur + 2 + q] = tx[q];
                     }
                 }
-                if (++g == 8) {
-                    g = 0;
-                    if (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16) put(); // 1790
+                num += __popc(km);
+                len += __shfl_sync(0xffffffffu, incl, 31);
+                if (!WRITE) {
+                    P += __popc(pm);
+                    S += __reduce_add_sync(0xffffffffu, pass ? 2 + tl : 0u);
+                }
+                last = __shfl_sync(0xffffffffu, loc, 31 - __clz(pm));
+                has = true;
+            }
+            if (!WRITE) {
+                if (P + 8 <= SWM_MAX_CIGAR && S + 16 * 16 <= SWM_MAX_CIGAR * 16) {
+                    if (lane == 0) {
+                        B.it_nrec[item] = num ? 1u : 0u;
+                        B.it_nw[item] = num ? 2 + num : 0u;
+                        B.it_nb[item] = len;
+                    }
+                } else if (lane == 0) {
+                    records_seq<false>(B, item, cap_recs, cap_words, cap_bytes, locs_total);
+                }
+            } else {
+                const uint32_t rb = __shfl_sync(0xffffffffu, g_rb, j);
+                if (!ok && lane == 0) atomicOr(&B.tot[TOT_FLAGS], OV_RECS);
+                if (lane == 0 && num) {
+                    if (ok) {
+                        out_w[wbase] = item;
+                        out_w[wbase + 1] = num | (1u << 31);
+                        B.rec_woff[rb] = wbase;
+                        B.rec_boff[rb] = bbase;
+                        B.rec_blen[rb] = len;
+                    }
+                    locs_total += num;
                 }
             }
-            if (g > 0 && (num + 8 > SWM_MAX_CIGAR || len + 16 * 16 > SWM_MAX_CIGAR * 16)) put(); // 1858
         }
-        put();
-        if (!WRITE) {
-            B.it_nrec[item] = nrec;
-            B.it_nw[item] = nw;
-            B.it_nb[item] = nby;
-        } else {
-            const bool mp = (item & 1) && (nrec + B.it_nrec[item - 1]) > 0;
-            mapped += mp ? 1u : 0u;
-            // unmapped reads as bits, 16 reads (one warp of items) per halfword
-            const uint32_t item0 = item & ~31u, left = nitems - item0;
-            const uint32_t wm = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
-            const uint32_t bal = __ballot_sync(wm, (item & 1) && !mp);
-            if ((item & 31) == 0) B.unm[item0 >> 5] = (uint16_t)even_bits(bal >> 1);
+        if (WRITE) {
+            // unmapped reads as bits, 16 reads (the group's 32 items) per halfword
+            const uint32_t prev = __shfl_up_sync(0xffffffffu, g_nrec, 1);
+            const bool valid = mine < nitems;
+            const bool mp = (lane & 1) && (g_nrec + prev) > 0;
+            const unsigned bal = __ballot_sync(0xffffffffu, valid && (lane & 1) && !mp);
+            const unsigned mb = __ballot_sync(0xffffffffu, valid && mp);
+            if (lane == 0) {
+                B.unm[item0 >> 5] = (uint16_t)even_bits(bal >> 1);
+                mapped += __popc(mb);
+            }
         }
     }
     if (WRITE) {
@@ -3352,6 +3479,7 @@ __global__ void k_batches_stat(MapBufs B) {
 static uint64_t cap_clamp(uint64_t c) { return c < CAP_MAX ? c : CAP_MAX; }
 
 static int g_sms = 0;
+static std::mutex g_chain_mu; // serialised mappers: wait, launch and record as one step
 
 static unsigned grid_cap(uint64_t work, unsigned threads, int per_sm) {
     if (!g_sms) {
@@ -3701,7 +3829,30 @@ static int enqueue(swm_mapper *m, const char *d_reads, const uint32_t *d_lens, u
         m->gx_gen[gclass][h] = m->gen;
         m->gx_tab[gclass][h] = m->ix->ctab_gen;
     }
+    if (m->ix->chain) { // one block's kernels at a time across the index's mappers
+        std::lock_guard<std::mutex> lk(g_chain_mu);
+        SWM_CUDA(cudaStreamWaitEvent(m->st, m->ix->chain_ev, 0));
+        SWM_CUDA(cudaGraphLaunch(m->gx[gclass][h], m->st));
+        SWM_CUDA(cudaEventRecord(m->ix->chain_ev, m->st));
+        return SWM_OK;
+    }
     SWM_CUDA(cudaGraphLaunch(m->gx[gclass][h], m->st));
+    return SWM_OK;
+}
+
+// Serialised mappers: a block's inputs are copied on its mapper's stream
+// before the wait on chain_ev, and its results after the record, so the
+// copies of one mapper overlap the kernels of another (the reference's
+// double buffering, mapper_mpe.c:972-1106) while the kernels of two blocks
+// never share the SMs.
+extern "C" int swm_index_serialize_mappers(swm_index *ix, int on) {
+    if (!ix) return SWM_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_chain_mu);
+    if (on && !ix->chain_ev) {
+        SWM_CUDA(cudaSetDevice(ix->device));
+        SWM_CUDA(cudaEventCreateWithFlags(&ix->chain_ev, cudaEventDisableTiming));
+    }
+    ix->chain = on ? 1 : 0;
     return SWM_OK;
 }
 

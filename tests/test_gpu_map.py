@@ -185,12 +185,15 @@ def test_gpu_rejects_out_of_envelope(cuda_lib):
         m.map(np.zeros((5, 100), np.uint8), np.full(5, 100, np.uint32), 5)
 
 
-def test_gpu_packed_pingpong_equals_strided(cuda_lib):
+@pytest.mark.parametrize("serial", [False, True])
+def test_gpu_packed_pingpong_equals_strided(cuda_lib, serial):
     """submit / wait_packed on two mappers (the host double-buffering of
-    mapper_mpe.c:972-1106) gives the same records as swm_map_batch."""
+    mapper_mpe.c:972-1106; with serial the two mappers' kernels run one block
+    at a time) gives the same records as swm_map_batch."""
     g = genome(2_000_000, 19, "repeats100m")
     reads, lens, _, _ = synth.reads(g, 6000, 150, 150, 0.03, seed=20)
     ix = cuda_lib.Index.build(g)
+    ix.serialize_mappers(serial)
     ma, mb = cuda_lib.Mapper(ix, max_reads=2000), cuda_lib.Mapper(ix, max_reads=2000)
     want = []
     for b0 in range(0, 6000, 2000):
@@ -290,10 +293,12 @@ def test_gpu_pinned_buffers_direct_copy(cuda_lib):
     assert got == want
 
 
-def test_gpu_device_submit_two_mappers(cuda_lib):
+@pytest.mark.parametrize("serial", [False, True])
+def test_gpu_device_submit_two_mappers(cuda_lib, serial):
     """swm_map_device_submit / swm_map_device_wait on two mappers in turn
-    (blocks overlapping on the GPU) give the same records and unmapped ids as
-    swm_map_device one block at a time."""
+    (blocks overlapping on the GPU, or with serial their kernels one block at
+    a time: swm_index_serialize_mappers) give the same records and unmapped
+    ids as swm_map_device one block at a time."""
     import ctypes
     rt = None
     for name in ("libcudart.so.13", "libcudart.so"):
@@ -309,6 +314,7 @@ def test_gpu_device_submit_two_mappers(cuda_lib):
     g = genome(3_000_000, 31, "human", nrun_min=2000, nrun_max=20000, copies_per_family=300)
     reads, lens, _, _ = synth.reads(g, 6000, 150, 150, 0.03, seed=32)
     ix = cuda_lib.Index.build(g)
+    ix.serialize_mappers(serial)
     d_reads, d_lens = ctypes.c_void_p(), ctypes.c_void_p()
     assert rt.cudaMalloc(ctypes.byref(d_reads), reads.nbytes) == 0
     assert rt.cudaMalloc(ctypes.byref(d_lens), lens.nbytes) == 0
@@ -467,3 +473,41 @@ def test_gpu_pair_verify_every_length(cuda_lib, e):
     _check(two, one.records(), one.unmapped)
     for k in ("candidates", "passed", "cells", "myers_steps"):
         assert st2[k] == st1[k], k
+
+
+def test_gpu_records_split_past_the_record_limit(cuda_lib):
+    """Reads from a unit copied 320 times (some copies with a substitution or
+    an indel) have more locations than one record holds (SWM_MAX_CIGAR), so
+    the records kernel's sequential path (flushes after groups of 8, dedup
+    reset after a flush, primary flag on the first record only) runs beside
+    its one-record fast path."""
+    rng = np.random.default_rng(61)
+    g = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, 600_000)]
+    unit = g[1000:1400].copy()
+    starts = np.sort(rng.choice(np.arange(5_000, 590_000, 1_700), 320, replace=False))
+    for i, s in enumerate(starts):
+        cp = unit.copy()
+        if i % 5 == 1:    # one substitution
+            cp[200] = ord("A") if cp[200] != ord("A") else ord("C")
+        elif i % 5 == 2:  # one deletion: the copy shifts by a base
+            cp = np.concatenate([cp[:180], cp[181:], unit[-1:]])
+        g[s:s + cp.size] = cp
+    reads = np.zeros((40, 150), np.uint8)
+    lens = np.full(40, 150, np.uint32)
+    for r in range(40):
+        o = 20 + 5 * r
+        s = unit[o:o + 150].copy()
+        if r % 3 == 1:
+            s[70] = ord("G") if s[70] != ord("G") else ord("T")
+        if r % 2:
+            s = s[::-1].copy()
+            s = np.frombuffer(bytes(s).translate(bytes.maketrans(b"ACGT", b"TGCA")), np.uint8)
+        reads[r] = s
+    _, mix = oracle_index(g)
+    ref = po.map_reads(mix, reads, lens, 7)
+    per_item = {}
+    for rec in ref.records():
+        per_item[rec[0]] = per_item.get(rec[0], 0) + 1
+    assert max(per_item.values()) >= 2, "the workload should split some item's locations over records"
+    out, _, _ = _gpu(cuda_lib, g, reads, lens, 7)
+    _check(out, ref.records(), ref.unmapped)
