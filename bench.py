@@ -400,8 +400,8 @@ def run_gpu(args):
     ix = swm.Index.build_device(d_g.value, g.size, k=w["k"], device=local)
     index_build_s = time.perf_counter() - t0
     rt.cudaFree(d_g)
-    if not args.table:
-        ix.candidate_table(False)
+    if args.table >= 0:  # else the library decides (large genomes only)
+        ix.candidate_table(bool(args.table))
     nreads, stride = reads.shape
     block = min(args.block, nreads)
     # inputs resident in HBM
@@ -707,7 +707,7 @@ def run_gpu(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded genome and reads of the workload's shapes; no public dataset)",
             "config": {**WORKLOAD, "block_reads": block, "mappers": args.mappers,
-                       "serialized_mappers": bool(args.serialize),
+                       "serialized_mappers": bool(args.serialize), "candidate_table": table,
                        "autotune": tuned, "length_buckets": bucketed,
                        "parallelism": f"replicas x{ws} (reads sharded by rank)",
                        "l2": (f"inputs {input_bytes / 1e6:.0f} MB (under {L2_FLUSH_BYTES >> 20} MiB, so treated as "
@@ -1050,8 +1050,9 @@ def main():
     ap.add_argument("--requests", type=int, default=None, help="requests of the serving workload")
     ap.add_argument("--verify", choices=["head64", "head32", "stream8", "stream16", "pair16"], default="stream16",
                     help="form of the verification stage when the autotuner does not choose it per length bucket")
-    ap.add_argument("--table", type=int, default=1,
-                    help="keep the index's candidate table (1) or drop it before the mappers are made (0)")
+    ap.add_argument("--table", type=int, default=-1,
+                    help="candidate table for k = 12: the library's choice (-1: built for genomes whose buckets "
+                         "average 8 or more entries, when the device has room), always (1) or never (0)")
     ap.add_argument("--serving", type=int, default=1,
                     help="with the human-scale workload, also run the serving loads on its index (1) or not (0)")
     ap.add_argument("--serialize", type=int, default=0,

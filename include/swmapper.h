@@ -98,7 +98,8 @@ int swm_hash_offset_noalloc(const uint32_t *d_hash_count, uint32_t *d_hash_offse
 
 /* No counterpart in the reference (a device-only structure derived from the
  * index arrays; the files are unchanged). For k = 12 the first mapper made on
- * an index builds a candidate table when the device has room for it: the
+ * an index whose buckets average 8 or more entries (a genome of about 540 Mbp
+ * or more) builds a candidate table when the device has room for it: the
  * entries of every bucket grouped, for each seed shift, by the 6 flank bits
  * long_seeds_filter compares (mapper_cpe.c:2090-2123), behind a directly
  * indexed table of 2^32 + 1 offsets (about 17 GiB, plus 16 bytes per index
@@ -106,7 +107,8 @@ int swm_hash_offset_noalloc(const uint32_t *d_hash_count, uint32_t *d_hash_offse
  * instead of every entry of the fetched buckets; results are identical
  * either way. enable = 0 drops the table and keeps it from being built again
  * (mappers fall back to filtering every entry; call it with no block in
- * flight), enable = 1 builds it now if it is missing and fits, enable < 0
+ * flight), enable = 1 builds it now if it is missing and fits, whatever the
+ * bucket sizes, enable < 0
  * only reports. *bytes (may be NULL) gets the table's device bytes, 0 when
  * there is none. */
 int swm_index_candidate_table(swm_index *ix, int enable, uint64_t *bytes);

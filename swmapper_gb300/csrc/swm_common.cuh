@@ -65,8 +65,11 @@ __host__ __device__ __forceinline__ uint32_t swm_ctab_flank(uint32_t ls, uint32_
     const uint32_t sh = SWM_SEED_STEP - 1 - t;
     return ((ls >> sh) & 7u) | (((ls >> (6 + sh)) & 7u) << 3);
 }
-// Build / drop the table (swm_index.cu); the mapper builds it on demand.
-int swm_ctab_build(swm_index *ix);
+// Build the table (swm_index.cu) when it is missing and the device has room:
+// forced = 1 for an explicit request, 0 when a mapper is made (then only for
+// indexes averaging SWM_CTAB_MIN_MEAN or more entries per bucket).
+#define SWM_CTAB_MIN_MEAN 8
+int swm_ctab_build(swm_index *ix, int forced);
 
 // Exclusive scan of n u32 values (n read from *d_n when d_n is not NULL,
 // else n_host; clamped to n_cap); out gets n + 1 entries, out[n] = total,

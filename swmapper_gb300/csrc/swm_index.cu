@@ -980,9 +980,14 @@ static uint64_t ctab_bytes(const swm_index *ix) { return (SWM_CTAB_KEYS + 1) * 4
 // dropped it, and the device holds it with a margin (8 GiB) to spare. Not
 // building it is not an error: the mapper then filters the buckets entry by
 // entry. Returns SWM_OK in both cases; a CUDA error while building is returned.
-int swm_ctab_build(swm_index *ix) {
+int swm_ctab_build(swm_index *ix, int forced) {
     std::lock_guard<std::mutex> lk(g_ctab_mu);
     if (ix->d_ctab_off || ix->ctab_off || ix->k != 12 || 4 * ix->n_seeds + 8 >= 0xffffffffull) return SWM_OK;
+    // Built on its own only for genomes whose buckets average SWM_CTAB_MIN_MEAN
+    // entries or more: its lookup is a random read of a 17 GiB array per
+    // selected seed, which costs more than filtering a bucket of a few entries
+    // (a 100 Mbp genome averages 1.5 per bucket, a 3.1 Gbp one 44).
+    if (!forced && ix->n_seeds < (uint64_t)SWM_CTAB_MIN_MEAN << (2 * ix->k)) return SWM_OK;
     SWM_CUDA(cudaSetDevice(ix->device));
     size_t fr = 0, total = 0;
     if (cudaMemGetInfo(&fr, &total) != cudaSuccess || fr < ctab_bytes(ix) + (8ull << 30)) {
@@ -1030,7 +1035,7 @@ extern "C" int swm_index_candidate_table(swm_index *ix, int enable, uint64_t *by
             std::lock_guard<std::mutex> lk(g_ctab_mu);
             ix->ctab_off = 0;
         }
-        const int rc = swm_ctab_build(ix);
+        const int rc = swm_ctab_build(ix, 1);
         if (rc) return rc;
     } else {
         std::lock_guard<std::mutex> lk(g_ctab_mu);

@@ -657,7 +657,7 @@ __device__ __forceinline__ uint32_t seed12_nfix(uint32_t sd, uint32_t nk, uint32
 // the 12-mer (set_read_long_seeds, 2474-2478). cnt gets the bucket counts summed per
 // long seed (choose_seed, 1372-1390), nref the refill chunks. Every lookup is
 // independent, so they all issue back to back.
-template <int NL, bool HASN>
+template <int NL, bool HASN, bool KEYS>
 __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const uint32_t (&plo)[8],
                                                const uint32_t (&phi)[8], const uint32_t (&pok)[8], uint32_t nl,
                                                const uint32_t *__restrict__ off, uint64_t pol,
@@ -690,26 +690,27 @@ __device__ __forceinline__ void seed12_records(const uint32_t (&iw)[NL], const u
             const uint32_t rl = ((lr & m) | ((lr >> kk) << sft)) & 7u;
             const uint32_t rh = ((hr & m) | ((hr >> kk) << sft)) & 7u;
             if (sft & 1) // two records per 16-byte store
-                reinterpret_cast<uint4 *>(rec)[(SWM_SEED_STEP * l + sft) >> 1] = make_uint4(po, pc, o0, c);
+                __stcs(reinterpret_cast<uint4 *>(rec) + ((SWM_SEED_STEP * l + sft) >> 1), make_uint4(po, pc, o0, c));
             po = o0;
             pc = c;
             f |= (rl | (rh << 3)) << (8 * sft);
-            kk4[sft] = swm_ctab_key(sd, sft, rl | (rh << 3));
+            if (KEYS) kk4[sft] = swm_ctab_key(sd, sft, rl | (rh << 3));
             csum += c;
             rsum += c > SWM_PER_FETCH ? (c - 1) / SWM_PER_FETCH : 0u;
         }
-        if (l & 1) reinterpret_cast<uint2 *>(flw)[l >> 1] = make_uint2(pf, f); // two long seeds per store
-        reinterpret_cast<uint4 *>(keys)[l] = make_uint4(kk4[0], kk4[1], kk4[2], kk4[3]);
+        if (l & 1) __stcs(reinterpret_cast<uint2 *>(flw) + (l >> 1), make_uint2(pf, f)); // two long seeds per store
+        if (KEYS) __stcs(reinterpret_cast<uint4 *>(keys) + l, make_uint4(kk4[0], kk4[1], kk4[2], kk4[3]));
         pf = f;
         cnt[l] = act ? csum : 0u;
         nref[l] = act ? rsum : 0u;
     }
 }
 
-template <int NL>
+template <int NL, bool TABLE>
 // Items whose read length is outside [lo_len, hi_len] belong to the other
 // instantiation launched beside this one (reads of up to 164 bases take the
-// 10-long-seed kernel, longer ones the 16-long-seed kernel).
+// 10-long-seed kernel, longer ones the 16-long-seed kernel). TABLE: the
+// candidate table is in use, so each seed's table key is stored too.
 __global__ void SEED12_BOUNDS k_seed12(const uint32_t *__restrict__ off, MapBufs B,
                                                            uint32_t lo_len, uint32_t hi_len) {
     const BlockParams P = *B.par;
@@ -942,21 +943,24 @@ __global__ void SEED12_BOUNDS k_seed12(const uint32_t *__restrict__ off, MapBufs
             }
         }
         uint4 *ow = reinterpret_cast<uint4 *>(it_w + (uint64_t)item * 32);
-        ow[0] = make_uint4(mlo[0], mhi[0], mlo[1], mhi[1]);
-        ow[1] = make_uint4(mlo[2], mhi[2], mlo[3], mhi[3]);
-        ow[2] = make_uint4(mlo[4], mhi[4], mlo[5], mhi[5]);
-        ow[3] = make_uint4(mlo[6], mhi[6], mlo[7], mhi[7]);
-        ow[4] = make_uint4(plo[0], phi[0], plo[1], phi[1]);
-        ow[5] = make_uint4(plo[2], phi[2], plo[3], phi[3]);
-        ow[6] = make_uint4(plo[4], phi[4], plo[5], phi[5]);
-        ow[7] = make_uint4(plo[6], phi[6], plo[7], phi[7]);
+        // the seed records and read words stream out with an evict-first hint
+        // (a block's are far larger than L2), keeping the bucket-offset table
+        // the lookups hit in L2
+        __stcs(ow + 0, make_uint4(mlo[0], mhi[0], mlo[1], mhi[1]));
+        __stcs(ow + 1, make_uint4(mlo[2], mhi[2], mlo[3], mhi[3]));
+        __stcs(ow + 2, make_uint4(mlo[4], mhi[4], mlo[5], mhi[5]));
+        __stcs(ow + 3, make_uint4(mlo[6], mhi[6], mlo[7], mhi[7]));
+        __stcs(ow + 4, make_uint4(plo[0], phi[0], plo[1], phi[1]));
+        __stcs(ow + 5, make_uint4(plo[2], phi[2], plo[3], phi[3]));
+        __stcs(ow + 6, make_uint4(plo[4], phi[4], plo[5], phi[5]));
+        __stcs(ow + 7, make_uint4(plo[6], phi[6], plo[7], phi[7]));
         // ---- every seed's record, all lookups in flight together
         const uint64_t sb = (uint64_t)item * SWM_MAX_SEL;
         uint32_t CNT[NL], IDX[NL], REF[NL];
         uint32_t *flw = reinterpret_cast<uint32_t *>(B.sel_fl + sb);
         uint32_t *keys = B.sel_key + sb;
-        if (has_n) seed12_records<NL, true>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, keys, CNT, REF);
-        else seed12_records<NL, false>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, keys, CNT, REF);
+        if (has_n) seed12_records<NL, true, TABLE>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, keys, CNT, REF);
+        else seed12_records<NL, false, TABLE>(iw, plo, phi, pok, nl, off, pol, sel + sb, flw, keys, CNT, REF);
 #pragma unroll
         for (int l = 0; l < NL; l++) IDX[l] = l;
         // exchange sort (1391-1399), unrolled
@@ -3601,7 +3605,8 @@ extern "C" int swm_mapper_create(swm_index *ix, uint64_t max_reads, swm_mapper *
     if (!ix || !out || max_reads == 0 || max_reads > (1ull << 30)) return SWM_ERR_ARG;
     SWM_CUDA(cudaSetDevice(ix->device));
     // the index's candidate table (k = 12), built once when the device has room
-    const int trc = swm_ctab_build(ix);
+    // and the buckets are large enough for it to pay
+    const int trc = swm_ctab_build(ix, 0);
     if (trc) return trc;
     swm_mapper *m = (swm_mapper *)calloc(1, sizeof(swm_mapper));
     if (!m) return SWM_ERR_OOM;
@@ -3694,12 +3699,14 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass, int vmode) {
     // stage events: external records become event nodes of the captured graph
     SWM_CUDA(cudaEventRecordWithFlags(m->ev[0], st, cudaEventRecordExternal));
     const uint32_t short_max = 10 * KL12 + KL12 - 1; // 164: longest read with <= 10 long seeds
+    const bool table = ix->d_ctab_off && ix->k == K12;
+    auto seed10 = table ? k_seed12<10, true> : k_seed12<10, false>;
+    auto seed16 = table ? k_seed12<16, true> : k_seed12<16, false>;
     if (gclass == 1) {
-        k_seed12<10><<<grid_cap(ci, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(ix->d_off, B, 0u, 0xffffffffu);
+        seed10<<<grid_cap(ci, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(ix->d_off, B, 0u, 0xffffffffu);
     } else if (gclass == 2) { // each read to the instantiation of its length
-        k_seed12<10><<<grid_cap(ci, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(ix->d_off, B, 0u, short_max);
-        k_seed12<16><<<grid_cap(ci, SEED12_THREADS, 8), SEED12_THREADS, 0, st>>>(ix->d_off, B, short_max + 1,
-                                                                                   0xffffffffu);
+        seed10<<<grid_cap(ci, SEED12_THREADS, 16), SEED12_THREADS, 0, st>>>(ix->d_off, B, 0u, short_max);
+        seed16<<<grid_cap(ci, SEED12_THREADS, 8), SEED12_THREADS, 0, st>>>(ix->d_off, B, short_max + 1, 0xffffffffu);
         m->launches++;
     } else
         k_seed<<<grid_cap(ci, SEED_WARPS * 32, 8), SEED_WARPS * 32, 0, st>>>(ix->d_off, ix->k, B);
@@ -3711,7 +3718,6 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass, int vmode) {
     rc = swm_exclusive_scan(B.it_nel, B.it_eloff, d_n, 0, ci, B.scan_tmp, B.tot + TOT_ELEMS, st);
     if (rc) return rc;
     m->launches += 6;
-    const bool table = ix->d_ctab_off && ix->k == K12;
     k_plan_list<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks, !table);
     k_plan_lanes<<<grid_cap(ci, PLAN_LANE_WARPS * 32, 6), PLAN_LANE_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
                                                                                          m->cap_elems);

@@ -15,10 +15,14 @@ GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "referen
 
 
 def _gpu(swm, g, reads, lens, e, eper=None, max_reads=None, table=True):
-    """Map on the GPU; table=False drops the index's candidate table first, so
-    the candidate stage filters every fetched entry (the path for k != 12)."""
+    """Map on the GPU; table=True builds the index's candidate table (the
+    library builds it on its own only for large genomes), table=False drops
+    it, so the candidate stage filters every fetched entry (the path for
+    k != 12 and for genomes of small buckets)."""
     ix = swm.Index.build(g)
-    if not table:
+    if table:
+        assert ix.candidate_table(True) > 0
+    else:
         assert ix.candidate_table(False) == 0
     m = swm.Mapper(ix, max_reads=max_reads or max(1, reads.shape[0]))
     out = m.map(reads, lens, e, errors_per_read=eper)
