@@ -431,6 +431,17 @@ def run_gpu(args):
             tuned["buckets"] = swtune.tune_buckets(ix, d_reads.value, d_lens.value, stride, lens, E,
                                                    d_e.value if eper is not None else None, args.mappers)
     blocks = block_plan(nreads, block, tuned, args.verify)
+    if tuned and tuned.get("buckets"):
+        # the per-bucket plan against the sorted reads in blocks of the tuned
+        # size (each with its main bucket's form), over all the reads
+        from swmapper_gb300 import tune as swtune
+        merged = swtune.merged_plan(tuned["buckets"], nreads, block)
+        best, rates = swtune.tune_plan(ix, d_reads.value, d_lens.value, stride, E,
+                                       d_e.value if eper is not None else None,
+                                       {"per_bucket": blocks, "merged": merged}, args.mappers)
+        tuned["plan"] = {"chosen": best, "reads_per_s": rates}
+        if best == "merged":
+            blocks = merged
     block = max(nb for _, nb, _ in blocks)
     mappers = [swm.Mapper(ix, max_reads=block) for _ in range(args.mappers)]
     if args.serialize:  # the mappers' blocks take the GPU one at a time

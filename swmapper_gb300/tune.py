@@ -12,8 +12,12 @@ so reads of very different lengths side by side waste lanes. The autotuner
   (for example GPU, k, length bucket, e), and
 * for each length bucket, times that bucket's reads under every
   (verification form, reads per block) pair and keeps the fastest
-  (`tune_buckets`). The forms: a first pass over 64 or 32 bases of every
-  candidate with an exact stop test, then the rest ("head64", "head32"), or
+  (`tune_buckets`), then times that per-bucket plan against the
+  length-sorted reads cut into blocks of the globally tuned size, each
+  block with its main bucket's form (`merged_plan`, `tune_plan`): small
+  buckets in blocks of their own pay each block's fixed cost more often.
+  The forms: a first pass over 64 or 32 bases of every candidate with an
+  exact stop test, then the rest ("head64", "head32"), or
   lanes that each run their own candidate and test a stop bound every 8 or
   16 bases, taking the next candidate as soon as theirs stops ("stream8",
   "stream16"), or two such candidates per lane when every threshold is <= 7
@@ -87,6 +91,57 @@ def run_blocks(mappers, d_reads: int, d_lens: int, stride: int, nreads: int, e: 
         pm.wait_device()
         if on_done:
             on_done(pm)
+
+
+def run_plan(mappers, d_reads: int, d_lens: int, stride: int, e: int, d_e: int | None, plan) -> None:
+    """Map the blocks of plan -- (first read, reads, verification form) each --
+    with the mappers in turn (swm_map_device_submit / swm_map_device_wait)."""
+    pend = []
+    for i, (b0, nb, form) in enumerate(plan):
+        if len(pend) == len(mappers):
+            pend.pop(0).wait_device()
+        m = mappers[i % len(mappers)]
+        m.set_verify(form)
+        m.submit_device(d_reads + b0 * stride, d_lens + b0 * 4, stride, nb, e, None if d_e is None else d_e + b0)
+        pend.append(m)
+    while pend:
+        pend.pop(0).wait_device()
+
+
+def merged_plan(buckets: list[dict], nreads: int, block: int) -> list[tuple[int, int, str]]:
+    """The length-sorted reads in blocks of `block` reads across bucket
+    boundaries, each block with the form its largest share of reads' bucket
+    chose: fewer, fuller blocks than one set per bucket, with the reads of a
+    block still of similar length."""
+    plan = []
+    for b0 in range(0, nreads, block):
+        nb = min(block, nreads - b0)
+        share = {}
+        for bk in buckets:
+            ov = min(b0 + nb, bk["first"] + bk["reads"]) - max(b0, bk["first"])
+            if ov > 0:
+                share[bk["verify"]] = share.get(bk["verify"], 0) + ov
+        plan.append((b0, nb, max(share, key=share.get) if share else "stream16"))
+    return plan
+
+
+def tune_plan(index, d_reads: int, d_lens: int, stride: int, e: int, d_e: int | None, plans: dict,
+              nmappers: int) -> tuple[str, dict]:
+    """The fastest of the named block plans over all the reads (a warm-up
+    pass, then a timed one each); returns its name and every plan's rate."""
+    import swmapper_gb300 as swm
+    rt = _cudart()
+    rates = {}
+    for name, plan in plans.items():
+        ms = [swm.Mapper(index, max_reads=max(nb for _, nb, _ in plan)) for _ in range(nmappers)]
+        run_plan(ms, d_reads, d_lens, stride, e, d_e, plan)
+        rt.cudaDeviceSynchronize()
+        t0 = time.perf_counter()
+        run_plan(ms, d_reads, d_lens, stride, e, d_e, plan)
+        rt.cudaDeviceSynchronize()
+        rates[name] = round(sum(nb for _, nb, _ in plan) / (time.perf_counter() - t0), 1)
+        del ms
+    return max(rates, key=rates.get), rates
 
 
 def tune(index, d_reads: int, d_lens: int, stride: int, nreads: int, e: int, d_e: int | None = None,
