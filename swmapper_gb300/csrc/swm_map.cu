@@ -3318,8 +3318,13 @@ __device__ uint32_t records_seq(const MapBufs &B, uint32_t item, uint64_t cap_re
     return nrec;
 }
 
-// Records, one warp per item, groups of 32 consecutive items taken from a
-// queue. Most items need none of the sequential machinery: while num + 8 <=
+// Items with at most this many candidates take the one-thread path of
+// k_records (records_seq); the others the warp path.
+#define RECORDS_LIGHT 16
+
+// Records, groups of 32 consecutive items taken from a queue: items with few
+// candidates one thread each (records_seq, all lanes at once), the others
+// one warp each. Most of those need none of the sequential machinery: while num + 8 <=
 // SWM_MAX_CIGAR and len + 256 <= 16 SWM_MAX_CIGAR the flush tests are false,
 // so when the item's passing candidates (P of them, S bytes of [NM, len,
 // text] before dedup) keep within those bounds, or (write pass) the count
@@ -3362,8 +3367,14 @@ __global__ void __launch_bounds__(128) k_records(MapBufs B, uint64_t cap_chunks,
                        (uint64_t)g_bb + B.it_nb[mine] <= cap_bytes;
             }
         }
-        const uint32_t cnt = min(32u, nitems - item0);
-        for (uint32_t j = 0; j < cnt; j++) {
+        // items with few candidates: one lane each, all at once (the warp
+        // path below would spend a pass of 32 lanes on a handful of flags)
+        const bool light = mine < nitems && g_nc <= RECORDS_LIGHT;
+        if (light && !(WRITE && g_nrec == 0))
+            records_seq<WRITE>(B, mine, cap_recs, cap_words, cap_bytes, locs_total);
+        const unsigned heavy = __ballot_sync(0xffffffffu, mine < nitems && !light);
+        for (unsigned hm = heavy; hm; hm &= hm - 1) {
+            const uint32_t j = __ffs(hm) - 1;
             const uint32_t item = item0 + j;
             const uint32_t cb = __shfl_sync(0xffffffffu, g_cb, j), nc = __shfl_sync(0xffffffffu, g_nc, j);
             const uint32_t nrec_c = __shfl_sync(0xffffffffu, g_nrec, j);
