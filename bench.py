@@ -598,13 +598,17 @@ def run_gpu(args):
         while pend:
             drain()
 
+    e2e_clocks = ClockSampler(local)
+    e2e_clocks.start()
     e2e_run(min(args.warmup, 2), {"mapped": 0, "h2d": 0, "d2h": 0})
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
     acc2 = {"mapped": 0, "h2d": 0, "d2h": 0}
     dist.barrier()
+    t_e2e0 = time.time()
     t0 = time.perf_counter()
     e2e_run(e2e_steps, acc2)
     e2e_t = time.perf_counter() - t0
+    e2e_clk = e2e_clocks.stop(t_e2e0, time.time())
     e2e_t, e2e_mapped = aggregate(dist, e2e_t, [acc2["mapped"]])
     ix.serialize_mappers(bool(args.serialize))
     rt.cudaHostUnregister.argtypes = [C.c_void_p]
@@ -612,7 +616,7 @@ def run_gpu(args):
         rt.cudaHostUnregister(a.ctypes.data)
     e2e = {"value": e2e_mapped / e2e_t, "unit": UNIT,
            "h2d_bytes_per_step": int(acc2["h2d"] / e2e_steps), "d2h_bytes_per_step": int(acc2["d2h"] / e2e_steps),
-           "serialized": bool(args.e2e_serialize),
+           "serialized": bool(args.e2e_serialize), "clocks": e2e_clk,
            "steps": e2e_steps, "path": f"swm_map_submit + swm_map_wait_packed, {ne} mappers in turn over a continuous stream of "
                    "blocks, page-locked host buffers"}
 
