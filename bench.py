@@ -670,6 +670,21 @@ def run_gpu(args):
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                 "fallback 6.8 TB/s"}
+    # the candidate stage against the HBM peak by the DRAM bytes it moves (ncu
+    # bytes per unit from its committed capture x this step's units): its
+    # scattered 4-byte reads each move a whole DRAM burst, so its algorithmic
+    # bytes understate what bounds it
+    cand_dram = None
+    ckern = "k_cand_table" if table else "k_cand"
+    ctr = profile_traffic(ckern) or {}
+    cper = ctr.get("dram_bytes_per_item_human" if table and w["genome_kind"] == "human" else "")
+    t_cand = per_step["ms_candidates"] / 1e3
+    if cper and t_cand > 0:
+        cgbs = cper * per_step["items"] / t_cand / 1e9
+        cand_dram = {"kernel": ckern, "dram_gbs": round(cgbs, 1), "peak": peak, "frac": round(cgbs / peak, 4),
+                     "algorithmic_gbs": stage_rows["candidates"]["gbs"],
+                     "model": f"{cper:.0f} B of DRAM per item (ncu, profiles/{ckern}_traffic.txt) x items / "
+                              "candidate-stage time"}
     # gather view of the seed and candidate kernels: they read scattered 32-byte
     # sectors (bucket offsets; flank codes and positions), so their ceiling is
     # the rate at which the device serves random sector reads from an array of
@@ -737,7 +752,8 @@ def run_gpu(args):
             "per_step": {k: int(v) if not k.startswith("ms_") else round(v, 3) for k, v in per_step.items()},
             "stages": stage_rows, "stage_timing": "kernel times of one mapper alone (untimed pass)",
             "clocks": clk, "e2e": e2e,
-            "gpu_launches": int(acc["launches"]), "roofline": roofline, "int_pipe": int_pipe, "gather_roofline": gather,
+            "gpu_launches": int(acc["launches"]), "roofline": roofline, "int_pipe": int_pipe,
+            "candidates_dram": cand_dram, "gather_roofline": gather,
             "plain_per_batch": plain}
     if rank == 0 and ws == 1 and (not args.no_cpu_baseline or args.parity_reads):
         arrays = ix.download()

@@ -6,22 +6,26 @@
 // same per-(read, strand) semantics run as a sequence of data-parallel kernels
 // over a whole block, each sized to its natural unit of work:
 //
-//   k_seed     thread / item   read encodings, seed lookups, long-seed order,
-//                              flank codes            (mapper_cpe.c:1246-1401,
+//   k_seed12   thread / item   read encodings, seed lookups, long-seed order,
+//   (k_seed)                   flank codes            (mapper_cpe.c:1246-1401,
 //                                                      2451-2499)
 //   scan       chunk and element offsets per item
-//   k_plan     thread / item   the fetch schedule: 32-position chunks,
-//                              heap-ordered refills, batch boundaries
+//   k_plan*    lane or warp /  the fetch schedule: 32-position chunks,
+//              item            heap-ordered refills, batch boundaries
 //                                                     (mapper_cpe.c:2124-2419)
-//   k_cand     warp / batch    gather + position adjust + flank filter +
+//   k_cand /   warp / item     gather + position adjust + flank filter (or
+//   k_cand_table               the candidate table's survivors) + per-batch
 //                              sort-unique            (mapper_cpe.c:1893-2123)
 //   scan       candidate offsets
-//   k_compact  warp / batch    dense candidate list
-//   k_verify   thread / cand   window, banded Myers, Hamming check or
-//                              traceback + CIGAR      (mapper_cpe.c:229-660,
+//   k_compact  thread or warp  dense candidate list
+//              / item
+//   k_verify_stream   lane /   window, banded Myers 16 bases at a time with a
+//   + k_verify_finish  cand    stop bound; last bases, final scan, Hamming
+//   (or k_verify, two passes)  check               (mapper_cpe.c:229-660,
 //                                                      1403-1435,1509-1586)
-//   k_records  warp / item     groups of 8, record flushes, dedup, primary
-//                              flag (count pass, scan, write pass)
+//   k_traceback thread / cand  traceback + CIGAR text (align_reads, mapper_cpe.c:229-517)
+//   k_records  thread or warp  groups of 8, record flushes, dedup, primary
+//              / item          flag (count pass, scan, write pass)
 //                                                     (mapper_cpe.c:1437-1507,
 //                                                      1753-1860)
 //
