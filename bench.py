@@ -791,20 +791,27 @@ def index_load(swm, rt, ix, k, device):
         return {"skipped": f"{free / 1e9:.1f} GB free in {tmp}, {need / 1e9:.1f} GB of files"}
     d = tempfile.mkdtemp(prefix="swm_index_", dir=tmp)
     try:
-        prefix = os.path.join(d, "genome")
-        t0 = time.perf_counter()
-        ix.save(prefix)
-        t_save = time.perf_counter() - t0
-        nbytes = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
-        rt.cudaDeviceSynchronize()
-        t0 = time.perf_counter()
-        ix2 = swm.Index.open(prefix, k=k, device=device)
-        rt.cudaDeviceSynchronize()
-        t_load = time.perf_counter() - t0
-        same = ix2.info().n_seeds == inf.n_seeds
-        ix2.close()
+        return _index_load(swm, rt, ix, k, device, inf, d)
+    except (OSError, RuntimeError) as ex:  # a full disk or a loader error is reported, not fatal
+        return {"skipped": f"{type(ex).__name__}: {ex}"}
     finally:
         shutil.rmtree(d, ignore_errors=True)
+
+
+def _index_load(swm, rt, ix, k, device, inf, d):
+    """Save the index as files in directory d, then time swm_index_open on them."""
+    prefix = os.path.join(d, "genome")
+    t0 = time.perf_counter()
+    ix.save(prefix)
+    t_save = time.perf_counter() - t0
+    nbytes = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
+    rt.cudaDeviceSynchronize()
+    t0 = time.perf_counter()
+    ix2 = swm.Index.open(prefix, k=k, device=device)
+    rt.cudaDeviceSynchronize()
+    t_load = time.perf_counter() - t0
+    same = ix2.info().n_seeds == inf.n_seeds
+    ix2.close()
     return {"load_s": round(t_load, 3), "save_s": round(t_save, 3), "file_bytes": int(nbytes),
             "load_gbs": round(nbytes / t_load / 1e9, 2), "entries_equal": bool(same),
             "path": "swm_index_open on the files swm_index_save just wrote (page cache warm): size checks, "
