@@ -1259,8 +1259,13 @@ __global__ void __launch_bounds__(PLAN_WARPS * 32) k_plan(const uint32_t *__rest
 #define PLAN_LANE_REFILL 16
 #endif
 
+// Per lane (one item each): every selected seed's next position index and
+// the end of its bucket (global indices into the position array), and the
+// seed heap (keys and seed indices). Two words per seed, not three, keep the
+// block at 26.5 KB: 8 resident blocks per SM instead of 6 -- the kernel waits
+// on one position-array key per refill, so resident lanes are what it runs on.
 struct PlanLaneSmem {
-    uint32_t sst[PLAN_LANE_SEEDS][32], scn[PLAN_LANE_SEEDS][32], pc[PLAN_LANE_SEEDS][32];
+    uint32_t cur[PLAN_LANE_SEEDS][32], end[PLAN_LANE_SEEDS][32];
     uint32_t hloc[PLAN_LANE_SEEDS + 1][32];
     uint8_t hidx[PLAN_LANE_SEEDS + 1][32];
 };
@@ -1312,9 +1317,8 @@ __global__ void __launch_bounds__(PLAN_LANE_WARPS * 32) k_plan_lanes(const uint3
                             for (uint32_t j = 0; j < 8; j++) {
                                 if (i0 + j >= ns) break;
                                 const uint32_t pc0 = sv[j].y > SWM_PER_FETCH ? SWM_PER_FETCH : sv[j].y;
-                                S.sst[i0 + j][lane] = sv[j].x;
-                                S.scn[i0 + j][lane] = sv[j].y;
-                                S.pc[i0 + j][lane] = pc0;
+                                S.cur[i0 + j][lane] = sv[j].x + pc0;
+                                S.end[i0 + j][lane] = sv[j].x + sv[j].y;
                                 e += pc0;
                                 npos += pc0;
                                 runs += pc0 ? 1u : 0u;
@@ -1328,8 +1332,8 @@ __global__ void __launch_bounds__(PLAN_LANE_WARPS * 32) k_plan_lanes(const uint3
 #pragma unroll
                             for (uint32_t j = 0; j < 8; j++) {
                                 const uint32_t i = i0 + j;
-                                ins[j] = i < ns && S.pc[i][lane] != S.scn[i][lane];
-                                key[j] = pos[ins[j] ? S.sst[i][lane] + S.pc[i][lane] - 1 : 0u];
+                                ins[j] = i < ns && S.cur[i][lane] != S.end[i][lane];
+                                key[j] = pos[ins[j] ? S.cur[i][lane] - 1 : 0u];
                             }
 #pragma unroll
                             for (uint32_t j = 0; j < 8; j++) {
@@ -1362,27 +1366,27 @@ __global__ void __launch_bounds__(PLAN_LANE_WARPS * 32) k_plan_lanes(const uint3
         // one refill (2261-2419), then the batch bounds
         if (hs > 0 && npos + SWM_PER_FETCH <= SWM_BATCH_POSITIONS && 1 + 2 * runs < SWM_MAX_RUNS_BLOCK) {
             const uint32_t i = S.hidx[1][lane];
-            const uint32_t st = S.sst[i][lane], cn = S.scn[i][lane];
-            uint32_t pc = S.pc[i][lane];
-            const uint32_t left = cn - pc;
+            const uint32_t en = S.end[i][lane];
+            uint32_t cu = S.cur[i][lane];
+            const uint32_t left = en - cu;
             const uint32_t get = left > SWM_PER_FETCH ? SWM_PER_FETCH : left;
-            B.ch_g[rb + rc] = st + pc;
+            B.ch_g[rb + rc] = cu;
             B.ch_meta[rb + rc] = get | (i << 8);
             rc++;
-            pc += get;
-            S.pc[i][lane] = pc;
+            cu += get;
+            S.cur[i][lane] = cu;
             e += get;
             npos += get;
             runs++;
             // seeds_heap_pop_and_insert (1936-1962): the root leaves or takes
             // the seed's next key, then sinks while q * 2 < size
             uint32_t xk, xi;
-            if (pc == cn) {
+            if (cu == en) {
                 xk = S.hloc[hs][lane];
                 xi = S.hidx[hs][lane];
                 hs--;
             } else {
-                xk = pos[st + pc - 1];
+                xk = pos[cu - 1];
                 xi = i;
             }
             uint32_t q = 1;
@@ -3734,7 +3738,7 @@ static int enqueue_ops(swm_mapper *m, cudaStream_t st, int gclass, int vmode) {
     if (rc) return rc;
     m->launches += 6;
     k_plan_list<<<grid_cap(ci, 256, 8), 256, 0, st>>>(B, m->cap_chunks, !table);
-    k_plan_lanes<<<grid_cap(ci, PLAN_LANE_WARPS * 32, 6), PLAN_LANE_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
+    k_plan_lanes<<<grid_cap(ci, PLAN_LANE_WARPS * 32, 8), PLAN_LANE_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
                                                                                          m->cap_elems);
     k_plan<<<grid_cap(ci, PLAN_WARPS * 32, 16), PLAN_WARPS * 32, 0, st>>>(ix->d_pos, B, m->cap_chunks,
                                                                           m->cap_elems);
