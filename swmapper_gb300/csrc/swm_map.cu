@@ -3332,8 +3332,8 @@ __device__ uint32_t records_seq(const MapBufs &B, uint32_t item, uint64_t cap_re
 
 // Records, groups of 32 consecutive items taken from a queue: items with few
 // candidates one thread each (records_seq, all lanes at once), the others
-// one warp each. Most of those need none of the sequential machinery: while num + 8 <=
-// SWM_MAX_CIGAR and len + 256 <= 16 SWM_MAX_CIGAR the flush tests are false,
+// one warp each. Most of those need none of the sequential machinery: while
+// num + 8 <= SWM_MAX_CIGAR and len + 256 <= 16 SWM_MAX_CIGAR the flush tests are false,
 // so when the item's passing candidates (P of them, S bytes of [NM, len,
 // text] before dedup) keep within those bounds, or (write pass) the count
 // pass found at most one record, the item is one record of every passing
