@@ -77,6 +77,10 @@ def test_bad_arguments(lib):
     assert rc == SWM_ERR_ARG
     h = C.c_void_p()
     assert lib.swm_index_open(None, 12, 0, C.byref(h)) == SWM_ERR_ARG
+    # entry points that take a handle reject a null one before any device work
+    assert lib.swm_index_serialize_mappers(None, 1) == SWM_ERR_ARG
+    assert lib.swm_index_candidate_table(None, -1, None) == SWM_ERR_ARG
+    assert lib.swm_mapper_tuning(None, None, None) == SWM_ERR_ARG
 
 
 def test_oracle_files_are_consistent(index_files):
